@@ -1,0 +1,181 @@
+/*
+ * nwcch.h - C ABI of libnwcch, a GB300 (sm_103a) implementation of the
+ * metric-dependent hot path of Customizable Contraction Hierarchies with
+ * negative arc weights: triangle (min,+) customization, the negative-cycle
+ * scan, partial re-customization and elimination-tree queries.
+ *
+ * Reference interface: python/cch_nb.py and python/cch.py of
+ * AaravG/negative-weight-cch; each entry point names the reference function
+ * (file:line) it replaces.
+ *
+ * Conventions
+ *   - Every function returns int: NWCCH_OK (0), NWCCH_SATURATED (1, see
+ *     below) or a negative NWCCH_ERR_* code.
+ *   - Vertices of the contracted graph are ranks (0 = eliminated first), as in
+ *     the reference (the upward CSR `first`/`head` is in rank space).
+ *   - Original arc weights are int32 (NWCCH_INF32 is not a valid weight).
+ *     Customized weights are stored as int32 (entry points without suffix)
+ *     or int64 (suffix _i64), with INT_MAX of the type meaning "no path".
+ *     An INF operand is tested before every addition. A finite sum outside
+ *     the storage range [INT_MIN+1, INT_MAX-1] is clamped to it and the call
+ *     returns NWCCH_SATURATED: every output is written, but clamped values
+ *     are not exact. Without a negative cycle, no customized value exceeds
+ *     n * max|w| in magnitude, so int64 storage saturates only on graphs
+ *     with a negative cycle. Query distances are int64 with NWCCH_INF64.
+ *   - Pointers named *_dev are device pointers (cudaMalloc / torch CUDA
+ *     tensors); all others are host pointers. `stream` is a cudaStream_t
+ *     (NULL = legacy default stream).
+ *   - A topology handle is immutable after creation and may be shared by
+ *     calls on different streams; its error word is shared by those calls.
+ */
+#ifndef NWCCH_H
+#define NWCCH_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define NWCCH_OK 0
+#define NWCCH_SATURATED 1       /* completed; some finite values were clamped to the storage range */
+#define NWCCH_ERR_ARG (-1)      /* invalid argument (null pointer, bad size, id or weight out of range) */
+#define NWCCH_ERR_NOMEM (-2)    /* host or device allocation failed */
+#define NWCCH_ERR_CUDA (-3)     /* a CUDA runtime call failed */
+#define NWCCH_ERR_TOPOLOGY (-4) /* arrays do not form a valid chordal upward CSR / arc map */
+#define NWCCH_ERR_TIMEOUT (-6)  /* a bounded device-side wait gave up */
+#define NWCCH_ERR_CAPACITY (-7) /* a fixed-size buffer is too small for the request */
+
+#define NWCCH_INF32 ((int32_t)0x7fffffff)
+#define NWCCH_INF64 ((int64_t)0x7fffffffffffffffLL)
+
+/* ------------------------------------------------------------------------
+ * Host-side, weight-independent preprocessing (stays on the host).
+ * Buffers returned through T** are malloc'ed; free them with nwcch_host_free.
+ * ---------------------------------------------------------------------- */
+
+void nwcch_host_free(void* p);
+
+/* Symmetric, de-duplicated neighbour lists without self-loops.
+ * Replaces cch_nb.undirected_csr (python/cch_nb.py:22-71).
+ * noff: int64[n+1] (caller-allocated); *nbr: int32[*slots] (library-allocated). */
+int nwcch_undirected_csr(int64_t n, const int64_t* off, const int32_t* tgt, int64_t* noff,
+                         int32_t** nbr, int64_t* slots);
+
+/* Nested-dissection order by inertial-flow bisection, cells of <= leaf
+ * vertices ordered by degree; rank[v] = position of v (0 = lowest).
+ * threads <= 0 uses every hardware thread.
+ * Replaces cch_nb.nested_dissection (python/cch_nb.py:336-426). */
+int nwcch_nested_dissection(int64_t n, const int64_t* noff, const int32_t* nbr, const double* x,
+                            const double* y, int64_t leaf, int threads, int32_t* rank);
+
+/* Chordal completion in rank space: first int64[n+1] and parent int32[n]
+ * (-1 = root) caller-allocated, *head int32[*m_plus] library-allocated,
+ * sorted per row. Replaces cch_nb.symbolic (python/cch_nb.py:431-481). */
+int nwcch_symbolic(int64_t n, const int64_t* noff, const int32_t* nbr, const int32_t* rank,
+                   int64_t* first, int32_t* parent, int32_t** head, int64_t* m_plus);
+
+/* Shortcut arc (-1 for a self-loop) and direction (1 = upward) of every
+ * original arc. Replaces cch_nb.edge_arcs (python/cch_nb.py:496-514). */
+int nwcch_edge_arcs(int64_t n, const int64_t* off, const int32_t* tgt, const int32_t* rank,
+                    const int64_t* first, const int32_t* head, int64_t* e_arc, int8_t* e_up);
+
+/* Unique undirected edges (u < v, sorted) of a triangle list int64[ntri*3];
+ * a helper of the synthetic graph generators (no reference counterpart). */
+int nwcch_triangle_edges(int64_t n, int64_t ntri, const int64_t* tri, int64_t** eu, int64_t** ev,
+                         int64_t* nedges);
+
+/* ------------------------------------------------------------------------
+ * Device-resident topology. The reference passes first/head/parent/e_arc/
+ * e_up to every call (python/cch_nb.py:529, 577); here they are validated,
+ * extended (tails, levels, elimination-tree depths, downward lists) and
+ * uploaded once.
+ * ---------------------------------------------------------------------- */
+
+typedef struct nwcch_topology nwcch_topology;
+
+/* first int64[n+1], head int32[m+], parent int32[n], e_arc int64[m],
+ * e_up int8[m] (host arrays, as produced by the functions above). */
+int nwcch_topology_create(int64_t n, const int64_t* first, const int32_t* head,
+                          const int32_t* parent, int64_t m, const int64_t* e_arc,
+                          const int8_t* e_up, nwcch_topology** out);
+int nwcch_topology_destroy(nwcch_topology* t);
+
+/* info[0..7] = n, m+, m, lower triangles, levels, elimination-tree depth,
+ * longest row, device bytes held by the handle. */
+int nwcch_topology_info(const nwcch_topology* t, int64_t* info, int64_t len);
+
+/* Reads and clears the error word of `t` after asynchronous calls
+ * (synchronizes `stream`). */
+int nwcch_check(nwcch_topology* t, void* stream);
+
+/* ------------------------------------------------------------------------
+ * Customization. Replaces cch_nb.customize (python/cch_nb.py:529-563) and
+ * CCH::customize (cpp/cch.cpp:437-463): base values are the minimum over
+ * parallel original arcs (self-loops skipped), then every lower triangle is
+ * relaxed. w_dev int32[m]; up_dev, dn_dev int32[m+] receive the customized
+ * weights. nwcch_customize synchronizes and reports NWCCH_SATURATED;
+ * the _async form only enqueues (status surfaces at nwcch_check).
+ * ---------------------------------------------------------------------- */
+int nwcch_customize(nwcch_topology* t, const int32_t* w_dev, int32_t* up_dev, int32_t* dn_dev,
+                    void* stream);
+int nwcch_customize_async(nwcch_topology* t, const int32_t* w_dev, int32_t* up_dev,
+                          int32_t* dn_dev, void* stream);
+/* The same with int64 storage (python/cch_nb.py:529-563). */
+int nwcch_customize_i64(nwcch_topology* t, const int32_t* w_dev, int64_t* up_dev, int64_t* dn_dev,
+                        void* stream);
+int nwcch_customize_i64_async(nwcch_topology* t, const int32_t* w_dev, int64_t* up_dev,
+                              int64_t* dn_dev, void* stream);
+
+/* Number of arcs with up + dn < 0 (Theorem 3: nonzero iff a negative cycle).
+ * Replaces cch_nb.negative_cycle_arcs (python/cch_nb.py:566-572) and
+ * CCH::negative_cycle_arcs (cpp/cch.cpp:531-536). Synchronous. */
+int nwcch_negative_cycle_arcs(nwcch_topology* t, const int32_t* up_dev, const int32_t* dn_dev,
+                              int64_t* count, void* stream);
+/* int64 storage (python/cch_nb.py:566-572). */
+int nwcch_negative_cycle_arcs_i64(nwcch_topology* t, const int64_t* up_dev, const int64_t* dn_dev,
+                                  int64_t* count, void* stream);
+
+/* Number of self-loop original arcs with a negative weight (loops never
+ * enter the contracted graph). Replaces CCH._negative_loop
+ * (python/cch.py:659-660). Synchronous. */
+int nwcch_negative_loops(nwcch_topology* t, const int32_t* w_dev, int64_t* count, void* stream);
+
+/* ------------------------------------------------------------------------
+ * Partial re-customization. Replaces CCH.update_edges (python/cch.py:349-402)
+ * together with the bookkeeping of CCH.update_created_negative_cycle
+ * (python/cch.py:666-671). edge_idx/new_w are HOST arrays of k changes
+ * (original arc ids, CSR order; the last write to an arc wins). w_dev is
+ * updated in place, up_dev/dn_dev re-customized in place.
+ * stats[0] = arcs re-evaluated, stats[1] = arcs changed, stats[2] = changed
+ * arcs with up + dn < 0. changed_dev (nullable, capacity m+) receives the
+ * changed arcs. Calls on one topology are serialized; synchronous.
+ * ---------------------------------------------------------------------- */
+int nwcch_update(nwcch_topology* t, int32_t* w_dev, int32_t* up_dev, int32_t* dn_dev,
+                 const int64_t* edge_idx, const int32_t* new_w, int64_t k, int64_t* stats,
+                 int32_t* changed_dev, void* stream);
+/* int64 storage (python/cch.py:349-402). */
+int nwcch_update_i64(nwcch_topology* t, int32_t* w_dev, int64_t* up_dev, int64_t* dn_dev,
+                     const int64_t* edge_idx, const int32_t* new_w, int64_t k, int64_t* stats,
+                     int32_t* changed_dev, void* stream);
+
+/* ------------------------------------------------------------------------
+ * Elimination-tree queries. Replaces cch_nb.query (python/cch_nb.py:577-615)
+ * and Query::run (cpp/cch.cpp:549-575), batched: dist_dev[i] = distance from
+ * rank s_rank_dev[i] to rank t_rank_dev[i] (NWCCH_INF64 if unreachable).
+ * The caller-owned scratch df/dr/mark of the reference is not needed.
+ * Synchronous.
+ * ---------------------------------------------------------------------- */
+int nwcch_query_batch(nwcch_topology* t, const int32_t* up_dev, const int32_t* dn_dev,
+                      const int32_t* s_rank_dev, const int32_t* t_rank_dev, int64_t nq,
+                      int64_t* dist_dev, void* stream);
+/* int64 storage (python/cch_nb.py:577-615). */
+int nwcch_query_batch_i64(nwcch_topology* t, const int64_t* up_dev, const int64_t* dn_dev,
+                          const int32_t* s_rank_dev, const int32_t* t_rank_dev, int64_t nq,
+                          int64_t* dist_dev, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NWCCH_H */

@@ -1,0 +1,97 @@
+// Shared device-side definitions of libnwcch.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "nwcch.h"
+
+namespace nwcch {
+
+constexpr int32_t INF32 = NWCCH_INF32;
+constexpr int64_t INF64 = NWCCH_INF64;
+
+// Bits of the per-topology device error word.
+enum ErrBits : int {
+    ERR_RANGE = 1,     // a finite (min,+) value was clamped to the storage range
+    ERR_TIMEOUT = 2,   // a bounded spin-wait gave up
+    ERR_CAPACITY = 4,  // a fixed-size buffer overflowed
+    ERR_TOPOLOGY = 8,  // an arc that chordality guarantees was not found
+    ERR_ARG = 16,      // an input value is invalid (weight equal to INF, id out of range)
+};
+
+// Storage of customized weights: INF is "no path", finite values live in
+// [LO, HI]. Sums leaving that range are clamped (saturated) and flagged.
+template <class T>
+struct Lim;
+template <>
+struct Lim<int32_t> {
+    static constexpr int32_t INF = INT32_MAX;
+    static constexpr int32_t HI = INT32_MAX - 1;
+    static constexpr int32_t LO = INT32_MIN + 1;
+};
+template <>
+struct Lim<int64_t> {
+    static constexpr int64_t INF = INT64_MAX;
+    static constexpr int64_t HI = INT64_MAX - 1;
+    static constexpr int64_t LO = INT64_MIN + 1;
+};
+
+// Candidate a + b of a (min,+) relaxation. Returns false when either side is
+// INF (no path): the INF test comes before the addition, so INF plus a
+// negative weight never looks finite.
+__device__ __forceinline__ bool splus(int32_t a, int32_t b, int32_t& out, int& err) {
+    if (a == Lim<int32_t>::INF || b == Lim<int32_t>::INF) return false;
+    const int64_t s = (int64_t)a + (int64_t)b;
+    if (s > Lim<int32_t>::HI) {
+        out = Lim<int32_t>::HI;
+        err |= ERR_RANGE;
+    } else if (s < Lim<int32_t>::LO) {
+        out = Lim<int32_t>::LO;
+        err |= ERR_RANGE;
+    } else {
+        out = (int32_t)s;
+    }
+    return true;
+}
+
+__device__ __forceinline__ bool splus(int64_t a, int64_t b, int64_t& out, int& err) {
+    if (a == Lim<int64_t>::INF || b == Lim<int64_t>::INF) return false;
+    if (b > 0 && a > Lim<int64_t>::HI - b) {
+        out = Lim<int64_t>::HI;
+        err |= ERR_RANGE;
+    } else if (b < 0 && a < Lim<int64_t>::LO - b) {
+        out = Lim<int64_t>::LO;
+        err |= ERR_RANGE;
+    } else {
+        out = a + b;
+    }
+    return true;
+}
+
+// Query labels are int64 whatever the storage; the result keeps INF64.
+template <class T>
+__device__ __forceinline__ int64_t label_plus(int64_t d, T w, int& err) {
+    if (d == INF64 || w == Lim<T>::INF) return INF64;
+    int64_t out;
+    splus(d, (int64_t)w, out, err);
+    return out;
+}
+
+// Sign of up + dn without overflow (the negative-cycle test).
+template <class T>
+__device__ __forceinline__ bool negative_pair(T u, T v) {
+    if (u == Lim<T>::INF || v == Lim<T>::INF) return false;
+    int64_t s;
+    int e = 0;
+    splus((int64_t)u, (int64_t)v, s, e);
+    return s < 0;
+}
+
+#define NWCCH_CUDA_TRY(expr)                            \
+    do {                                                \
+        cudaError_t _e = (expr);                        \
+        if (_e != cudaSuccess) return NWCCH_ERR_CUDA;   \
+    } while (0)
+
+}  // namespace nwcch

@@ -1,0 +1,128 @@
+// Plain elimination-tree query: one warp per (s, t) pair.
+//
+// The reference (python/cch_nb.py:577-615 = cpp/cch.cpp:549-575) relaxes the
+// upward arcs of every ancestor of s in increasing rank (forward labels with
+// up weights), then of every ancestor of t (backward labels with dn weights),
+// and takes min(df + dr) over the ancestors the two chains share. Arcs out of
+// an ancestor only reach ancestors, so labels are indexed by elimination-tree
+// depth along one chain: the label of ancestor v of s lives at
+// depth(s) - depth(v). Lanes relax the arcs of one row in parallel (distinct
+// heads, no conflicts); the warp walks the chain in order.
+
+#include <algorithm>
+
+#include "common.cuh"
+#include "topology.h"
+
+namespace nwcch {
+
+template <class T>
+__global__ void __launch_bounds__(128) k_query_plain(DevTopo D, const T* __restrict__ up, const T* __restrict__ dn,
+                                                     const int32_t* __restrict__ s_rank,
+                                                     const int32_t* __restrict__ t_rank, int64_t nq,
+                                                     int64_t* __restrict__ dist, int64_t* __restrict__ scratch,
+                                                     int* __restrict__ err) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const int64_t Dp = D.max_depth + 1;
+    int64_t* F = scratch + warp * (2 * Dp + (Dp + 1) / 2 + 1);
+    int64_t* R = F + Dp;
+    int32_t* chain = reinterpret_cast<int32_t*>(R + Dp);
+    int e = 0;
+    for (int64_t q = warp; q < nq; q += nwarps) {
+        const int32_t s = s_rank[q], t = t_rank[q];
+        if (s < 0 || s >= D.n || t < 0 || t >= D.n) {
+            if (lane == 0) dist[q] = INF64;
+            e |= ERR_ARG;
+            continue;
+        }
+        const int32_t ds = D.depth[s], dt = D.depth[t];
+        for (int i = lane; i <= ds; i += 32) F[i] = INF64;
+        for (int i = lane; i <= dt; i += 32) R[i] = INF64;
+        __syncwarp();
+        if (lane == 0) {
+            F[0] = 0;
+            R[0] = 0;
+        }
+        __syncwarp();
+        int i = 0;
+        for (int32_t x = s; x >= 0; x = D.parent[x], i++) {
+            if (lane == 0) chain[i] = x;
+            const int64_t fx = F[i];
+            if (fx != INF64) {
+                for (int64_t a = D.first[x] + lane; a < D.first[x + 1]; a += 32) {
+                    const int64_t c = label_plus(fx, up[a], e);
+                    int64_t* slot = &F[ds - D.hdep[a]];
+                    if (c < *slot) *slot = c;
+                }
+            }
+            __syncwarp();
+        }
+        int64_t best = INF64;
+        i = 0;
+        for (int32_t x = t; x >= 0; x = D.parent[x], i++) {
+            const int64_t rx = R[i];
+            if (rx != INF64) {
+                const int32_t dx = dt - i;  // depth of x
+                if (dx <= ds && chain[ds - dx] == x) {
+                    const int64_t fx = F[ds - dx];
+                    if (fx != INF64) {
+                        int64_t v;
+                        splus(rx, fx, v, e);
+                        best = min(best, v);
+                    }
+                }
+                for (int64_t a = D.first[x] + lane; a < D.first[x + 1]; a += 32) {
+                    const int64_t c = label_plus(rx, dn[a], e);
+                    int64_t* slot = &R[dt - D.hdep[a]];
+                    if (c < *slot) *slot = c;
+                }
+            }
+            __syncwarp();
+        }
+        if (lane == 0) dist[q] = best;
+        __syncwarp();
+    }
+    if (e) atomicOr(err, e);
+}
+
+template <class T>
+int query_plain(nwcch_topology* t, const T* up, const T* dn, const int32_t* s_rank, const int32_t* t_rank, int64_t nq,
+                int64_t* dist, cudaStream_t s) {
+    const int64_t Dp = t->d.max_depth + 1;
+    const int64_t per_warp = 2 * Dp + (Dp + 1) / 2 + 1;  // int64 words: F, R, chain (int32)
+    const int64_t warps = std::min<int64_t>(nq, 152 * 32);
+    const int block = 128;
+    const int64_t blocks = (warps * 32 + block - 1) / block;
+    void* scratch = nullptr;
+    NWCCH_CUDA_TRY(cudaMallocAsync(&scratch, (size_t)(blocks * (block / 32)) * per_warp * sizeof(int64_t), s));
+    k_query_plain<T><<<(unsigned)blocks, block, 0, s>>>(t->d, up, dn, s_rank, t_rank, nq, dist, (int64_t*)scratch,
+                                                       t->err);
+    const cudaError_t launch = cudaGetLastError();
+    NWCCH_CUDA_TRY(cudaFreeAsync(scratch, s));
+    NWCCH_CUDA_TRY(launch);
+    return consume_error(t, s);
+}
+
+}  // namespace nwcch
+
+using namespace nwcch;
+
+extern "C" int nwcch_query_batch(nwcch_topology* t, const int32_t* up_dev, const int32_t* dn_dev,
+                                 const int32_t* s_rank_dev, const int32_t* t_rank_dev, int64_t nq,
+                                 int64_t* dist_dev, void* stream) {
+    if (!t || nq < 0 || (nq > 0 && (!up_dev || !dn_dev || !s_rank_dev || !t_rank_dev || !dist_dev)))
+        return NWCCH_ERR_ARG;
+    if (nq == 0) return NWCCH_OK;
+    return query_plain<int32_t>(t, up_dev, dn_dev, s_rank_dev, t_rank_dev, nq, dist_dev, (cudaStream_t)stream);
+}
+
+extern "C" int nwcch_query_batch_i64(nwcch_topology* t, const int64_t* up_dev, const int64_t* dn_dev,
+                                     const int32_t* s_rank_dev, const int32_t* t_rank_dev, int64_t nq,
+                                     int64_t* dist_dev, void* stream) {
+    if (!t || nq < 0 || (nq > 0 && (!up_dev || !dn_dev || !s_rank_dev || !t_rank_dev || !dist_dev)))
+        return NWCCH_ERR_ARG;
+    if (nq == 0) return NWCCH_OK;
+    return query_plain<int64_t>(t, up_dev, dn_dev, s_rank_dev, t_rank_dev, nq, dist_dev, (cudaStream_t)stream);
+}

@@ -1,0 +1,229 @@
+// Topology handle: validates the upward CSR produced by the host-side
+// preprocessing, derives the structures the kernels need (tails, levels,
+// elimination-tree depths, downward lists, arc -> original-arc index) and
+// uploads everything once. Customization, scans, updates and queries for any
+// number of metrics then run against this resident copy.
+
+#include <algorithm>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "common.cuh"
+#include "topology.h"
+
+namespace nwcch {
+
+namespace {
+
+template <class T>
+int upload(nwcch_topology* t, const T* src, size_t count, T** dst) {
+    void* p = nullptr;
+    const size_t bytes = std::max<size_t>(1, count) * sizeof(T);
+    if (cudaMalloc(&p, bytes) != cudaSuccess) return NWCCH_ERR_NOMEM;
+    t->allocations.push_back(p);
+    t->device_bytes += bytes;
+    if (count && cudaMemcpy(p, src, count * sizeof(T), cudaMemcpyHostToDevice) != cudaSuccess)
+        return NWCCH_ERR_CUDA;
+    *dst = static_cast<T*>(p);
+    return NWCCH_OK;
+}
+
+void release(nwcch_topology* t) {
+    if (t->free_plans) t->free_plans(t);
+    for (void* p : t->allocations) cudaFree(p);
+    t->allocations.clear();
+}
+
+}  // namespace
+
+int consume_error(nwcch_topology* t, cudaStream_t stream) {
+    int h = 0;
+    NWCCH_CUDA_TRY(cudaMemcpyAsync(&h, t->err, sizeof(int), cudaMemcpyDeviceToHost, stream));
+    NWCCH_CUDA_TRY(cudaStreamSynchronize(stream));
+    if (h) NWCCH_CUDA_TRY(cudaMemsetAsync(t->err, 0, sizeof(int), stream));
+    if (h & ERR_TIMEOUT) return NWCCH_ERR_TIMEOUT;
+    if (h & ERR_CAPACITY) return NWCCH_ERR_CAPACITY;
+    if (h & ERR_TOPOLOGY) return NWCCH_ERR_TOPOLOGY;
+    if (h & ERR_ARG) return NWCCH_ERR_ARG;
+    if (h & ERR_RANGE) return NWCCH_SATURATED;
+    return NWCCH_OK;
+}
+
+}  // namespace nwcch
+
+using namespace nwcch;
+
+extern "C" int nwcch_topology_create(int64_t n, const int64_t* first, const int32_t* head,
+                                     const int32_t* parent, int64_t m, const int64_t* e_arc,
+                                     const int8_t* e_up, nwcch_topology** out) {
+    if (!out || n < 1 || n > INT32_MAX || !first || !parent || m < 0 || (m > 0 && (!e_arc || !e_up)))
+        return NWCCH_ERR_ARG;
+    *out = nullptr;
+    const int64_t mp = first[n];
+    if (first[0] != 0 || mp < 0 || mp >= INT32_MAX || (mp > 0 && !head) || m >= INT32_MAX)
+        return NWCCH_ERR_TOPOLOGY;
+    // rows: strictly increasing heads above the tail; parent = lowest head
+    for (int64_t x = 0; x < n; x++) {
+        if (first[x + 1] < first[x]) return NWCCH_ERR_TOPOLOGY;
+        int64_t prev = x;
+        for (int64_t a = first[x]; a < first[x + 1]; a++) {
+            if (head[a] <= prev || head[a] >= n) return NWCCH_ERR_TOPOLOGY;
+            prev = head[a];
+        }
+        const int32_t p = first[x + 1] > first[x] ? head[first[x]] : -1;
+        if (parent[x] != p) return NWCCH_ERR_TOPOLOGY;
+    }
+    for (int64_t k = 0; k < m; k++)
+        if (e_arc[k] < -1 || e_arc[k] >= mp) return NWCCH_ERR_TOPOLOGY;
+
+    auto* t = new (std::nothrow) nwcch_topology();
+    if (!t) return NWCCH_ERR_NOMEM;
+    int rc = NWCCH_OK;
+    do {
+        std::vector<int32_t> tail(mp), depth(n, 0), hdep(mp), lvl(n, 0);
+        int64_t tri = 0;
+        int32_t maxdeg = 0;
+        for (int64_t x = 0; x < n; x++) {
+            const int64_t d = first[x + 1] - first[x];
+            tri += d * (d - 1) / 2;
+            maxdeg = std::max<int32_t>(maxdeg, (int32_t)d);
+            for (int64_t a = first[x]; a < first[x + 1]; a++) {
+                tail[a] = (int32_t)x;
+                lvl[head[a]] = std::max(lvl[head[a]], lvl[x] + 1);
+            }
+        }
+        int32_t maxd = 0;
+        for (int64_t x = n - 1; x >= 0; x--)
+            if (parent[x] >= 0) {
+                depth[x] = depth[parent[x]] + 1;
+                maxd = std::max(maxd, depth[x]);
+            }
+        for (int64_t a = 0; a < mp; a++) hdep[a] = depth[head[a]];
+        // downward lists, ascending in the tail (arc ids grow with the tail)
+        std::vector<int64_t> doff(n + 1, 0);
+        for (int64_t a = 0; a < mp; a++) doff[head[a] + 1]++;
+        for (int64_t v = 0; v < n; v++) doff[v + 1] += doff[v];
+        std::vector<int32_t> darc(mp);
+        {
+            std::vector<int64_t> fill(doff.begin(), doff.end() - 1);
+            for (int64_t a = 0; a < mp; a++) darc[fill[head[a]]++] = (int32_t)a;
+        }
+        // levels: vertices bucketed by level, stable in rank
+        int32_t L = 0;
+        for (int64_t x = 0; x < n; x++) L = std::max(L, lvl[x] + 1);
+        t->levels = L;
+        t->level_off.assign(L + 1, 0);
+        for (int64_t x = 0; x < n; x++) t->level_off[lvl[x] + 1]++;
+        for (int32_t l = 0; l < L; l++) t->level_off[l + 1] += t->level_off[l];
+        std::vector<int32_t> lverts(n);
+        t->level_maxdeg.assign(L, 0);
+        t->level_tri.assign(L, 0);
+        t->level_arc_off.assign(L + 1, 0);
+        {
+            std::vector<int64_t> fill(t->level_off.begin(), t->level_off.end() - 1);
+            for (int64_t x = 0; x < n; x++) {
+                const int32_t l = lvl[x];
+                lverts[fill[l]++] = (int32_t)x;
+                t->level_maxdeg[l] = std::max<int32_t>(t->level_maxdeg[l], (int32_t)(first[x + 1] - first[x]));
+                t->level_arc_off[l + 1] += first[x + 1] - first[x];
+            }
+        }
+        for (int32_t l = 0; l < L; l++) t->level_arc_off[l + 1] += t->level_arc_off[l];
+        for (int64_t a = 0; a < mp; a++) {
+            const int64_t x = tail[a];
+            t->level_tri[lvl[head[a]]] += first[x + 1] - a - 1;  // pull work lands on the head's level
+        }
+        // original arcs mapped onto each shortcut arc, and the self-loops
+        std::vector<int64_t> aeoff(mp + 1, 0);
+        std::vector<int32_t> loops;
+        for (int64_t k = 0; k < m; k++) {
+            if (e_arc[k] >= 0) aeoff[e_arc[k] + 1]++;
+            else loops.push_back((int32_t)k);
+        }
+        for (int64_t a = 0; a < mp; a++) aeoff[a + 1] += aeoff[a];
+        std::vector<int32_t> aeidx(aeoff[mp]);
+        {
+            std::vector<int64_t> fill(aeoff.begin(), aeoff.end() - 1);
+            for (int64_t k = 0; k < m; k++)
+                if (e_arc[k] >= 0) aeidx[fill[e_arc[k]]++] = (int32_t)k;
+        }
+        t->triangles = tri;
+        t->max_deg = maxdeg;
+        t->nloops = (int64_t)loops.size();
+        DevTopo& d = t->d;
+        d.n = n;
+        d.m_plus = mp;
+        d.m = m;
+        d.max_depth = maxd;
+        int64_t* p64;
+        int32_t* p32;
+        int8_t* p8;
+        if ((rc = upload(t, first, n + 1, &p64))) break;
+        d.first = p64;
+        if ((rc = upload(t, head, mp, &p32))) break;
+        d.head = p32;
+        if ((rc = upload(t, parent, n, &p32))) break;
+        d.parent = p32;
+        if ((rc = upload(t, depth.data(), n, &p32))) break;
+        d.depth = p32;
+        if ((rc = upload(t, hdep.data(), mp, &p32))) break;
+        d.hdep = p32;
+        if ((rc = upload(t, tail.data(), mp, &p32))) break;
+        d.tail = p32;
+        if ((rc = upload(t, doff.data(), n + 1, &p64))) break;
+        d.doff = p64;
+        if ((rc = upload(t, darc.data(), mp, &p32))) break;
+        d.darc = p32;
+        if ((rc = upload(t, lvl.data(), n, &p32))) break;
+        d.vlevel = p32;
+        if ((rc = upload(t, e_arc, m, &p64))) break;
+        d.e_arc = p64;
+        if ((rc = upload(t, e_up, m, &p8))) break;
+        d.e_up = p8;
+        if ((rc = upload(t, aeoff.data(), mp + 1, &p64))) break;
+        d.aeoff = p64;
+        if ((rc = upload(t, aeidx.data(), aeidx.size(), &p32))) break;
+        d.aeidx = p32;
+        if ((rc = upload(t, loops.data(), loops.size(), &p32))) break;
+        t->loops = p32;
+        if ((rc = upload(t, lverts.data(), n, &p32))) break;
+        t->level_verts = p32;
+        if ((rc = upload(t, t->level_arc_off.data(), t->level_arc_off.size(), &p64))) break;
+        t->d_level_arc_off = p64;
+        const int zero = 0;
+        if ((rc = upload(t, &zero, 1, &p32))) break;
+        t->err = reinterpret_cast<int*>(p32);
+        const int64_t zeros[16] = {0};
+        if ((rc = upload(t, zeros, 16, &p64))) break;
+        t->counters = reinterpret_cast<unsigned long long*>(p64);
+    } while (false);
+    if (rc != NWCCH_OK) {
+        release(t);
+        delete t;
+        return rc;
+    }
+    *out = t;
+    return NWCCH_OK;
+}
+
+extern "C" int nwcch_topology_destroy(nwcch_topology* t) {
+    if (!t) return NWCCH_ERR_ARG;
+    cudaDeviceSynchronize();
+    release(t);
+    delete t;
+    return NWCCH_OK;
+}
+
+extern "C" int nwcch_topology_info(const nwcch_topology* t, int64_t* info, int64_t len) {
+    if (!t || !info || len < 8) return NWCCH_ERR_ARG;
+    info[0] = t->d.n;
+    info[1] = t->d.m_plus;
+    info[2] = t->d.m;
+    info[3] = t->triangles;
+    info[4] = t->levels;
+    info[5] = t->d.max_depth;
+    info[6] = t->max_deg;
+    info[7] = (int64_t)t->device_bytes;
+    return NWCCH_OK;
+}

@@ -1,0 +1,62 @@
+// Device-resident topology handle of libnwcch (internal layout).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <mutex>
+#include <vector>
+
+#include "nwcch.h"
+
+namespace nwcch {
+
+// Read-only views passed to kernels by value.
+struct DevTopo {
+    int64_t n, m_plus, m;
+    int32_t max_depth;
+    const int64_t* first;   // [n+1] upward CSR offsets (rank space)
+    const int32_t* head;    // [m+]  upper endpoint of every arc, sorted per row
+    const int32_t* parent;  // [n]   elimination-tree parent (-1 = root)
+    const int32_t* depth;   // [n]   elimination-tree depth (root 0)
+    const int32_t* hdep;    // [m+]  depth of head[a]
+    const int32_t* tail;    // [m+]  lower endpoint of every arc
+    const int64_t* doff;    // [n+1] downward lists: arcs (x,y) grouped by y ...
+    const int32_t* darc;    // [m+]  ... ascending in x
+    const int32_t* vlevel;  // [n]   level: 1 + max level of the lower neighbours
+    const int64_t* e_arc;   // [m]   shortcut arc of every original arc (-1 = self-loop)
+    const int8_t* e_up;     // [m]   1 if the original arc goes up in rank
+    const int64_t* aeoff;   // [m+ + 1] original arcs mapped onto each shortcut arc ...
+    const int32_t* aeidx;   // [...]     ... as original arc ids
+};
+
+}  // namespace nwcch
+
+struct nwcch_topology {
+    nwcch::DevTopo d{};
+    int64_t triangles = 0;
+    int32_t levels = 0;
+    int32_t max_deg = 0;
+    int64_t nloops = 0;
+    int32_t* loops = nullptr;                 // device: original arcs that are self-loops
+    std::vector<int64_t> level_off;           // [levels+1] into level_verts
+    std::vector<int32_t> level_maxdeg;        // longest row of each level
+    std::vector<int64_t> level_tri;           // pull triangles of each level
+    int32_t* level_verts = nullptr;           // device: vertices sorted by (level, rank)
+    std::vector<int64_t> level_arc_off;       // [levels+1]: arcs bucketed by tail level
+    int64_t* d_level_arc_off = nullptr;       // device copy
+    int* err = nullptr;                       // device error word
+    unsigned long long* counters = nullptr;   // device: 16 scratch counters (scan results)
+    std::vector<void*> allocations;           // every cudaMalloc of this handle
+    size_t device_bytes = 0;
+    std::mutex mu;                            // serialises lazily built plans
+    void* plans = nullptr;                    // owned by the modules that build plans
+    void (*free_plans)(nwcch_topology*) = nullptr;
+};
+
+namespace nwcch {
+
+// Reads and clears the device error word (synchronizes `stream`).
+int consume_error(nwcch_topology* t, cudaStream_t stream);
+
+}  // namespace nwcch

@@ -1,0 +1,260 @@
+"""Device-resident topology and metrics over the libnwcch C ABI.
+
+PyTorch provides the device buffers and the current CUDA stream; every kernel
+is libnwcch's own sm_103a code. There is no CPU fallback: without a CUDA
+device (or without the built library) every call raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import warnings
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _lib
+
+P, I64, I32 = C.c_void_p, C.c_int64, C.c_int32
+PP = C.POINTER(C.c_void_p)
+PI64 = C.POINTER(C.c_int64)
+
+for _name, _args in {
+    "nwcch_topology_create": [I64, P, P, P, I64, P, P, PP],
+    "nwcch_topology_destroy": [P],
+    "nwcch_topology_info": [P, P, I64],
+    "nwcch_check": [P, P],
+    "nwcch_customize": [P, P, P, P, P],
+    "nwcch_customize_async": [P, P, P, P, P],
+    "nwcch_customize_i64": [P, P, P, P, P],
+    "nwcch_customize_i64_async": [P, P, P, P, P],
+    "nwcch_negative_cycle_arcs": [P, P, P, PI64, P],
+    "nwcch_negative_cycle_arcs_i64": [P, P, P, PI64, P],
+    "nwcch_negative_loops": [P, P, PI64, P],
+    "nwcch_update": [P, P, P, P, P, P, I64, P, P, P],
+    "nwcch_update_i64": [P, P, P, P, P, P, I64, P, P, P],
+    "nwcch_query_batch": [P, P, P, P, P, I64, P, P],
+    "nwcch_query_batch_i64": [P, P, P, P, P, I64, P, P],
+}.items():
+    _lib.register(_name, _args)
+
+SATURATED = 1
+
+
+class SaturationWarning(RuntimeWarning):
+    """Some customized values were clamped to the storage range."""
+
+
+def _torch():
+    import torch
+    if not torch.cuda.is_available():
+        raise RuntimeError("nwcch device calls need a CUDA device (no CPU fallback)")
+    return torch
+
+
+def _stream(torch):
+    return C.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def _status(code: int, where: str) -> bool:
+    """True if the call saturated; raises on errors."""
+    if code == SATURATED:
+        return True
+    _lib.check(code, where)
+    return False
+
+
+def parent_from_rows(first, head):
+    """parent[x] = lowest upper neighbour of x (first entry of its sorted row)."""
+    first = np.asarray(first, np.int64)
+    n = first.size - 1
+    deg = np.diff(first)
+    parent = np.full(n, -1, np.int64)
+    has = deg > 0
+    parent[has] = np.asarray(head)[first[:-1][has]]
+    return parent
+
+
+@dataclass
+class Metric:
+    """One customized metric resident on the device."""
+    topo: "DeviceTopology"
+    w: object        # torch int32 [m], current original weights
+    up: object       # torch int32/int64 [m+]
+    dn: object
+    saturated: bool = False
+    last_changed: object = None
+    stats: dict = field(default_factory=dict)
+
+    @property
+    def storage(self) -> str:
+        return "int64" if self.up.element_size() == 8 else "int32"
+
+    def to_numpy(self):
+        """(up, dn) as int64 numpy arrays with INT64_MAX for "no path"."""
+        inf_in = _lib.INF32 if self.storage == "int32" else _lib.INF64
+        out = []
+        for t in (self.up, self.dn):
+            a = t.cpu().numpy().astype(np.int64)
+            a[a == inf_in] = _lib.INF64
+            out.append(a)
+        return tuple(out)
+
+    def to_reference(self):
+        """(upw, dnw) in the reference's convention: float64 with inf."""
+        out = []
+        for a in self.to_numpy():
+            f = a.astype(np.float64)
+            f[a == _lib.INF64] = np.inf
+            out.append(f)
+        return tuple(out)
+
+
+class DeviceTopology:
+    """Validated, extended and uploaded contracted graph (one handle)."""
+
+    def __init__(self, n, first, head, parent, e_arc, e_up):
+        self._torch = _torch()
+        lib = _lib.lib()
+        self.n = int(n)
+        first = np.ascontiguousarray(first, np.int64)
+        head = np.ascontiguousarray(head, np.int32)
+        parent = np.ascontiguousarray(parent if parent is not None else parent_from_rows(first, head), np.int32)
+        e_arc = np.ascontiguousarray(e_arc, np.int64)
+        e_up = np.ascontiguousarray(e_up, np.int8)
+        h = C.c_void_p()
+        self._torch.cuda.init()
+        _lib.check(lib.nwcch_topology_create(self.n, _lib.ptr(first), _lib.ptr(head), _lib.ptr(parent), e_arc.size,
+                                             _lib.ptr(e_arc), _lib.ptr(e_up), C.byref(h)), "topology_create")
+        self._h = h
+        info = np.zeros(8, np.int64)
+        _lib.check(lib.nwcch_topology_info(h, _lib.ptr(info), 8), "topology_info")
+        (self.n, self.m_plus, self.m, self.triangles, self.levels, self.depth, self.max_row,
+         self.device_bytes) = (int(v) for v in info)
+
+    @classmethod
+    def from_dict(cls, t: dict) -> "DeviceTopology":
+        return cls(t["n"], t["first"], t["head"], t.get("parent"), t["e_arc"], t["e_up"])
+
+    @property
+    def handle(self):
+        if self._h is None:
+            raise RuntimeError("topology is closed")
+        return self._h
+
+    def close(self):
+        if getattr(self, "_h", None) is not None:
+            _lib.lib().nwcch_topology_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ------------------------------------------------------------ helpers
+    def weights(self, w):
+        """int32 device tensor of original weights (copied from host if needed)."""
+        torch = self._torch
+        if isinstance(w, torch.Tensor):
+            t = w.to(device="cuda", dtype=torch.int32)
+        else:
+            a = np.asarray(w)
+            if a.dtype.kind == "f":
+                if not np.all(np.isfinite(a)) or not np.array_equal(a, np.rint(a)):
+                    raise ValueError("weights must be integral")
+            a = a.astype(np.int64)
+            if a.size and (a.max() >= _lib.INF32 or a.min() < -_lib.INF32):
+                raise ValueError("weights must fit int32 (and differ from INT32_MAX)")
+            t = torch.from_numpy(a.astype(np.int32)).to("cuda")
+        if t.numel() != self.m:
+            raise ValueError(f"expected {self.m} weights, got {t.numel()}")
+        return t.contiguous()
+
+    # ------------------------------------------------------------ customization
+    def customize(self, w, storage: str = "int32", out: Metric | None = None, sync: bool = True) -> Metric:
+        torch = self._torch
+        lib = _lib.lib()
+        wt = self.weights(w)
+        dt = {"int32": torch.int32, "int64": torch.int64}[storage]
+        if out is not None and out.up.dtype == dt:
+            up, dn = out.up, out.dn
+        else:
+            up = torch.empty(self.m_plus, dtype=dt, device="cuda")
+            dn = torch.empty(self.m_plus, dtype=dt, device="cuda")
+        fn = {("int32", True): lib.nwcch_customize, ("int32", False): lib.nwcch_customize_async,
+              ("int64", True): lib.nwcch_customize_i64, ("int64", False): lib.nwcch_customize_i64_async}[storage, sync]
+        sat = _status(fn(self.handle, wt.data_ptr(), up.data_ptr(), dn.data_ptr(), _stream(torch)), "customize")
+        m = Metric(self, wt, up, dn, saturated=sat)
+        if sat:
+            warnings.warn(f"customization ({storage}) saturated: some values left the storage range",
+                          SaturationWarning, stacklevel=2)
+        return m
+
+    def check(self) -> bool:
+        """Status of asynchronous calls since the last check (True = saturated)."""
+        return _status(_lib.lib().nwcch_check(self.handle, _stream(self._torch)), "check")
+
+    def negative_cycle_arcs(self, m: Metric) -> int:
+        lib = _lib.lib()
+        fn = lib.nwcch_negative_cycle_arcs if m.storage == "int32" else lib.nwcch_negative_cycle_arcs_i64
+        c = C.c_int64()
+        _lib.check(fn(self.handle, m.up.data_ptr(), m.dn.data_ptr(), C.byref(c), _stream(self._torch)),
+                   "negative_cycle_arcs")
+        return int(c.value)
+
+    def negative_loops(self, m: Metric) -> int:
+        c = C.c_int64()
+        _lib.check(_lib.lib().nwcch_negative_loops(self.handle, m.w.data_ptr(), C.byref(c), _stream(self._torch)),
+                   "negative_loops")
+        return int(c.value)
+
+    # ------------------------------------------------------------ update
+    def update(self, m: Metric, edge_idx, new_w):
+        """Partial re-customization in place (python/cch.py:349-402).
+        Returns the number of arcs re-evaluated."""
+        torch = self._torch
+        lib = _lib.lib()
+        idx = np.ascontiguousarray(edge_idx, np.int64)
+        val = np.asarray(new_w)
+        if val.dtype.kind == "f" and not np.array_equal(val, np.rint(val)):
+            raise ValueError("weights must be integral")
+        val = np.ascontiguousarray(val, np.int64)
+        if val.size and (val.max() >= _lib.INF32 or val.min() < -_lib.INF32):
+            raise ValueError("weights must fit int32")
+        val = val.astype(np.int32)
+        stats = np.zeros(3, np.int64)
+        changed = torch.empty(max(self.m_plus, 1), dtype=torch.int32, device="cuda")
+        fn = lib.nwcch_update if m.storage == "int32" else lib.nwcch_update_i64
+        sat = _status(fn(self.handle, m.w.data_ptr(), m.up.data_ptr(), m.dn.data_ptr(), _lib.ptr(idx), _lib.ptr(val),
+                         idx.size, _lib.ptr(stats), changed.data_ptr(), _stream(torch)), "update")
+        m.saturated = m.saturated or sat
+        m.last_changed = changed[:int(stats[1])]
+        m.stats = dict(evaluated=int(stats[0]), changed=int(stats[1]), changed_negative=int(stats[2]),
+                       saturated=sat)
+        return int(stats[0])
+
+    # ------------------------------------------------------------ queries
+    def query_batch(self, m: Metric, s_rank, t_rank):
+        """int64 device tensor of distances (INT64_MAX = unreachable)."""
+        torch = self._torch
+        lib = _lib.lib()
+        s = torch.as_tensor(np.asarray(s_rank) if not isinstance(s_rank, torch.Tensor) else s_rank)
+        t = torch.as_tensor(np.asarray(t_rank) if not isinstance(t_rank, torch.Tensor) else t_rank)
+        s = s.to(device="cuda", dtype=torch.int32).contiguous()
+        t = t.to(device="cuda", dtype=torch.int32).contiguous()
+        if s.numel() != t.numel():
+            raise ValueError("s and t differ in length")
+        out = torch.empty(s.numel(), dtype=torch.int64, device="cuda")
+        fn = lib.nwcch_query_batch if m.storage == "int32" else lib.nwcch_query_batch_i64
+        _status(fn(self.handle, m.up.data_ptr(), m.dn.data_ptr(), s.data_ptr(), t.data_ptr(), s.numel(),
+                   out.data_ptr(), _stream(torch)), "query_batch")
+        return out
+
+
+def distances_to_float(d) -> np.ndarray:
+    """int64 distances (INT64_MAX = unreachable) -> float64 with inf."""
+    a = d.cpu().numpy() if hasattr(d, "cpu") else np.asarray(d)
+    f = a.astype(np.float64)
+    f[a == _lib.INF64] = np.inf
+    return f

@@ -1,0 +1,70 @@
+/*
+ * CPU oracle for the metric-dependent CCH hot path - TEST INFRASTRUCTURE ONLY.
+ *
+ * A plain-C restatement of the reference algorithms (AaravG/negative-weight-
+ * cch), each function citing the reference lines it follows, in exact integer
+ * arithmetic: int32 arc weights, int64 customized values and distances, and
+ * ORC_INF = INT64_MAX for "no path" (an INF operand is tested before every
+ * addition). On integer weights the reference's float64 values are exact
+ * integers (below 2^53), so equality with this oracle is bit-exact parity.
+ *
+ * Only tests, the smoke check and the benchmark's CPU-baseline / reference
+ * legs may load this library; the product never does.
+ *
+ * Pinning: tests/test_oracle.py checks every function against golden vectors
+ * produced by the reference's own code (tests/golden/make_golden.py).
+ */
+#ifndef NWCCH_ORACLE_H
+#define NWCCH_ORACLE_H
+
+#include <stdint.h>
+
+#define ORC_INF INT64_MAX
+
+/* python/cch_nb.py:529-563 (= cpp/cch.cpp:437-463): base values from the
+ * original arcs, then lower triangles (x; y, z) for x ascending. */
+void orc_customize(int64_t n, const int64_t* first, const int32_t* head, int64_t m, const int64_t* e_arc,
+                   const int8_t* e_up, const int32_t* w, int64_t* up, int64_t* dn);
+
+/* cpp/cch.cpp:468-529: vertices bucketed by level, each level in parallel
+ * with OpenMP (threads <= 0: all) and an atomic minimum. Same result as
+ * orc_customize. Returns the number of levels. */
+int64_t orc_customize_parallel(int64_t n, const int64_t* first, const int32_t* head, int64_t m,
+                               const int64_t* e_arc, const int8_t* e_up, const int32_t* w, int64_t* up,
+                               int64_t* dn, int threads);
+
+/* python/cch_nb.py:566-572: arcs with up + dn < 0. */
+int64_t orc_negative_cycle_arcs(int64_t m_plus, const int64_t* up, const int64_t* dn);
+
+/* python/cch_nb.py:577-615: elimination-tree query with caller scratch
+ * df/dr (int64[n]) and mark (int64[n]); q is a fresh query id. */
+int64_t orc_query(int64_t s_rank, int64_t t_rank, const int64_t* first, const int32_t* head,
+                  const int64_t* parent, const int64_t* up, const int64_t* dn, int64_t* df, int64_t* dr,
+                  int64_t* mark, int64_t q);
+
+/* Batch of orc_query over rank pairs; threads <= 0 uses all cores. */
+void orc_query_batch(int64_t n, const int64_t* first, const int32_t* head, const int64_t* parent,
+                     const int64_t* up, const int64_t* dn, int64_t nq, const int64_t* s_rank,
+                     const int64_t* t_rank, int64_t* out, int threads);
+
+/* python/cch.py:349-402: partial re-customization. w (current weights, int32[m])
+ * is updated in place by the k changes (last write wins), up/dn re-customized
+ * in place. stats[0] = arcs evaluated, stats[1] = arcs changed,
+ * stats[2] = changed arcs with up + dn < 0 (python/cch.py:666-671).
+ * changed (nullable, capacity m+) receives the changed arcs in pop order. */
+void orc_update(int64_t n, const int64_t* first, const int32_t* head, int64_t m, const int64_t* e_arc,
+                const int8_t* e_up, int32_t* w, int64_t* up, int64_t* dn, int64_t k, const int64_t* edge_idx,
+                const int32_t* new_w, int64_t* stats, int64_t* changed);
+
+/* python/search.py:8-29 (queue-based Bellman-Ford) on the original graph,
+ * single source, original vertex ids. Returns 1 if a negative cycle is
+ * reachable from s (a vertex relaxed n times), else 0; dist int64[n]. */
+int orc_bellman_ford(int64_t n, const int64_t* off, const int32_t* tgt, const int32_t* w, int64_t s,
+                     int64_t* dist);
+
+/* Negative-cycle test of the whole graph (python/preprocess.py:13-59 role:
+ * virtual source with 0-arcs to every vertex). Returns 1 if a negative cycle
+ * exists. */
+int orc_has_negative_cycle(int64_t n, const int64_t* off, const int32_t* tgt, const int32_t* w);
+
+#endif

@@ -1,0 +1,194 @@
+"""GPU parity: the sm_103a kernels (through the C ABI) against the golden
+vectors of the reference and against the pinned CPU oracle. Integer work, so
+every comparison is exact."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from conftest import family_case, i32_to_i64, load_golden
+
+pytestmark = pytest.mark.gpu
+INF = np.iinfo(np.int64).max
+
+
+def dev_topo(z, n=None):
+    from nwcch.device import DeviceTopology
+    return DeviceTopology(int(n if n is not None else z["n"]), z["first"], z["head"], z["parent"], z["e_arc"],
+                          z["e_up"])
+
+
+def gpu_ranks(z, key):
+    return z["rank"][z[key]]
+
+
+@pytest.mark.parametrize("storage", ["int32", "int64"])
+def test_techniques_union(gpu, storage):
+    z = load_golden("techniques.npz")
+    T = dev_topo(z)
+    m = T.customize(z["w"], storage)
+    up, dn = m.to_numpy()
+    assert np.array_equal(up, i32_to_i64(z["up"])) and np.array_equal(dn, i32_to_i64(z["dn"]))
+    assert T.negative_cycle_arcs(m) == 0 and not m.saturated
+    d = T.query_batch(m, gpu_ranks(z, "qs"), gpu_ranks(z, "qt")).cpu().numpy()
+    assert np.array_equal(d, i32_to_i64(z["ans"]))
+    assert np.array_equal(d, i32_to_i64(z["truth"]))
+
+
+@pytest.mark.parametrize("storage", ["int32", "int64"])
+@pytest.mark.parametrize("i", range(12))
+def test_family_customize_query(gpu, storage, i):
+    c = family_case(load_golden("family.npz"), i)
+    T = dev_topo(c)
+    m = T.customize(c["w"], storage)
+    up, dn = m.to_numpy()
+    assert np.array_equal(up, i32_to_i64(c["up"])) and np.array_equal(dn, i32_to_i64(c["dn"]))
+    d = T.query_batch(m, gpu_ranks(c, "qs"), gpu_ranks(c, "qt")).cpu().numpy()
+    assert np.array_equal(d, c["ans"]) and np.array_equal(d, c["truth"])
+
+
+@pytest.mark.parametrize("storage", ["int32", "int64"])
+@pytest.mark.parametrize("i", range(12))
+def test_family_updates(gpu, storage, i):
+    c = family_case(load_golden("family.npz"), i)
+    T = dev_topo(c)
+    m = T.customize(c["w"], storage)
+    for st in c["step_list"]:
+        ev = T.update(m, st["idx"], st["val"])
+        assert ev == int(st["evaluated"])
+        changed = np.sort(m.last_changed.cpu().numpy().astype(np.int64))
+        assert np.array_equal(changed, st["changed"])
+        up, dn = m.to_numpy()
+        assert np.array_equal(up[st["changed"]], i32_to_i64(st["up"]))
+        assert np.array_equal(dn[st["changed"]], i32_to_i64(st["dn"]))
+        assert (m.stats["changed_negative"] > 0) == bool(st["created"])
+        full = T.customize(m.w, storage)  # partial == full
+        fu, fd = full.to_numpy()
+        assert np.array_equal(fu, up) and np.array_equal(fd, dn)
+    before = m.to_numpy()
+    k = int(c["negcycle_edge"])
+    T.update(m, [k], [int(c["negcycle_w"])])
+    assert m.stats["changed_negative"] > 0 and T.negative_cycle_arcs(m) > 0
+    T.update(m, [k], [int(c["negcycle_restore_w"])])
+    assert T.negative_cycle_arcs(m) == 0
+    after = m.to_numpy()
+    assert np.array_equal(after[0], before[0]) and np.array_equal(after[1], before[1])
+    assert np.array_equal(after[0], i32_to_i64(c["final_up"]))
+
+
+def test_grid64(gpu):
+    z = load_golden("grid64.npz")
+    T = dev_topo(z)
+    for storage in ("int32", "int64"):
+        m = T.customize(z["w"], storage)
+        up, dn = m.to_numpy()
+        assert np.array_equal(up, i32_to_i64(z["up"])) and np.array_equal(dn, i32_to_i64(z["dn"]))
+        assert T.negative_cycle_arcs(m) == int(z["neg"])
+        d = T.query_batch(m, gpu_ranks(z, "qs"), gpu_ranks(z, "qt")).cpu().numpy()
+        assert np.array_equal(d, z["ans"])
+
+
+def test_delaunay_negative_cycles(gpu):
+    z = load_golden("delaunay_negcycle.npz")
+    T = dev_topo(z)
+    m = T.customize(z["w0"], "int32")
+    up, dn = m.to_numpy()
+    assert np.array_equal(up, i32_to_i64(z["up0"])) and np.array_equal(dn, i32_to_i64(z["dn0"]))
+    assert T.negative_cycle_arcs(m) == 0
+    d = T.query_batch(m, gpu_ranks(z, "qs"), gpu_ranks(z, "qt")).cpu().numpy()
+    assert np.array_equal(d, z["ans0"])
+    m = T.customize(z["mild_w"], "int32")
+    up, dn = m.to_numpy()
+    assert not m.saturated
+    assert np.array_equal(up, i32_to_i64(z["mild_up"])) and np.array_equal(dn, i32_to_i64(z["mild_dn"]))
+    assert T.negative_cycle_arcs(m) == int(z["mild_neg"])
+    for storage in ("int32", "int64"):
+        with pytest.warns(Warning):
+            m = T.customize(z["wild_w"], storage)
+        assert m.saturated and T.negative_cycle_arcs(m) > 0
+
+
+def _seeded(kind, n, seed):
+    from nwcch import graphs as G
+    from nwcch import topology as TT
+    g = {"delaunay": G.delaunay, "road": G.road_like}[kind](n, seed=seed)
+    return g, TT.build_topology(g)
+
+
+@pytest.mark.parametrize("kind,n", [("delaunay", 50_000), ("road", 80_000)])
+def test_against_oracle(gpu, oracle, kind, n):
+    from nwcch import graphs as G
+    from nwcch.device import DeviceTopology
+    g, top = _seeded(kind, n, seed=21)
+    T = DeviceTopology.from_dict(top)
+    OT = oracle.Topo.from_dict(top)
+    oup, odn = oracle.customize(OT, g["w"])
+    m = T.customize(g["w"], "int32")
+    up, dn = m.to_numpy()
+    assert np.array_equal(up, oup) and np.array_equal(dn, odn)
+    s, t = G.random_pairs(g["n"], 3000, seed=5)
+    d = T.query_batch(m, top["rank"][s], top["rank"][t]).cpu().numpy()
+    assert np.array_equal(d, oracle.query_batch(OT, oup, odn, top["rank"][s], top["rank"][t]))
+    # partial updates of 1, 100 and 1000 random arcs: equal to the oracle's
+    # update (evaluated count, changed set, values) and to a full recompute
+    rng = np.random.default_rng(9)
+    w = g["w"].copy()
+    for k in (1, 100, 1000):
+        idx = rng.choice(g["w"].size, size=k, replace=False)
+        val = (g["w"][idx] + rng.integers(-40, 200, size=k)).astype(np.int32)
+        ev = T.update(m, idx, val)
+        oev, och, oneg = oracle.update(OT, w, oup, odn, idx, val)
+        assert ev == oev
+        assert np.array_equal(np.sort(m.last_changed.cpu().numpy().astype(np.int64)), np.sort(och))
+        up, dn = m.to_numpy()
+        assert np.array_equal(up, oup) and np.array_equal(dn, odn)
+        assert (m.stats["changed_negative"] > 0) == (oneg > 0)
+        fu, fd = T.customize(m.w, "int32").to_numpy()
+        assert np.array_equal(fu, up) and np.array_equal(fd, dn)
+
+
+def test_dropin_cch_nb(gpu, oracle):
+    """The reference's run_nb.py call pattern, unchanged."""
+    from nwcch import cch_nb as nb
+    from nwcch import graphs as G
+    g = G.grid(48, seed=4)
+    n, off, tgt = g["n"], g["off"], g["tgt"]
+    noff, nbrs, rev = nb.undirected_csr(n, off, tgt)
+    rank = nb.nested_dissection(n, noff, nbrs, rev, g["x"], g["y"], 64)
+    first, head, parent = nb.symbolic(n, noff, nbrs, rank)
+    e_arc, e_up = nb.edge_arcs(n, off, tgt, rank, first, head)
+    upw, dnw = nb.customize(n, first, head, e_arc, e_up, g["w"].astype(np.float64))
+    assert nb.negative_cycle_arcs(upw, dnw) == 0
+    OT = oracle.Topo(n, first, head, parent, e_arc, e_up)
+    oup, odn = oracle.customize(OT, g["w"])
+    ref_up, ref_dn = nb.to_reference(upw, dnw)
+    assert np.array_equal(ref_up, oracle.to_float(oup)) and np.array_equal(ref_dn, oracle.to_float(odn))
+    df = dr = np.full(n, np.inf)
+    mark = np.zeros(n, np.int64)
+    s, t = G.random_pairs(n, 50, seed=3)
+    want = oracle.query_batch(OT, oup, odn, rank[s], rank[t])
+    for i in range(50):
+        got = nb.query(rank[s[i]], rank[t[i]], first, head, parent, upw, dnw, df, dr, mark, i + 1)
+        assert got == float(want[i])
+
+
+def test_cch_class_workflow(gpu, oracle):
+    """python/test_cch.py's workflow on the GPU class."""
+    from nwcch import graphs as G
+    from nwcch.cch import CCH
+    g = G.road_like(5_000, seed=8)
+    c = CCH.from_graph(g)
+    assert c.customize(g["w"]) == []
+    assert not c.has_negative_cycle()
+    rng = np.random.default_rng(1)
+    for _ in range(3):
+        picked = rng.choice(g["w"].size, size=10, replace=False)
+        c.update_edges(list(zip(picked, g["w"][picked] + 25)))
+        assert not c.update_created_negative_cycle()
+        c.update_edges(list(zip(picked, g["w"][picked])))
+    s, t = G.random_pairs(g["n"], 200, seed=2)
+    d = c.query_batch(s, t)
+    for i in range(0, 200, 40):
+        bf, neg = oracle.bellman_ford(g["n"], g["off"], g["tgt"], g["w"], int(s[i]))
+        want = np.inf if bf[t[i]] == INF else float(bf[t[i]])
+        assert d[i] == want

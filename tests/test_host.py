@@ -1,0 +1,117 @@
+"""Host-side, weight-independent preprocessing (C++ in libnwcch) and the
+C ABI surface. No GPU needed."""
+from __future__ import annotations
+
+import re
+
+import numpy as np
+import pytest
+
+from conftest import ROOT, family_case, load_golden
+
+
+def test_every_declared_symbol_is_exported(built_lib):
+    header = (ROOT / "include" / "nwcch.h").read_text()
+    names = set(re.findall(r"^\s*(?:int|void)\s+(nwcch_\w+)\s*\(", header, flags=re.M))
+    assert len(names) >= 20
+    missing = [n for n in sorted(names) if not hasattr(built_lib, n)]
+    assert not missing, missing
+
+
+def test_library_is_cuda_sm103a_build():
+    import build as nwbuild
+    assert "arch=compute_103a,code=sm_103a" in " ".join(nwbuild.NVCC_FLAGS)
+
+
+@pytest.mark.parametrize("name", ["grid64.npz", "delaunay_negcycle.npz"])
+def test_symbolic_matches_reference(built_lib, name):
+    from nwcch import topology as T
+    z = load_golden(name)
+    g = dict(n=int(z["n"]), off=z["off"], tgt=z["tgt"])
+    top = T.build_topology(g, rank=z["rank"])
+    for k in ("first", "head", "parent", "e_arc", "e_up"):
+        assert np.array_equal(top[k], z[k]), k
+
+
+def test_symbolic_matches_reference_family(built_lib):
+    from nwcch import topology as T
+    F = load_golden("family.npz")
+    for i in range(int(F["cases"])):
+        c = family_case(F, i)
+        top = T.build_topology(dict(n=int(c["n"]), off=c["off"], tgt=c["tgt"]), rank=c["rank"])
+        for k in ("first", "head", "parent", "e_arc", "e_up"):
+            assert np.array_equal(top[k], c[k]), (i, k)
+
+
+def test_techniques_union_topology(built_lib):
+    from nwcch import topology as T
+    z = load_golden("techniques.npz")
+    top = T.build_topology(dict(n=int(z["n"]), off=z["off"], tgt=z["tgt"]), rank=z["rank"])
+    for k in ("first", "head", "parent", "e_arc", "e_up"):
+        assert np.array_equal(top[k], z[k]), k
+
+
+def test_nested_dissection_is_a_permutation_and_deterministic(built_lib):
+    from nwcch import graphs as G
+    from nwcch import topology as T
+    g = G.delaunay(20_000, seed=3)
+    noff, nbrs, rev = T.undirected_csr(g["n"], g["off"], g["tgt"])
+    r1 = T.nested_dissection(g["n"], noff, nbrs, rev, g["x"], g["y"], 64, threads=4)
+    r2 = T.nested_dissection(g["n"], noff, nbrs, rev, g["x"], g["y"], 64, threads=1)
+    assert np.array_equal(np.sort(r1), np.arange(g["n"]))
+    assert np.array_equal(r1, r2)  # independent of the thread schedule
+
+
+def test_undirected_csr_reverse_slots(built_lib):
+    from nwcch import graphs as G
+    from nwcch import topology as T
+    g = G.grid(16, seed=1)
+    noff, nbrs, rev = T.undirected_csr(g["n"], g["off"], g["tgt"])
+    owner = np.repeat(np.arange(g["n"]), np.diff(noff))
+    assert np.array_equal(nbrs[rev], owner)
+    assert np.array_equal(owner[rev], nbrs)
+
+
+def test_triangle_edges_helper(built_lib):
+    import ctypes as C
+
+    from nwcch import _lib
+    tri = np.array([[0, 1, 2], [1, 2, 3], [2, 3, 0]], np.int64)
+    eu, ev, ne = C.c_void_p(), C.c_void_p(), C.c_int64()
+    _lib.check(built_lib.nwcch_triangle_edges(4, 3, _lib.ptr(tri), C.byref(eu), C.byref(ev), C.byref(ne)), "tri")
+    u = _lib.take_buffer(eu, ne.value, np.int64)
+    v = _lib.take_buffer(ev, ne.value, np.int64)
+    assert list(zip(u, v)) == [(0, 1), (0, 2), (0, 3), (1, 2), (1, 3), (2, 3)]
+
+
+def test_tiled_delaunay_equals_qhull():
+    from nwcch import delaunay as Dl
+    P = np.random.default_rng(2).random((450_000, 2))
+    eu, ev = Dl.delaunay_edges(P, workers=4)
+    du, dv = Dl._direct(P)
+    assert np.array_equal(eu, du) and np.array_equal(ev, dv)
+
+
+def test_generators_are_conservative(oracle):
+    from nwcch import graphs as G
+    for g in (G.grid(24, seed=2), G.delaunay(2_000, seed=2), G.road_like(3_000, seed=2)):
+        assert (g["w"] < 0).any()
+        assert not oracle.has_negative_cycle(g["n"], g["off"], g["tgt"], g["w"])
+    g, cyc = G.inject_negative_triangle(G.delaunay(2_000, seed=4), seed=1)
+    assert oracle.has_negative_cycle(g["n"], g["off"], g["tgt"], g["w"])
+
+
+def test_topology_create_rejects_bad_input_without_gpu(built_lib):
+    """Validation happens on the host before any device allocation."""
+    import ctypes as C
+
+    from nwcch import _lib
+    first = np.array([0, 1, 1], np.int64)
+    head = np.array([0], np.int32)      # head must lie above its tail
+    parent = np.array([0, -1], np.int32)
+    e_arc = np.zeros(0, np.int64)
+    e_up = np.zeros(0, np.int8)
+    h = C.c_void_p()
+    rc = built_lib.nwcch_topology_create(2, _lib.ptr(first), _lib.ptr(head), _lib.ptr(parent), 0, _lib.ptr(e_arc),
+                                         _lib.ptr(e_up), C.byref(h))
+    assert rc == -4  # NWCCH_ERR_TOPOLOGY

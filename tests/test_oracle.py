@@ -1,0 +1,121 @@
+"""The CPU oracle against golden vectors produced by the reference's own code
+(tests/golden/make_golden.py). These pin the oracle before any GPU result is
+compared with it."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from conftest import family_case, i32_to_i64, load_golden
+
+INF = np.iinfo(np.int64).max
+
+
+def topo(oracle, z, n=None):
+    return oracle.Topo(int(n if n is not None else z["n"]), z["first"], z["head"], z["parent"], z["e_arc"], z["e_up"])
+
+
+def test_saturated_infinity_pitfall(oracle):
+    # python/test_techniques.py:216-220: INF + (-5) must stay INF. Two-vertex
+    # graph where vertex 1 cannot reach vertex 0 and the arc 0->1 is negative.
+    T = oracle.Topo(2, [0, 1, 1], [1], [1, -1], [0], [1])
+    up, dn = oracle.customize(T, np.array([-5], np.int32))
+    assert up[0] == -5 and dn[0] == INF
+    assert oracle.negative_cycle_arcs(up, dn) == 0
+    d = oracle.query_batch(T, up, dn, [1, 0], [0, 1])
+    assert d[0] == INF and d[1] == -5
+
+
+def test_techniques_union(oracle):
+    z = load_golden("techniques.npz")
+    T = topo(oracle, z)
+    up, dn = oracle.customize(T, z["w"])
+    assert np.array_equal(up, i32_to_i64(z["up"]))
+    assert np.array_equal(dn, i32_to_i64(z["dn"]))
+    assert oracle.negative_cycle_arcs(up, dn) == 0
+    ans = oracle.query_batch(T, up, dn, z["rank"][z["qs"]], z["rank"][z["qt"]])
+    assert np.array_equal(ans, i32_to_i64(z["ans"]))
+    # the exact ET query equals Bellman-Ford on every pair
+    assert np.array_equal(ans, i32_to_i64(z["truth"]))
+    assert int(z["exhaustive"]) == 14440
+
+
+@pytest.mark.parametrize("i", range(12))
+def test_family_customize_query(oracle, i):
+    c = family_case(load_golden("family.npz"), i)
+    T = topo(oracle, c)
+    up, dn = oracle.customize(T, c["w"])
+    assert np.array_equal(up, i32_to_i64(c["up"]))
+    assert np.array_equal(dn, i32_to_i64(c["dn"]))
+    ans = oracle.query_batch(T, up, dn, c["rank"][c["qs"]], c["rank"][c["qt"]])
+    assert np.array_equal(ans, c["ans"])
+    assert np.array_equal(ans, c["truth"])
+    pup, pdn = oracle.customize_parallel(T, c["w"], threads=2)
+    assert np.array_equal(pup, up) and np.array_equal(pdn, dn)
+
+
+@pytest.mark.parametrize("i", [0, 4, 8, 11])
+def test_family_updates(oracle, i):
+    c = family_case(load_golden("family.npz"), i)
+    T = topo(oracle, c)
+    w = np.array(c["w"], np.int32)
+    up, dn = oracle.customize(T, w)
+    for st in c["step_list"]:
+        ev, changed, neg = oracle.update(T, w, up, dn, st["idx"], st["val"])
+        assert ev == int(st["evaluated"])
+        order = np.argsort(changed)
+        assert np.array_equal(changed[order], st["changed"])
+        assert np.array_equal(up[st["changed"]], i32_to_i64(st["up"]))
+        assert np.array_equal(dn[st["changed"]], i32_to_i64(st["dn"]))
+        assert (neg > 0) == bool(st["created"])
+        fup, fdn = oracle.customize(T, w)  # partial == full
+        assert np.array_equal(fup, up) and np.array_equal(fdn, dn)
+    # negative cycle created by an update, then removed by restoring
+    before = (up.copy(), dn.copy())
+    ev, changed, neg = oracle.update(T, w, up, dn, [int(c["negcycle_edge"])], [int(c["negcycle_w"])])
+    assert neg > 0 and oracle.negative_cycle_arcs(up, dn) > 0
+    oracle.update(T, w, up, dn, [int(c["negcycle_edge"])], [int(c["negcycle_restore_w"])])
+    assert oracle.negative_cycle_arcs(up, dn) == 0
+    assert np.array_equal(up, before[0]) and np.array_equal(dn, before[1])
+    assert np.array_equal(up, i32_to_i64(c["final_up"])) and np.array_equal(dn, i32_to_i64(c["final_dn"]))
+
+
+def test_grid64(oracle):
+    z = load_golden("grid64.npz")
+    T = topo(oracle, z)
+    up, dn = oracle.customize(T, z["w"])
+    assert np.array_equal(up, i32_to_i64(z["up"])) and np.array_equal(dn, i32_to_i64(z["dn"]))
+    assert oracle.negative_cycle_arcs(up, dn) == int(z["neg"]) == 0
+    ans = oracle.query_batch(T, up, dn, z["rank"][z["qs"]], z["rank"][z["qt"]], threads=2)
+    assert np.array_equal(ans, z["ans"])
+    pup, pdn = oracle.customize_parallel(T, z["w"], threads=4)
+    assert np.array_equal(pup, up) and np.array_equal(pdn, dn)
+
+
+def test_delaunay_negative_cycles(oracle):
+    z = load_golden("delaunay_negcycle.npz")
+    T = topo(oracle, z)
+    up, dn = oracle.customize(T, z["w0"])
+    assert np.array_equal(up, i32_to_i64(z["up0"])) and np.array_equal(dn, i32_to_i64(z["dn0"]))
+    assert oracle.negative_cycle_arcs(up, dn) == 0
+    ans = oracle.query_batch(T, up, dn, z["rank"][z["qs"]], z["rank"][z["qt"]])
+    assert np.array_equal(ans, z["ans0"])
+    # mild cycle: exact values; wild cycle: values explode, detection only
+    up, dn = oracle.customize(T, z["mild_w"])
+    assert bool(z["mild_exact"])
+    assert np.array_equal(up, i32_to_i64(z["mild_up"])) and np.array_equal(dn, i32_to_i64(z["mild_dn"]))
+    assert oracle.negative_cycle_arcs(up, dn) == int(z["mild_neg"])
+    assert oracle.has_negative_cycle(int(z["n"]), z["off"], z["tgt"], z["mild_w"])
+    assert oracle.has_negative_cycle(int(z["n"]), z["off"], z["tgt"], z["wild_w"])
+    assert not oracle.has_negative_cycle(int(z["n"]), z["off"], z["tgt"], z["w0"])
+
+
+def test_bellman_ford_pins_queries(oracle):
+    z = load_golden("grid64.npz")
+    n = int(z["n"])
+    for s in range(0, n, 997):
+        dist, neg = oracle.bellman_ford(n, z["off"], z["tgt"], z["w"], s)
+        assert not neg
+        sel = np.nonzero(z["qs"] == s)[0]
+        for q in sel:
+            assert dist[z["qt"][q]] == z["ans"][q]
