@@ -195,6 +195,18 @@ def run_ours(args, W, rank, world):
             torch.cuda.synchronize()
             q_ms.append(e0.elapsed_time(e1))
     sat = T.check()
+    # ---- the plain per-metric form (one launch per elimination level), for comparison
+    plain_ms = []
+    plain_metric = T.customize(w_dev, "int32", method="plain")
+    for _ in range(args.plain_steps):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        T.customize(w_dev, "int32", out=plain_metric, sync=False, method="plain")
+        e1.record(stream)
+        torch.cuda.synchronize()
+        plain_ms.append(e0.elapsed_time(e1))
+    same = all(bool(torch.equal(a, b)) for a, b in ((plain_metric.up, metric.up), (plain_metric.dn, metric.dn)))
     # ---- e2e through the public API from pinned host memory
     e2e_ms = []
     count_host = torch.empty(1, dtype=torch.int64).pin_memory()
@@ -213,7 +225,7 @@ def run_ours(args, W, rank, world):
         t0 = time.perf_counter()
         T.query_batch(good, qs[i:i + 1], qt[i:i + 1])
         lat.append((time.perf_counter() - t0) * 1e6)
-    res = dict(cust_ms=cust_ms, q_ms=q_ms, e2e_ms=e2e_ms, lat_us=lat, clocks=clocks.summary(), neg=neg_k,
+    res = dict(plain_ms=plain_ms, plain_equal=same, cust_ms=cust_ms, q_ms=q_ms, e2e_ms=e2e_ms, lat_us=lat, clocks=clocks.summary(), neg=neg_k,
                saturated=bool(sat or metric.saturated), wall_cust=wall_cust, T=T)
     return res
 
@@ -263,6 +275,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default=os.environ.get("NWCCH_BENCH_WORKLOAD", "usa24m"), choices=list(WORKLOADS))
     ap.add_argument("--cpu-budget", type=float, default=20.0)
+    ap.add_argument("--plain-steps", type=int, default=2)
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -309,6 +322,9 @@ def main():
                    "l2": "flushed between steps" if T.m_plus * 8 < 129e6 else "inputs larger than L2",
                    "parallelism": f"replicas x{world}"},
         "customize_ms_median": round(cust, 4),
+        "plain_customize_ms": round(statistics.median(R["plain_ms"]), 3) if R["plain_ms"] else None,
+        "plain_equals_supernodal": R["plain_equal"],
+        "supernodes": T.supernodes, "supernode_levels": T.sn_levels, "launches_per_customization": 2 + T.sn_launches,
         "negative_cycle_arcs": R["neg"], "saturated": R["saturated"],
         "queries_per_s": round(nq / (qms / 1000) * world, 1), "query_batch_ms": round(qms, 4),
         "query_latency_us": {"p50": round(lat[len(lat) // 2], 2), "p99": round(lat[int(len(lat) * 0.99) - 1], 2),
@@ -321,8 +337,9 @@ def main():
                          "sample": f"{cb['runs']} level-parallel customizations + scans of the same metric"},
         "clocks": R["clocks"],
     }
-    levels_with_work = int(T.levels)  # upper bound of per-level launches
-    line["gpu_launches"] = (2 + levels_with_work) * args.steps + args.steps * 2
+    # per customization: 2 base-value launches + the supernodal plan; 1 scan;
+    # 1 launch per query batch
+    line["gpu_launches"] = (2 + T.sn_launches + 1) * args.steps + args.steps
     print(json.dumps(line), flush=True)
 
 

@@ -85,6 +85,12 @@ int nwcch_edge_arcs(int64_t n, const int64_t* off, const int32_t* tgt, const int
 int nwcch_triangle_edges(int64_t n, int64_t ntri, const int64_t* tri, int64_t** eu, int64_t** ev,
                          int64_t* nedges);
 
+/* Minimum spanning forest (Kruskal, ties by edge id) of m weighted edges:
+ * mask[i] = 1 if edge i is in it. A helper of the synthetic road-like graph
+ * generator (no reference counterpart). */
+int nwcch_emst_mask(int64_t n, int64_t m, const int64_t* eu, const int64_t* ev, const double* length,
+                    uint8_t* mask);
+
 /* ------------------------------------------------------------------------
  * Device-resident topology. The reference passes first/head/parent/e_arc/
  * e_up to every call (python/cch_nb.py:529, 577); here they are validated,
@@ -102,7 +108,10 @@ int nwcch_topology_create(int64_t n, const int64_t* first, const int32_t* head,
 int nwcch_topology_destroy(nwcch_topology* t);
 
 /* info[0..7] = n, m+, m, lower triangles, levels, elimination-tree depth,
- * longest row, device bytes held by the handle. */
+ * longest row, device bytes held by the handle; with len >= 12 also
+ * info[8..11] = supernodes, supernode-tree levels, kernel launches of one
+ * supernodal customization (after the two base-value launches), outgoing
+ * arc ids stored. */
 int nwcch_topology_info(const nwcch_topology* t, int64_t* info, int64_t len);
 
 /* Reads and clears the error word of `t` after asynchronous calls
@@ -126,6 +135,14 @@ int nwcch_customize_i64(nwcch_topology* t, const int32_t* w_dev, int64_t* up_dev
                         void* stream);
 int nwcch_customize_i64_async(nwcch_topology* t, const int32_t* w_dev, int64_t* up_dev,
                               int64_t* dn_dev, void* stream);
+/* The plain form of the same computation: one launch per elimination level,
+ * a block per row pulling its lower triangles (the level structure of
+ * CCH::levels / customize_parallel, cpp/cch.cpp:465-529). Same results; kept
+ * as the per-metric baseline the supernodal path is measured against. */
+int nwcch_customize_plain(nwcch_topology* t, const int32_t* w_dev, int32_t* up_dev, int32_t* dn_dev,
+                          void* stream);
+int nwcch_customize_plain_async(nwcch_topology* t, const int32_t* w_dev, int32_t* up_dev,
+                                int32_t* dn_dev, void* stream);
 
 /* Number of arcs with up + dn < 0 (Theorem 3: nonzero iff a negative cycle).
  * Replaces cch_nb.negative_cycle_arcs (python/cch_nb.py:566-572) and

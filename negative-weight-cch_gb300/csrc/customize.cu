@@ -18,6 +18,7 @@
 
 #include "common.cuh"
 #include "customize.h"
+#include "supernodal.h"
 #include "topology.h"
 
 namespace nwcch {
@@ -185,13 +186,26 @@ using namespace nwcch;
 extern "C" int nwcch_customize_async(nwcch_topology* t, const int32_t* w_dev, int32_t* up_dev,
                                      int32_t* dn_dev, void* stream) {
     if (!t || !up_dev || !dn_dev || (t->d.m > 0 && !w_dev)) return NWCCH_ERR_ARG;
-    return customize_plain<int32_t>(t, w_dev, up_dev, dn_dev, (cudaStream_t)stream);
+    return run_supernodal<int32_t>(t, static_cast<SnPlan*>(t->sn_plan), w_dev, up_dev, dn_dev, (cudaStream_t)stream);
 }
 
 extern "C" int nwcch_customize_i64_async(nwcch_topology* t, const int32_t* w_dev, int64_t* up_dev,
                                          int64_t* dn_dev, void* stream) {
     if (!t || !up_dev || !dn_dev || (t->d.m > 0 && !w_dev)) return NWCCH_ERR_ARG;
-    return customize_plain<int64_t>(t, w_dev, up_dev, dn_dev, (cudaStream_t)stream);
+    return run_supernodal<int64_t>(t, static_cast<SnPlan*>(t->sn_plan), w_dev, up_dev, dn_dev, (cudaStream_t)stream);
+}
+
+extern "C" int nwcch_customize_plain_async(nwcch_topology* t, const int32_t* w_dev, int32_t* up_dev,
+                                           int32_t* dn_dev, void* stream) {
+    if (!t || !up_dev || !dn_dev || (t->d.m > 0 && !w_dev)) return NWCCH_ERR_ARG;
+    return customize_plain<int32_t>(t, w_dev, up_dev, dn_dev, (cudaStream_t)stream);
+}
+
+extern "C" int nwcch_customize_plain(nwcch_topology* t, const int32_t* w_dev, int32_t* up_dev, int32_t* dn_dev,
+                                     void* stream) {
+    const int rc = nwcch_customize_plain_async(t, w_dev, up_dev, dn_dev, stream);
+    if (rc) return rc;
+    return consume_error(t, (cudaStream_t)stream);
 }
 
 extern "C" int nwcch_check(nwcch_topology* t, void* stream) {

@@ -123,4 +123,55 @@ int nwcch_triangle_edges(int64_t n, int64_t ntri, const int64_t* tri, int64_t** 
     return NWCCH_OK;
 }
 
+int nwcch_emst_mask(int64_t n, int64_t m, const int64_t* eu, const int64_t* ev, const double* length,
+                    uint8_t* mask) {
+    if (n < 0 || m < 0 || (m > 0 && (!eu || !ev || !length || !mask))) return NWCCH_ERR_ARG;
+    // Kruskal: edges by (length, id), union-find with path halving
+    std::vector<int64_t> order(m);
+    for (int64_t i = 0; i < m; i++) {
+        if (eu[i] < 0 || eu[i] >= n || ev[i] < 0 || ev[i] >= n) return NWCCH_ERR_ARG;
+        order[i] = i;
+    }
+    const auto less = [&](int64_t a, int64_t b) {
+        return length[a] < length[b] || (length[a] == length[b] && a < b);
+    };
+    const int nth = (int)std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+    {
+        // sort nth chunks in parallel, then merge pairwise
+        std::vector<int64_t> bounds(nth + 1);
+        for (int t = 0; t <= nth; t++) bounds[t] = m * t / nth;
+        std::vector<std::thread> ts;
+        for (int t = 0; t < nth; t++)
+            ts.emplace_back([&, t] { std::sort(order.begin() + bounds[t], order.begin() + bounds[t + 1], less); });
+        for (auto& th : ts) th.join();
+        for (int width = 1; width < nth; width *= 2) {
+            std::vector<std::thread> ms;
+            for (int t = 0; t + width < nth; t += 2 * width) {
+                const int64_t lo = bounds[t], mid = bounds[t + width], hi = bounds[std::min(nth, t + 2 * width)];
+                ms.emplace_back([&, lo, mid, hi] {
+                    std::inplace_merge(order.begin() + lo, order.begin() + mid, order.begin() + hi, less);
+                });
+            }
+            for (auto& th : ms) th.join();
+        }
+    }
+    std::vector<int64_t> up(n);
+    for (int64_t v = 0; v < n; v++) up[v] = v;
+    auto find = [&](int64_t v) {
+        while (up[v] != v) {
+            up[v] = up[up[v]];
+            v = up[v];
+        }
+        return v;
+    };
+    std::memset(mask, 0, (size_t)m);
+    for (int64_t i : order) {
+        const int64_t a = find(eu[i]), b = find(ev[i]);
+        if (a == b) continue;
+        up[a] = b;
+        mask[i] = 1;
+    }
+    return NWCCH_OK;
+}
+
 }  // extern "C"

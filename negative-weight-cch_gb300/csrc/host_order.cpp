@@ -114,8 +114,18 @@ class VertexCut {
         const int32_t m = g.m;
         through_.assign(m, 0);
         flow_.assign(g.edges, 0);
-        level_.assign(2 * (size_t)m, -1);
+        level_.assign(2 * (size_t)m, 0);
+        seen_.assign(2 * (size_t)m, 0);
         ptr_.assign(2 * (size_t)m, 0);
+        // only sources with a non-source neighbour can start a path
+        for (int32_t v = 0; v < m; v++) {
+            if (role[v] != SOURCE) continue;
+            for (int64_t j = g.off[v]; j < g.off[v + 1]; j++)
+                if (role[g.adj[j]] != SOURCE) {
+                    frontier_.push_back(v);
+                    break;
+                }
+        }
     }
 
     CutResult run() {
@@ -128,9 +138,21 @@ class VertexCut {
     const vector<int8_t>& role_;
     vector<int8_t> through_;   // unit flow through a normal vertex (in -> out)
     vector<int8_t> flow_;      // flow on an undirected edge, + from lower to higher id
-    vector<int32_t> level_;
+    vector<int32_t> level_;    // BFS depth, valid where seen_ == phase_
+    vector<int32_t> seen_;
+    int32_t phase_ = 0;
     vector<int64_t> ptr_;
     vector<int64_t> queue_;
+    vector<int32_t> frontier_;
+
+    // Sources are the super-source: always reached, at depth 0.
+    bool reached(int64_t x) const { return role_[x >> 1] == SOURCE || seen_[x] == phase_; }
+    int32_t depth(int64_t x) const { return role_[x >> 1] == SOURCE ? 0 : level_[x]; }
+    void reach(int64_t x, int32_t d) {
+        seen_[x] = phase_;
+        level_[x] = d;
+        queue_.push_back(x);
+    }
 
     // flow on the slot j (from its owner vertex towards adj[j])
     int flow_on(int64_t j) const { return g_.fwd[j] ? flow_[g_.eid[j]] : -flow_[g_.eid[j]]; }
@@ -160,65 +182,59 @@ class VertexCut {
         return g_.off[v + 1] - g_.off[v];
     }
 
+    // Level graph from the sources; true if a sink was reached.
     bool bfs() {
-        std::fill(level_.begin(), level_.end(), -1);
+        phase_++;
         queue_.clear();
-        for (int32_t v = 0; v < g_.m; v++)
-            if (role_[v] == SOURCE) {
-                level_[2 * (size_t)v] = 0;
-                level_[2 * (size_t)v + 1] = 0;
-                queue_.push_back(2 * (int64_t)v);
-                queue_.push_back(2 * (int64_t)v + 1);
-            }
-        bool reached = false;
+        for (int32_t v : frontier_) {
+            queue_.push_back(2 * (int64_t)v);
+            queue_.push_back(2 * (int64_t)v + 1);
+        }
+        bool hit = false;
         for (size_t qh = 0; qh < queue_.size(); qh++) {
             const int64_t x = queue_[qh];
-            const int32_t v = (int32_t)(x >> 1);
-            if (role_[v] == SINK) {
-                reached = true;
+            if (role_[x >> 1] == SINK) {
+                hit = true;
                 continue;
             }
+            const int32_t dx = depth(x);
             const int64_t deg = degree(x);
             for (int64_t a = 0; a <= deg; a++) {
                 const int64_t y = arc_head(x, a);
-                if (y >= 0 && level_[y] < 0) {
-                    level_[y] = level_[x] + 1;
-                    queue_.push_back(y);
-                }
+                if (y >= 0 && !reached(y)) reach(y, dx + 1);
             }
         }
-        return reached;
+        return hit;
     }
 
     void blocking_flow() {
         for (int64_t x : queue_) ptr_[x] = 0;
         vector<int64_t> path;
-        vector<int64_t> used;  // arc index used at each path node
-        for (int32_t s = 0; s < g_.m; s++) {
-            if (role_[s] != SOURCE) continue;
+        for (int32_t s : frontier_) {
             const int64_t start = 2 * (int64_t)s + 1;
+            ptr_[start] = 0;
             while (true) {
                 path.assign(1, start);
                 bool found = false;
                 while (!path.empty()) {
                     const int64_t x = path.back();
-                    const int32_t v = (int32_t)(x >> 1);
-                    if (role_[v] == SINK) {
+                    if (role_[x >> 1] == SINK) {
                         found = true;
                         break;
                     }
                     const int64_t deg = degree(x);
+                    const int32_t want = depth(x) + 1;
                     bool advanced = false;
                     for (; ptr_[x] <= deg; ptr_[x]++) {
                         const int64_t y = arc_head(x, ptr_[x]);
-                        if (y >= 0 && level_[y] == level_[x] + 1) {
+                        if (y >= 0 && role_[y >> 1] != SOURCE && seen_[y] == phase_ && level_[y] == want) {
                             path.push_back(y);
                             advanced = true;
                             break;
                         }
                     }
                     if (!advanced) {
-                        level_[x] = -1;  // dead end for this phase
+                        if (role_[x >> 1] != SOURCE) level_[x] = -2;  // dead end for this phase
                         path.pop_back();
                         if (!path.empty()) ptr_[path.back()]++;
                     }
@@ -243,29 +259,23 @@ class VertexCut {
 
     CutResult extract() {
         // residual reachability from the sources
-        std::fill(level_.begin(), level_.end(), -1);
+        phase_++;
         queue_.clear();
-        for (int32_t v = 0; v < g_.m; v++)
-            if (role_[v] == SOURCE) {
-                level_[2 * (size_t)v] = 0;
-                level_[2 * (size_t)v + 1] = 0;
-                queue_.push_back(2 * (int64_t)v);
-                queue_.push_back(2 * (int64_t)v + 1);
-            }
+        for (int32_t v : frontier_) {
+            queue_.push_back(2 * (int64_t)v);
+            queue_.push_back(2 * (int64_t)v + 1);
+        }
         for (size_t qh = 0; qh < queue_.size(); qh++) {
             const int64_t x = queue_[qh];
             const int64_t deg = degree(x);
             for (int64_t a = 0; a <= deg; a++) {
                 const int64_t y = arc_head(x, a);
-                if (y >= 0 && level_[y] < 0) {
-                    level_[y] = 0;
-                    queue_.push_back(y);
-                }
+                if (y >= 0 && !reached(y)) reach(y, 0);
             }
         }
         CutResult r;
         for (int32_t v = 0; v < g_.m; v++) {
-            const bool rin = level_[2 * (size_t)v] >= 0, rout = level_[2 * (size_t)v + 1] >= 0;
+            const bool rin = reached(2 * (int64_t)v), rout = reached(2 * (int64_t)v + 1);
             if (rin && !rout) r.sep.push_back(v);
             else if (rout) r.a.push_back(v);
             else r.b.push_back(v);
@@ -304,6 +314,7 @@ class Dissector {
     const int32_t* nbr_;
     const double *x_, *y_;
     int64_t leaf_;
+    int64_t band_min_ = 250000;
     int threads_;
     std::unique_ptr<std::atomic<int64_t>[]> owner_;  // cell stamp currently holding a vertex
     vector<int32_t> local_;               // local id inside that cell
@@ -400,7 +411,12 @@ class Dissector {
         std::stable_sort(perm.begin(), perm.end(), [&](int32_t a, int32_t b) {
             return key(c.verts[a], dir) < key(c.verts[b], dir);
         });
-        const int32_t k = std::max<int32_t>(1, m / 4);
+        // inertial flow takes the first and last quarter as sources and sinks;
+        // on very large cells the cut is searched in a narrower middle band
+        // (10% of the cell, at least band_min_ vertices) to bound the flow work
+        int64_t band = m / 2;
+        if (m > band_min_ * 2) band = std::max<int64_t>(band_min_, m / 10);
+        const int32_t k = std::max<int32_t>(1, (int32_t)((m - band) / 2));
         vector<int8_t> role(m, NORMAL);
         for (int32_t i = 0; i < k; i++) {
             role[perm[i]] = SOURCE;

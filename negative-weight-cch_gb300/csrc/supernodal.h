@@ -1,0 +1,62 @@
+// Supernodal customization plan (internal).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <vector>
+
+struct nwcch_topology;
+
+namespace nwcch {
+
+// A supernode is a maximal run of ranks [s0, s0+k) in which every vertex's
+// upper row is the next vertex plus the row of that next vertex (rows nested).
+// Its arcs form a dense trapezoid: row i (vertex s0+i) holds the columns
+// j in (i, k + b): ranks s0+i+1..s0+k-1 and then the boundary B (the row of
+// the last vertex, b entries), at index first[s0+i] + (j - i - 1).
+struct SnDev {
+    const int32_t* s0;       // [nsn]
+    const int32_t* k;        // [nsn]
+    const int32_t* b;        // [nsn]
+    const int64_t* rel_off;  // [nsn] start of the supernode's outgoing arc ids
+    const int32_t* rel;      // arc id of (B[p], B[q]) for p < q, packed upper triangle
+};
+
+enum SnKind : int {
+    SN_INT_SMALL = 0,  // warp per supernode: vertex-sequential internal triangles
+    SN_PANEL = 1,      // CTA per (supernode, column tile): one 32-row panel
+    SN_TRAIL = 2,      // CTA per (supernode, row tile, column tile): trailing update
+    SN_OUT_BIG = 3,    // CTA per 64x64 tile of the outgoing boundary x boundary block
+    SN_OUT_SMALL = 4,  // CTA per 16x16 tile of the same
+};
+
+struct SnLaunch {
+    int kind;
+    int level;
+    int panel;
+    int64_t off;    // first item (int32 triples) in the plan's item array
+    int64_t count;  // items
+};
+
+struct SnPlan {
+    int64_t nsn = 0;
+    int32_t levels = 0;
+    int64_t items = 0;
+    int64_t rel_entries = 0;
+    std::vector<SnLaunch> launches;
+    SnDev dev{};
+    int32_t* d_items = nullptr;
+    std::vector<void*> allocations;
+    size_t bytes = 0;
+};
+
+// Builds the plan from the host copy of a topology; nullptr on failure.
+SnPlan* build_supernodal_plan(int64_t n, const int64_t* first, const int32_t* head, const int32_t* parent, int* rc);
+void free_supernodal_plan(SnPlan* p);
+
+// Enqueues a full customization on stream s (base values + every launch).
+template <class T>
+int run_supernodal(nwcch_topology* t, SnPlan* P, const int32_t* w, T* up, T* dn, cudaStream_t s);
+
+}  // namespace nwcch

@@ -10,6 +10,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "supernodal.h"
 #include "topology.h"
 
 namespace nwcch {
@@ -31,6 +32,8 @@ int upload(nwcch_topology* t, const T* src, size_t count, T** dst) {
 
 void release(nwcch_topology* t) {
     if (t->free_plans) t->free_plans(t);
+    free_supernodal_plan(static_cast<SnPlan*>(t->sn_plan));
+    t->sn_plan = nullptr;
     for (void* p : t->allocations) cudaFree(p);
     t->allocations.clear();
 }
@@ -148,6 +151,9 @@ extern "C" int nwcch_topology_create(int64_t n, const int64_t* first, const int3
             for (int64_t k = 0; k < m; k++)
                 if (e_arc[k] >= 0) aeidx[fill[e_arc[k]]++] = (int32_t)k;
         }
+        t->sn_plan = build_supernodal_plan(n, first, head, parent, &rc);
+        if (rc) break;
+        t->device_bytes += static_cast<SnPlan*>(t->sn_plan)->bytes;
         t->triangles = tri;
         t->max_deg = maxdeg;
         t->nloops = (int64_t)loops.size();
@@ -225,5 +231,12 @@ extern "C" int nwcch_topology_info(const nwcch_topology* t, int64_t* info, int64
     info[5] = t->d.max_depth;
     info[6] = t->max_deg;
     info[7] = (int64_t)t->device_bytes;
+    if (len >= 12) {
+        const auto* p = static_cast<const SnPlan*>(t->sn_plan);
+        info[8] = p ? p->nsn : 0;
+        info[9] = p ? p->levels : 0;
+        info[10] = p ? (int64_t)p->launches.size() : 0;
+        info[11] = p ? p->rel_entries : 0;
+    }
     return NWCCH_OK;
 }

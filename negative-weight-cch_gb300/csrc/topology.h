@@ -49,6 +49,7 @@ struct nwcch_topology {
     unsigned long long* counters = nullptr;   // device: 16 scratch counters (scan results)
     std::vector<void*> allocations;           // every cudaMalloc of this handle
     size_t device_bytes = 0;
+    void* sn_plan = nullptr;                  // nwcch::SnPlan (supernodal customization)
     std::mutex mu;                            // serialises lazily built plans
     void* plans = nullptr;                    // owned by the modules that build plans
     void (*free_plans)(nwcch_topology*) = nullptr;

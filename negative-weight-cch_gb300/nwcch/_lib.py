@@ -51,6 +51,7 @@ _SIGNATURES = {
     "nwcch_symbolic": [I64, P, P, P, P, P, PP, PI64],
     "nwcch_edge_arcs": [I64, P, P, P, P, P, P, P],
     "nwcch_triangle_edges": [I64, I64, P, PP, PP, PI64],
+    "nwcch_emst_mask": [I64, I64, P, P, P, P],
 }
 _VOID = {"nwcch_host_free"}
 

@@ -71,9 +71,15 @@ def _hull_size(P):
 
 
 def _edges_from_triangles(tri: np.ndarray, n: int):
-    e = np.concatenate([tri[:, [0, 1]], tri[:, [1, 2]], tri[:, [0, 2]]]).astype(np.int64)
-    code = np.unique(e[:, 0] * n + e[:, 1])
-    return code // n, code % n
+    """Unique sorted edges of a triangle list (counting sort in libnwcch)."""
+    import ctypes as C
+
+    from . import _lib
+    tri = np.ascontiguousarray(tri, np.int64)
+    eu, ev, ne = C.c_void_p(), C.c_void_p(), C.c_int64()
+    _lib.check(_lib.lib().nwcch_triangle_edges(n, tri.shape[0], _lib.ptr(tri), C.byref(eu), C.byref(ev),
+                                               C.byref(ne)), "triangle_edges")
+    return _lib.take_buffer(eu, ne.value, np.int64), _lib.take_buffer(ev, ne.value, np.int64)
 
 
 def _direct(P):

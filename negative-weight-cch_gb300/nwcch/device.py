@@ -27,6 +27,8 @@ for _name, _args in {
     "nwcch_customize_async": [P, P, P, P, P],
     "nwcch_customize_i64": [P, P, P, P, P],
     "nwcch_customize_i64_async": [P, P, P, P, P],
+    "nwcch_customize_plain": [P, P, P, P, P],
+    "nwcch_customize_plain_async": [P, P, P, P, P],
     "nwcch_negative_cycle_arcs": [P, P, P, PI64, P],
     "nwcch_negative_cycle_arcs_i64": [P, P, P, PI64, P],
     "nwcch_negative_loops": [P, P, PI64, P],
@@ -126,10 +128,11 @@ class DeviceTopology:
         _lib.check(lib.nwcch_topology_create(self.n, _lib.ptr(first), _lib.ptr(head), _lib.ptr(parent), e_arc.size,
                                              _lib.ptr(e_arc), _lib.ptr(e_up), C.byref(h)), "topology_create")
         self._h = h
-        info = np.zeros(8, np.int64)
-        _lib.check(lib.nwcch_topology_info(h, _lib.ptr(info), 8), "topology_info")
+        info = np.zeros(12, np.int64)
+        _lib.check(lib.nwcch_topology_info(h, _lib.ptr(info), 12), "topology_info")
         (self.n, self.m_plus, self.m, self.triangles, self.levels, self.depth, self.max_row,
-         self.device_bytes) = (int(v) for v in info)
+         self.device_bytes, self.supernodes, self.sn_levels, self.sn_launches,
+         self.rel_entries) = (int(v) for v in info)
 
     @classmethod
     def from_dict(cls, t: dict) -> "DeviceTopology":
@@ -172,7 +175,10 @@ class DeviceTopology:
         return t.contiguous()
 
     # ------------------------------------------------------------ customization
-    def customize(self, w, storage: str = "int32", out: Metric | None = None, sync: bool = True) -> Metric:
+    def customize(self, w, storage: str = "int32", out: Metric | None = None, sync: bool = True,
+                  method: str = "supernodal") -> Metric:
+        """method "supernodal" (default) or "plain" (one launch per level,
+        int32 only: the plain per-metric form kept for comparison)."""
         torch = self._torch
         lib = _lib.lib()
         wt = self.weights(w)
@@ -182,8 +188,14 @@ class DeviceTopology:
         else:
             up = torch.empty(self.m_plus, dtype=dt, device="cuda")
             dn = torch.empty(self.m_plus, dtype=dt, device="cuda")
-        fn = {("int32", True): lib.nwcch_customize, ("int32", False): lib.nwcch_customize_async,
-              ("int64", True): lib.nwcch_customize_i64, ("int64", False): lib.nwcch_customize_i64_async}[storage, sync]
+        if method == "plain":
+            if storage != "int32":
+                raise ValueError("the plain customization stores int32")
+            fn = lib.nwcch_customize_plain if sync else lib.nwcch_customize_plain_async
+        else:
+            fn = {("int32", True): lib.nwcch_customize, ("int32", False): lib.nwcch_customize_async,
+                  ("int64", True): lib.nwcch_customize_i64,
+                  ("int64", False): lib.nwcch_customize_i64_async}[storage, sync]
         sat = _status(fn(self.handle, wt.data_ptr(), up.data_ptr(), dn.data_ptr(), _stream(torch)), "customize")
         m = Metric(self, wt, up, dn, saturated=sat)
         if sat:

@@ -106,18 +106,16 @@ def delaunay(n: int = 264_000, seed: int = 0, hmax: int = 500, scale: float = 10
 
 
 def _emst_mask(n, eu, ev, length):
-    """Kruskal over the Delaunay edges (which contain the Euclidean MST)."""
-    from scipy.sparse import coo_matrix
-    from scipy.sparse.csgraph import minimum_spanning_tree
-    # distinct positive keys keep the tree unique: length, then edge id
-    key = length.astype(np.float64) + (np.arange(eu.size) + 1.0) / (eu.size + 2.0) * 1e-9
-    g = coo_matrix((key, (eu, ev)), shape=(n, n)).tocsr()
-    t = minimum_spanning_tree(g).tocoo()
-    tu = np.minimum(t.row, t.col).astype(np.int64)
-    tv = np.maximum(t.row, t.col).astype(np.int64)
-    code = eu.astype(np.int64) * n + ev
-    tcode = tu * n + tv
-    return np.isin(code, tcode)
+    """Kruskal over the Delaunay edges (which contain the Euclidean MST),
+    ties broken by edge id; in C++ (libnwcch)."""
+    from . import _lib
+    eu = np.ascontiguousarray(eu, np.int64)
+    ev = np.ascontiguousarray(ev, np.int64)
+    length = np.ascontiguousarray(length, np.float64)
+    mask = np.empty(eu.size, np.uint8)
+    _lib.check(_lib.lib().nwcch_emst_mask(n, eu.size, _lib.ptr(eu), _lib.ptr(ev), _lib.ptr(length),
+                                          _lib.ptr(mask)), "emst_mask")
+    return mask.astype(bool)
 
 
 def road_like(n: int = 264_000, arcs: int | None = None, seed: int = 0, hmax: int = 500,
