@@ -186,13 +186,15 @@ using namespace nwcch;
 extern "C" int nwcch_customize_async(nwcch_topology* t, const int32_t* w_dev, int32_t* up_dev,
                                      int32_t* dn_dev, void* stream) {
     if (!t || !up_dev || !dn_dev || (t->d.m > 0 && !w_dev)) return NWCCH_ERR_ARG;
-    return run_supernodal<int32_t>(t, static_cast<SnPlan*>(t->sn_plan), w_dev, up_dev, dn_dev, (cudaStream_t)stream);
+    return launch_supernodal<int32_t>(t, static_cast<SnPlan*>(t->sn_plan), w_dev, up_dev, dn_dev,
+                                      (cudaStream_t)stream);
 }
 
 extern "C" int nwcch_customize_i64_async(nwcch_topology* t, const int32_t* w_dev, int64_t* up_dev,
                                          int64_t* dn_dev, void* stream) {
     if (!t || !up_dev || !dn_dev || (t->d.m > 0 && !w_dev)) return NWCCH_ERR_ARG;
-    return run_supernodal<int64_t>(t, static_cast<SnPlan*>(t->sn_plan), w_dev, up_dev, dn_dev, (cudaStream_t)stream);
+    return launch_supernodal<int64_t>(t, static_cast<SnPlan*>(t->sn_plan), w_dev, up_dev, dn_dev,
+                                      (cudaStream_t)stream);
 }
 
 extern "C" int nwcch_customize_plain_async(nwcch_topology* t, const int32_t* w_dev, int32_t* up_dev,

@@ -1,0 +1,389 @@
+// Kernels of the supernodal customization (included by supernodal.cu).
+//
+// Arithmetic policies. Exact<T> relaxes with the saturating sum of common.cuh
+// (the reference semantics, storage int32 or int64). FastI32 is the int32
+// path on the DPX min-plus instruction: operands are stored "compact" (no
+// path = CINF = 2^30-1, finite values within +-2^28), so a + b never
+// overflows int32, finite sums stay within +-2^29 and sums involving no-path
+// are >= 2^30-1-2^28 > 2^29. A block takes the fast path only if every value
+// it reads is within +-2^28 and (for recurrences that feed results back as
+// operands) every value it would write is too; otherwise it recomputes with
+// Exact from the unchanged inputs. Within those bounds both paths are the
+// same integer arithmetic, so the result does not depend on the path.
+#pragma once
+
+#include <type_traits>
+
+#include "common.cuh"
+
+namespace nwcch {
+
+struct FastI32 {
+    using V = int32_t;
+    static constexpr int32_t CINF = (1 << 30) - 1;
+    static constexpr int32_t THR = 1 << 29;    // above: no path
+    static constexpr int32_t RANGE = 1 << 28;  // finite operands stay within +-RANGE
+    __device__ static V from(int32_t x) { return x == INF32 ? CINF : x; }
+    __device__ static bool in(int32_t x) { return x == INF32 || (x >= -RANGE && x <= RANGE); }
+    __device__ static V clean(V x) { return x > THR ? CINF : x; }
+    __device__ static V inf() { return CINF; }
+    __device__ static void relax(V& c, V a, V b, int&) { c = __viaddmin_s32(a, b, c); }
+    __device__ static bool out_ok(V x) { return x > THR || (x >= -RANGE && x <= RANGE); }
+    __device__ static bool finite(V x) { return x <= THR; }
+    __device__ static int32_t to(V x) { return x > THR ? INF32 : x; }
+};
+
+template <class T>
+struct Exact {
+    using V = T;
+    __device__ static V from(T x) { return x; }
+    __device__ static V clean(V x) { return x; }
+    __device__ static V inf() { return Lim<T>::INF; }
+    __device__ static void relax(V& c, V a, V b, int& e) {
+        V s;
+        if (splus(a, b, s, e) && s < c) c = s;
+    }
+    __device__ static bool out_ok(V) { return true; }
+    __device__ static bool finite(V x) { return x != Lim<T>::INF; }
+    __device__ static T to(V x) { return x; }
+};
+
+__device__ __forceinline__ void atomic_min_t(int32_t* p, int32_t v) { atomicMin(p, v); }
+__device__ __forceinline__ void atomic_min_t(int64_t* p, int64_t v) {
+    atomicMin(reinterpret_cast<long long*>(p), (long long)v);
+}
+
+// ------------------------------------------------------------------ panel
+
+// Shared state of one panel block: the panel's diagonal triangle (arcs among
+// its own <= 32 vertices) and CT columns of its rows.
+template <class V, int CT>
+struct PanelSmem {
+    V Ud[SN_P][SN_P + 1], Dd[SN_P][SN_P + 1];
+    V cU[SN_P][CT], cD[SN_P][CT];
+    int64_t rowb[SN_P];
+};
+
+// Factor the diagonal triangle, then run the panel recurrence down this
+// thread's column. Rows a < r of the panel: for every column c beyond r,
+//   U(r, c) <- Dn(a, r) + U(a, c),   Dn(r, c) <- Dn(a, c) + U(a, r).
+template <class P, class V, int CT>
+__device__ void panel_compute(PanelSmem<V, CT>& sm, int pn, bool hasj, int& e) {
+    constexpr int RS = CT / 32;  // row stride of the diagonal mapping
+    const int tid = threadIdx.x;
+    const int c = tid & 31, r0 = tid >> 5;
+    // Diagonal triangle, right-looking: step a relaxes every pair a < r < c.
+    // Row a + 1 receives its last update in step a and becomes the operand row
+    // of step a + 1, so it is stored clean right then (row 0 is clean input).
+    for (int a = 0; a + 2 < pn; a++) {
+        if (c < pn && c > a + 1) {
+            const V uac = sm.Ud[a][c], dac = sm.Dd[a][c];
+            int r = a + 1 + ((r0 - a - 1) % RS + RS) % RS;
+            for (; r < c; r += RS) {
+                V u = sm.Ud[r][c], d = sm.Dd[r][c];
+                P::relax(u, sm.Dd[a][r], uac, e);
+                P::relax(d, dac, sm.Ud[a][r], e);
+                if (r == a + 1) {
+                    u = P::clean(u);
+                    d = P::clean(d);
+                }
+                sm.Ud[r][c] = u;
+                sm.Dd[r][c] = d;
+            }
+        }
+        __syncthreads();
+    }
+    // the last row may not have been touched: clean every entry once
+    for (int t = tid; t < SN_P * SN_P; t += CT) {
+        const int rr = t >> 5, cc = t & 31;
+        if (rr < cc && cc < pn) {
+            sm.Ud[rr][cc] = P::clean(sm.Ud[rr][cc]);
+            sm.Dd[rr][cc] = P::clean(sm.Dd[rr][cc]);
+        }
+    }
+    __syncthreads();
+    if (hasj) {
+        for (int a = 0; a + 1 < pn; a++) {
+            const V cu = P::clean(sm.cU[a][tid]), cd = P::clean(sm.cD[a][tid]);
+#pragma unroll 4
+            for (int r = a + 1; r < pn; r++) {
+                P::relax(sm.cU[r][tid], sm.Dd[a][r], cu, e);
+                P::relax(sm.cD[r][tid], cd, sm.Ud[a][r], e);
+            }
+        }
+    }
+}
+
+// Loads the diagonal triangle and the thread's column (converted by P).
+// Returns true if some value is outside the fast range (FastI32 only).
+template <class P, class T, class V, int CT>
+__device__ bool panel_load(PanelSmem<V, CT>& sm, const T* __restrict__ up, const T* __restrict__ dn, int pn,
+                           int i0, int j, bool hasj) {
+    const int tid = threadIdx.x;
+    bool bad = false;
+    for (int t = tid; t < SN_P * SN_P; t += CT) {
+        const int a = t >> 5, c = t & 31;
+        if (a < c && c < pn) {
+            const T u = up[sm.rowb[a] + c - a - 1], d = dn[sm.rowb[a] + c - a - 1];
+            if constexpr (std::is_same<P, FastI32>::value) bad |= !P::in(u) || !P::in(d);
+            sm.Ud[a][c] = P::from(u);
+            sm.Dd[a][c] = P::from(d);
+        }
+    }
+    if (hasj)
+        for (int a = 0; a < pn; a++) {
+            const int64_t idx = sm.rowb[a] + (j - (i0 + a)) - 1;
+            const T u = up[idx], d = dn[idx];
+            if constexpr (std::is_same<P, FastI32>::value) bad |= !P::in(u) || !P::in(d);
+            sm.cU[a][tid] = P::from(u);
+            sm.cD[a][tid] = P::from(d);
+        }
+    return bad;
+}
+
+template <class P, class T, class V, int CT>
+__device__ void panel_store(PanelSmem<V, CT>& sm, T* __restrict__ up, T* __restrict__ dn, int pn, int i0, int j,
+                            bool hasj, bool diag) {
+    const int tid = threadIdx.x;
+    if (diag)
+        for (int t = tid; t < SN_P * SN_P; t += CT) {
+            const int a = t >> 5, c = t & 31;
+            if (a < c && c < pn) {
+                up[sm.rowb[a] + c - a - 1] = P::to(sm.Ud[a][c]);
+                dn[sm.rowb[a] + c - a - 1] = P::to(sm.Dd[a][c]);
+            }
+        }
+    if (hasj)
+        for (int a = 1; a < pn; a++) {
+            const int64_t idx = sm.rowb[a] + (j - (i0 + a)) - 1;
+            up[idx] = P::to(sm.cU[a][tid]);
+            dn[idx] = P::to(sm.cD[a][tid]);
+        }
+}
+
+template <class P, class V, int CT>
+__device__ bool panel_outputs_ok(const PanelSmem<V, CT>& sm, int pn, bool hasj) {
+    const int tid = threadIdx.x;
+    bool ok = true;
+    for (int t = tid; t < SN_P * SN_P; t += CT) {
+        const int a = t >> 5, c = t & 31;
+        if (a < c && c < pn) ok &= P::out_ok(sm.Ud[a][c]) && P::out_ok(sm.Dd[a][c]);
+    }
+    if (hasj)
+        for (int a = 0; a < pn; a++) ok &= P::out_ok(sm.cU[a][tid]) && P::out_ok(sm.cD[a][tid]);
+    return ok;
+}
+
+// One 32-row panel [i0, i0+pn) of a supernode with k >= 2, CT columns per
+// block (the item's 128-column tile in 128/CT passes). Block ct == 0 also
+// writes the diagonal triangle.
+template <class T, int CT>
+__global__ void __launch_bounds__(CT) k_sn_panel(DevTopo D, SnDev S, const int32_t* __restrict__ items, int panel,
+                                                 T* __restrict__ up, T* __restrict__ dn, int* __restrict__ err) {
+    using E = Exact<T>;
+    __shared__ PanelSmem<T, CT> sm;
+    const int32_t s = items[3 * blockIdx.x], ct = items[3 * blockIdx.x + 1];
+    const int32_t s0 = S.s0[s], k = S.k[s], cols = k + S.b[s];
+    const int i0 = panel * SN_P;
+    const int pn = min(SN_P, k - i0);
+    const int tid = threadIdx.x;
+    int e = 0;
+    if (tid < pn) sm.rowb[tid] = D.first[s0 + i0 + tid];
+    __syncthreads();
+    for (int pass = 0; pass < 128 / CT; pass++) {
+        const int j = i0 + pn + ct * 128 + pass * CT + tid;
+        const bool hasj = j < cols;
+        const bool diag = ct == 0 && pass == 0;
+        bool done = false;
+        if constexpr (sizeof(T) == 4) {
+            auto& fs = reinterpret_cast<PanelSmem<int32_t, CT>&>(sm);
+            const bool bad = panel_load<FastI32, T, int32_t, CT>(fs, up, dn, pn, i0, j, hasj);
+            if (!__syncthreads_or(bad)) {
+                panel_compute<FastI32, int32_t, CT>(fs, pn, hasj, e);
+                const bool ok = panel_outputs_ok<FastI32, int32_t, CT>(fs, pn, hasj);
+                if (!__syncthreads_or(!ok)) {
+                    panel_store<FastI32, T, int32_t, CT>(fs, up, dn, pn, i0, j, hasj, diag);
+                    done = true;
+                }
+            }
+        }
+        if (!done) {
+            __syncthreads();
+            panel_load<E, T, T, CT>(sm, up, dn, pn, i0, j, hasj);
+            __syncthreads();
+            panel_compute<E, T, CT>(sm, pn, hasj, e);
+            panel_store<E, T, T, CT>(sm, up, dn, pn, i0, j, hasj, diag);
+        }
+        __syncthreads();
+    }
+    if (e) atomicOr(err, e);
+}
+
+// ------------------------------------------------------------------ tiles
+
+// (min,+) tile product over inner rows [ibeg, iend) of a supernode:
+//   U(y, z)  <- min_i Dn(i, y) + U(i, z)     (arc y -> z through x = s0+i)
+//   Dn(y, z) <- min_i Dn(i, z) + U(i, y)
+// for the tile's output rows y (columns abase.. of the trapezoid) and output
+// columns z (bbase..). OUT = false: trailing update of `panel`, y ranges over
+// the supernode's own later vertices, outputs folded into its own arcs.
+// OUT = true: y and z are boundary entries, the inner rows are the whole
+// supernode, outputs atomically folded into the ancestors' arcs.
+template <class T, int TILE, int MT, bool OUT>
+struct TileCtx {
+    int32_t s, s0, k, b, cols;
+    int ibeg, iend, abase, bbase, alim;
+};
+
+template <class T, int TILE, int MT, bool OUT>
+__device__ __forceinline__ TileCtx<T, TILE, MT, OUT> tile_ctx(const SnDev& S, const int32_t* items, int panel) {
+    TileCtx<T, TILE, MT, OUT> c;
+    c.s = items[3 * blockIdx.x];
+    const int tr = items[3 * blockIdx.x + 1], tc = items[3 * blockIdx.x + 2];
+    c.s0 = S.s0[c.s];
+    c.k = S.k[c.s];
+    c.b = S.b[c.s];
+    c.cols = c.k + c.b;
+    if (OUT) {
+        c.ibeg = 0;
+        c.iend = c.k;
+        c.abase = c.k + tr * TILE;
+        c.bbase = c.k + tc * TILE;
+        c.alim = c.cols;
+    } else {
+        c.ibeg = panel * SN_P;
+        c.iend = min(c.k, c.ibeg + SN_P);
+        c.abase = c.iend + tr * TILE;
+        c.bbase = c.iend + tc * TILE;
+        c.alim = c.k;
+    }
+    return c;
+}
+
+template <class V, int TILE, int CH>
+struct TileSmem {
+    V Ad[CH][TILE], Au[CH][TILE], Bu[CH][TILE], Bd[CH][TILE];
+    int64_t rowb[CH];
+};
+
+// Runs the product with policy P; returns false (fast policy only) as soon as
+// an operand leaves the fast range, leaving the accumulators meaningless.
+template <class P, class T, int TILE, int MT, int CH, bool OUT>
+__device__ bool tile_product(const DevTopo& D, const TileCtx<T, TILE, MT, OUT>& c,
+                             TileSmem<typename P::V, TILE, CH>& sm, const T* __restrict__ up,
+                             const T* __restrict__ dn, typename P::V (&accU)[MT][MT], typename P::V (&accD)[MT][MT],
+                             int& e) {
+    using V = typename P::V;
+    constexpr int TH = TILE / MT;
+    constexpr int NT = TH * TH;
+    constexpr bool FAST = std::is_same<P, FastI32>::value;
+    const int tid = threadIdx.x, ty = tid / TH, tx = tid % TH;
+#pragma unroll
+    for (int ii = 0; ii < MT; ii++)
+#pragma unroll
+        for (int jj = 0; jj < MT; jj++) {
+            accU[ii][jj] = P::inf();
+            accD[ii][jj] = P::inf();
+        }
+    for (int i0 = c.ibeg; i0 < c.iend; i0 += CH) {
+        const int nch = min(CH, c.iend - i0);
+        __syncthreads();
+        if (tid < CH) sm.rowb[tid] = tid < nch ? D.first[c.s0 + i0 + tid] : 0;
+        __syncthreads();
+        bool bad = false;
+        for (int t = tid; t < CH * TILE; t += NT) {
+            const int a = t / TILE, cc = t % TILE;
+            const int ac = c.abase + cc, bc = c.bbase + cc;
+            const bool okr = a < nch;
+            const int64_t rb = sm.rowb[a] - (i0 + a) - 1;
+            const T ad = (okr && ac < c.alim) ? dn[rb + ac] : Lim<T>::INF;
+            const T au = (okr && ac < c.alim) ? up[rb + ac] : Lim<T>::INF;
+            const T bu = (okr && bc < c.cols) ? up[rb + bc] : Lim<T>::INF;
+            const T bd = (okr && bc < c.cols) ? dn[rb + bc] : Lim<T>::INF;
+            if constexpr (FAST) bad |= !FastI32::in(ad) || !FastI32::in(au) || !FastI32::in(bu) || !FastI32::in(bd);
+            sm.Ad[a][cc] = P::from(ad);
+            sm.Au[a][cc] = P::from(au);
+            sm.Bu[a][cc] = P::from(bu);
+            sm.Bd[a][cc] = P::from(bd);
+        }
+        if constexpr (FAST) {
+            if (__syncthreads_or(bad)) return false;
+        } else {
+            __syncthreads();
+        }
+        for (int a = 0; a < nch; a++) {
+            V ad[MT], au[MT], bu[MT], bd[MT];
+#pragma unroll
+            for (int ii = 0; ii < MT; ii++) {
+                ad[ii] = sm.Ad[a][ty + TH * ii];
+                au[ii] = sm.Au[a][ty + TH * ii];
+                bu[ii] = sm.Bu[a][tx + TH * ii];
+                bd[ii] = sm.Bd[a][tx + TH * ii];
+            }
+#pragma unroll
+            for (int ii = 0; ii < MT; ii++)
+#pragma unroll
+                for (int jj = 0; jj < MT; jj++) {
+                    P::relax(accU[ii][jj], ad[ii], bu[jj], e);
+                    P::relax(accD[ii][jj], bd[jj], au[ii], e);
+                }
+        }
+    }
+    return true;
+}
+
+template <class P, class T, int TILE, int MT, bool OUT>
+__device__ void tile_store(const DevTopo& D, const SnDev& S, const TileCtx<T, TILE, MT, OUT>& c, T* __restrict__ up,
+                           T* __restrict__ dn, const typename P::V (&accU)[MT][MT],
+                           const typename P::V (&accD)[MT][MT]) {
+    constexpr int TH = TILE / MT;
+    const int tid = threadIdx.x, ty = tid / TH, tx = tid % TH;
+#pragma unroll
+    for (int ii = 0; ii < MT; ii++)
+#pragma unroll
+        for (int jj = 0; jj < MT; jj++) {
+            const int rr = c.abase + ty + TH * ii, cc = c.bbase + tx + TH * jj;  // trapezoid columns
+            if (cc <= rr || cc >= c.cols || rr >= c.alim) continue;
+            const bool fu = P::finite(accU[ii][jj]), fd = P::finite(accD[ii][jj]);
+            if (!fu && !fd) continue;
+            int64_t a;
+            if (OUT) {
+                const int p = rr - c.k, q = cc - c.k;
+                a = S.rel[S.rel_off[c.s] + (int64_t)p * (2 * c.b - p - 1) / 2 + (q - p - 1)];
+                if (fu) atomic_min_t(&up[a], (T)P::to(accU[ii][jj]));
+                if (fd) atomic_min_t(&dn[a], (T)P::to(accD[ii][jj]));
+            } else {
+                a = D.first[c.s0 + rr] + (cc - rr - 1);
+                if (fu) up[a] = min(up[a], (T)P::to(accU[ii][jj]));
+                if (fd) dn[a] = min(dn[a], (T)P::to(accD[ii][jj]));
+            }
+        }
+}
+
+template <class T, int TILE, int MT, bool OUT>
+__global__ void __launch_bounds__((TILE / MT) * (TILE / MT))
+    k_sn_tile(DevTopo D, SnDev S, const int32_t* __restrict__ items, int panel, T* __restrict__ up,
+              T* __restrict__ dn, int* __restrict__ err) {
+    constexpr int CH = sizeof(T) == 4 ? 32 : 16;
+    using E = Exact<T>;
+    __shared__ TileSmem<T, TILE, CH> sm;
+    const auto c = tile_ctx<T, TILE, MT, OUT>(S, items, panel);
+    int e = 0;
+    bool done = false;
+    if constexpr (sizeof(T) == 4) {
+        auto& fs = reinterpret_cast<TileSmem<int32_t, TILE, CH>&>(sm);
+        int32_t accU[MT][MT], accD[MT][MT];
+        if (tile_product<FastI32, T, TILE, MT, CH, OUT>(D, c, fs, up, dn, accU, accD, e)) {
+            tile_store<FastI32, T, TILE, MT, OUT>(D, S, c, up, dn, accU, accD);
+            done = true;
+        }
+    }
+    if (!done) {
+        T accU[MT][MT], accD[MT][MT];
+        tile_product<E, T, TILE, MT, CH, OUT>(D, c, sm, up, dn, accU, accD, e);
+        tile_store<E, T, TILE, MT, OUT>(D, S, c, up, dn, accU, accD);
+    }
+    if (e) atomicOr(err, e);
+}
+
+}  // namespace nwcch

@@ -26,6 +26,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <cstdlib>
 #include <new>
 #include <thread>
 #include <vector>
@@ -38,7 +39,7 @@
 namespace nwcch {
 
 constexpr int SN_P = 32;          // panel height
-constexpr int SN_SMALL_K = 32;    // supernodes up to this width use the warp kernel
+constexpr int SN_SMALL_K = 1;     // every supernode with k >= 2 runs the panel kernel
 constexpr int PANEL_THREADS = 128;
 
 // ------------------------------------------------------------------ plan
@@ -64,6 +65,7 @@ int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
 
 void free_supernodal_plan(SnPlan* p) {
     if (!p) return;
+    for (auto& g : p->graphs) cudaGraphExecDestroy(g.exec);
     for (void* a : p->allocations) cudaFree(a);
     delete p;
 }
@@ -216,280 +218,24 @@ SnPlan* build_supernodal_plan(int64_t n, const int64_t* first, const int32_t* he
     return P;
 }
 
-// ------------------------------------------------------------------ kernels
 
-// Extended accumulator of a (min,+) product over storage T: int32 storage
-// accumulates in int64 with "no path" as a large sentinel (no branch per
-// term); int64 storage uses the saturating sum.
-template <class T>
-struct Acc;
-template <>
-struct Acc<int32_t> {
-    using V = int64_t;
-    static constexpr int64_t BIG = (int64_t)1 << 61;    // any sum >= 2^60 is "no path"
-    __device__ static V load(int32_t x) { return x == INF32 ? BIG : (int64_t)x; }
-    __device__ static V init() { return BIG; }
-    __device__ static void relax(V& acc, V a, V b, int&) { acc = min(acc, a + b); }
-    // fold into the stored value; returns the new stored value
-    __device__ static int32_t fold(int32_t cur, V acc, int& err) {
-        if (acc >= ((int64_t)1 << 60)) return cur;
-        int32_t c;
-        if (acc > Lim<int32_t>::HI) {
-            c = Lim<int32_t>::HI;
-            err |= ERR_RANGE;
-        } else if (acc < Lim<int32_t>::LO) {
-            c = Lim<int32_t>::LO;
-            err |= ERR_RANGE;
-        } else {
-            c = (int32_t)acc;
-        }
-        return min(cur, c);
-    }
-    __device__ static bool finite(V acc) { return acc < ((int64_t)1 << 60); }
-};
-template <>
-struct Acc<int64_t> {
-    using V = int64_t;
-    __device__ static V load(int64_t x) { return x; }
-    __device__ static V init() { return INF64; }
-    __device__ static void relax(V& acc, V a, V b, int& err) {
-        int64_t s;
-        if (splus(a, b, s, err)) acc = min(acc, s);
-    }
-    __device__ static int64_t fold(int64_t cur, V acc, int&) { return min(cur, acc); }
-    __device__ static bool finite(V acc) { return acc != INF64; }
-};
+}  // namespace nwcch
 
-__device__ __forceinline__ void atomic_min_t(int32_t* p, int32_t v) { atomicMin(p, v); }
-__device__ __forceinline__ void atomic_min_t(int64_t* p, int64_t v) {
-    atomicMin(reinterpret_cast<long long*>(p), (long long)v);
-}
+#include "sn_kernels.cuh"
 
-// Internal triangles of a supernode with k <= 32, one warp each: for row i
-// (final once rows < i are done), every pair (r, j), i < r < j, relaxes
-// arc (r, j) by (i -> r -> ... ) i.e. y = s0+r, z = column j.
-template <class T>
-__global__ void __launch_bounds__(128) k_sn_int_small(DevTopo D, SnDev S, const int32_t* __restrict__ items,
-                                                      int64_t count, T* __restrict__ up, T* __restrict__ dn,
-                                                      int* __restrict__ err) {
-    const int lane = threadIdx.x & 31;
-    const int64_t w = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    int e = 0;
-    for (int64_t it = w; it < count; it += nw) {
-        const int32_t s = items[3 * it];
-        const int32_t s0 = S.s0[s], k = S.k[s], cols = k + S.b[s];
-        for (int i = 0; i + 1 < k; i++) {
-            const int64_t bi = D.first[s0 + i];
-            for (int r = i + 1; r < k; r++) {
-                const T d_ir = dn[bi + r - i - 1], u_ir = up[bi + r - i - 1];
-                const int64_t br = D.first[s0 + r];
-                for (int j = r + 1 + lane; j < cols; j += 32) {
-                    const T u_ij = up[bi + j - i - 1], d_ij = dn[bi + j - i - 1];
-                    const int64_t a = br + j - r - 1;
-                    T c;
-                    if (splus(d_ir, u_ij, c, e) && c < up[a]) up[a] = c;  // y -> x -> z
-                    if (splus(d_ij, u_ir, c, e) && c < dn[a]) dn[a] = c;  // z -> x -> y
-                }
-            }
-            __syncwarp();
-        }
-    }
-    if (e) atomicOr(err, e);
-}
-
-// One 32-row panel [i0, i0+pn) of a big supernode. Every CTA loads and
-// factors the panel's diagonal triangle (arcs among the panel's own vertices)
-// in shared memory; CTA 0 writes it back. Each thread then owns one column j
-// beyond the panel and runs the panel recurrence down it in registers.
-template <class T>
-__global__ void __launch_bounds__(PANEL_THREADS) k_sn_panel(DevTopo D, SnDev S, const int32_t* __restrict__ items,
-                                                            int panel, T* __restrict__ up, T* __restrict__ dn,
-                                                            int* __restrict__ err) {
-    __shared__ T Ud[SN_P][SN_P + 1], Dd[SN_P][SN_P + 1];
-    __shared__ int64_t rowb[SN_P];
-    const int32_t s = items[3 * blockIdx.x], ct = items[3 * blockIdx.x + 1];
-    const int32_t s0 = S.s0[s], k = S.k[s], cols = k + S.b[s];
-    const int i0 = panel * SN_P;
-    const int pn = min(SN_P, k - i0);
-    const int tid = threadIdx.x;
-    int e = 0;
-    if (tid < pn) rowb[tid] = D.first[s0 + i0 + tid];
-    __syncthreads();
-    for (int t = tid; t < pn * pn; t += blockDim.x) {
-        const int a = t / pn, c = t % pn;
-        if (a < c) {
-            Ud[a][c] = up[rowb[a] + c - a - 1];
-            Dd[a][c] = dn[rowb[a] + c - a - 1];
-        }
-    }
-    __syncthreads();
-    for (int a = 0; a + 2 < pn; a++) {
-        for (int t = tid; t < pn * pn; t += blockDim.x) {
-            const int r = t / pn, c = t % pn;
-            if (a < r && r < c) {
-                T v;
-                if (splus(Dd[a][r], Ud[a][c], v, e) && v < Ud[r][c]) Ud[r][c] = v;
-                if (splus(Dd[a][c], Ud[a][r], v, e) && v < Dd[r][c]) Dd[r][c] = v;
-            }
-        }
-        __syncthreads();
-    }
-    if (ct == 0) {
-        for (int t = tid; t < pn * pn; t += blockDim.x) {
-            const int a = t / pn, c = t % pn;
-            if (a < c) {
-                up[rowb[a] + c - a - 1] = Ud[a][c];
-                dn[rowb[a] + c - a - 1] = Dd[a][c];
-            }
-        }
-    }
-    const int j = i0 + pn + ct * PANEL_THREADS + tid;
-    if (j < cols) {
-        T cu[SN_P], cd[SN_P];
-#pragma unroll
-        for (int a = 0; a < SN_P; a++)
-            if (a < pn) {
-                const int64_t idx = rowb[a] + (j - (i0 + a)) - 1;
-                cu[a] = up[idx];
-                cd[a] = dn[idx];
-            }
-#pragma unroll
-        for (int a = 0; a < SN_P; a++) {
-#pragma unroll
-            for (int r = a + 1; r < SN_P; r++) {
-                if (r < pn) {
-                    T v;
-                    if (splus(Dd[a][r], cu[a], v, e) && v < cu[r]) cu[r] = v;
-                    if (splus(cd[a], Ud[a][r], v, e) && v < cd[r]) cd[r] = v;
-                }
-            }
-        }
-#pragma unroll
-        for (int a = 1; a < SN_P; a++)
-            if (a < pn) {
-                const int64_t idx = rowb[a] + (j - (i0 + a)) - 1;
-                up[idx] = cu[a];
-                dn[idx] = cd[a];
-            }
-    }
-    if (e) atomicOr(err, e);
-}
-
-// (min,+) tile product over the rows [ibeg, iend) of a supernode:
-//   U(x, y) <- min_i Dn(i, ycol) + U(i, xcol)   (arc y -> z through x = s0+i)
-//   Dn(x, y) <- min_i Dn(i, xcol) + U(i, ycol)
-// for the tile's "row" columns A (the y of the output arc) and "column"
-// columns B (the z). OUT = false: trailing update of panel `panel`, rows are
-// the supernode's own vertices after the panel; outputs folded into its own
-// arcs. OUT = true: rows and columns are boundary entries, inner rows are the
-// whole supernode, outputs atomically folded into the ancestors' arcs.
-template <class T, int TILE, int MT, bool OUT>
-__global__ void __launch_bounds__((TILE / MT) * (TILE / MT))
-    k_sn_tile(DevTopo D, SnDev S, const int32_t* __restrict__ items, int panel, T* __restrict__ up,
-              T* __restrict__ dn, int* __restrict__ err) {
-    using A = Acc<T>;
-    using V = typename A::V;
-    constexpr int TH = TILE / MT;        // threads per tile edge
-    constexpr int NT = TH * TH;
-    constexpr int CH = sizeof(T) == 4 ? 32 : 16;  // inner rows staged per round
-    __shared__ T Ad[CH][TILE], Au[CH][TILE], Bu[CH][TILE], Bd[CH][TILE];
-    __shared__ int64_t rowb[CH];
-    const int32_t s = items[3 * blockIdx.x], tr = items[3 * blockIdx.x + 1], tc = items[3 * blockIdx.x + 2];
-    const int32_t s0 = S.s0[s], k = S.k[s], b = S.b[s], cols = k + b;
-    int ibeg, iend, abase, bbase, alim;
-    if (OUT) {
-        ibeg = 0;
-        iend = k;
-        abase = k + tr * TILE;
-        bbase = k + tc * TILE;
-        alim = cols;
-    } else {
-        ibeg = panel * SN_P;
-        iend = min(k, ibeg + SN_P);
-        abase = iend + tr * TILE;
-        bbase = iend + tc * TILE;
-        alim = k;
-    }
-    const int tid = threadIdx.x, ty = tid / TH, tx = tid % TH;
-    int e = 0;
-    V accU[MT][MT], accD[MT][MT];
-#pragma unroll
-    for (int ii = 0; ii < MT; ii++)
-#pragma unroll
-        for (int jj = 0; jj < MT; jj++) {
-            accU[ii][jj] = A::init();
-            accD[ii][jj] = A::init();
-        }
-    for (int i0 = ibeg; i0 < iend; i0 += CH) {
-        const int nch = min(CH, iend - i0);
-        if (tid < CH) rowb[tid] = tid < nch ? D.first[s0 + i0 + tid] : 0;
-        __syncthreads();
-        for (int t = tid; t < CH * TILE; t += NT) {
-            const int a = t / TILE, c = t % TILE;
-            const int ac = abase + c, bc = bbase + c;
-            const bool okr = a < nch;
-            const int64_t rb = rowb[a] - (i0 + a) - 1;
-            Ad[a][c] = (okr && ac < alim) ? dn[rb + ac] : Lim<T>::INF;
-            Au[a][c] = (okr && ac < alim) ? up[rb + ac] : Lim<T>::INF;
-            Bu[a][c] = (okr && bc < cols) ? up[rb + bc] : Lim<T>::INF;
-            Bd[a][c] = (okr && bc < cols) ? dn[rb + bc] : Lim<T>::INF;
-        }
-        __syncthreads();
-        for (int a = 0; a < nch; a++) {
-            V ad[MT], au[MT], bu[MT], bd[MT];
-#pragma unroll
-            for (int ii = 0; ii < MT; ii++) {
-                ad[ii] = A::load(Ad[a][ty + TH * ii]);
-                au[ii] = A::load(Au[a][ty + TH * ii]);
-                bu[ii] = A::load(Bu[a][tx + TH * ii]);
-                bd[ii] = A::load(Bd[a][tx + TH * ii]);
-            }
-#pragma unroll
-            for (int ii = 0; ii < MT; ii++)
-#pragma unroll
-                for (int jj = 0; jj < MT; jj++) {
-                    A::relax(accU[ii][jj], ad[ii], bu[jj], e);
-                    A::relax(accD[ii][jj], bd[jj], au[ii], e);
-                }
-        }
-        __syncthreads();
-    }
-#pragma unroll
-    for (int ii = 0; ii < MT; ii++)
-#pragma unroll
-        for (int jj = 0; jj < MT; jj++) {
-            const int rr = abase + ty + TH * ii, cc = bbase + tx + TH * jj;  // columns of the trapezoid
-            if (cc <= rr || cc >= cols || rr >= alim) continue;
-            if (OUT) {
-                const int p = rr - k, q = cc - k;
-                const int64_t a = S.rel[S.rel_off[s] + (int64_t)p * (2 * b - p - 1) / 2 + (q - p - 1)];
-                if (A::finite(accU[ii][jj])) atomic_min_t(&up[a], A::fold(Lim<T>::INF, accU[ii][jj], e));
-                if (A::finite(accD[ii][jj])) atomic_min_t(&dn[a], A::fold(Lim<T>::INF, accD[ii][jj], e));
-            } else {
-                const int64_t a = D.first[s0 + rr] + (cc - rr - 1);
-                up[a] = A::fold(up[a], accU[ii][jj], e);
-                dn[a] = A::fold(dn[a], accD[ii][jj], e);
-            }
-        }
-    if (e) atomicOr(err, e);
-}
+namespace nwcch {
 
 template <class T>
 int run_supernodal(nwcch_topology* t, SnPlan* P, const int32_t* w, T* up, T* dn, cudaStream_t s) {
     int rc = base_init<T>(t, w, up, dn, s);
     if (rc) return rc;
     const DevTopo& D = t->d;
+    constexpr int CT = sizeof(T) == 4 ? 128 : 32;
     for (const SnLaunch& la : P->launches) {
         const int32_t* it = P->d_items + 3 * la.off;
         switch (la.kind) {
-            case SN_INT_SMALL: {
-                const int64_t blocks = std::min<int64_t>(ceil_div(la.count, 4), 152 * 64);
-                k_sn_int_small<T><<<(unsigned)blocks, 128, 0, s>>>(D, P->dev, it, la.count, up, dn, t->err);
-                break;
-            }
             case SN_PANEL:
-                k_sn_panel<T><<<(unsigned)la.count, PANEL_THREADS, 0, s>>>(D, P->dev, it, la.panel, up, dn, t->err);
+                k_sn_panel<T, CT><<<(unsigned)la.count, CT, 0, s>>>(D, P->dev, it, la.panel, up, dn, t->err);
                 break;
             case SN_TRAIL:
                 k_sn_tile<T, 64, 4, false><<<(unsigned)la.count, 256, 0, s>>>(D, P->dev, it, la.panel, up, dn, t->err);
@@ -500,11 +246,53 @@ int run_supernodal(nwcch_topology* t, SnPlan* P, const int32_t* w, T* up, T* dn,
             case SN_OUT_SMALL:
                 k_sn_tile<T, 16, 2, true><<<(unsigned)la.count, 64, 0, s>>>(D, P->dev, it, 0, up, dn, t->err);
                 break;
+            default:
+                return NWCCH_ERR_TOPOLOGY;
         }
     }
     return cudaGetLastError() == cudaSuccess ? NWCCH_OK : NWCCH_ERR_CUDA;
 }
 
+template <class T>
+int launch_supernodal(nwcch_topology* t, SnPlan* P, const int32_t* w, T* up, T* dn, cudaStream_t s) {
+    static const bool no_graph = getenv("NWCCH_NO_GRAPH") != nullptr;
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    NWCCH_CUDA_TRY(cudaStreamIsCapturing(s, &cap));
+    if (no_graph || cap != cudaStreamCaptureStatusNone) return run_supernodal<T>(t, P, w, up, dn, s);
+    std::lock_guard<std::mutex> lock(P->graph_mu);
+    const int storage = (int)sizeof(T);
+    SnGraph* hit = nullptr;
+    for (auto& g : P->graphs)
+        if (g.storage == storage && g.w == w && g.up == up && g.dn == dn) hit = &g;
+    if (!hit) {
+        cudaStream_t cs;
+        NWCCH_CUDA_TRY(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+        cudaGraph_t graph = nullptr;
+        int rc = NWCCH_OK;
+        if (cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal) != cudaSuccess) rc = NWCCH_ERR_CUDA;
+        if (!rc) rc = run_supernodal<T>(t, P, w, up, dn, cs);
+        if (cudaStreamEndCapture(cs, &graph) != cudaSuccess && !rc) rc = NWCCH_ERR_CUDA;
+        cudaGraphExec_t exec = nullptr;
+        if (!rc && cudaGraphInstantiate(&exec, graph, 0) != cudaSuccess) rc = NWCCH_ERR_CUDA;
+        if (graph) cudaGraphDestroy(graph);
+        cudaStreamDestroy(cs);
+        if (rc) return rc;
+        if (P->graphs.size() >= 8) {
+            auto old = std::min_element(P->graphs.begin(), P->graphs.end(),
+                                        [](const SnGraph& a, const SnGraph& b) { return a.last_use < b.last_use; });
+            cudaGraphExecDestroy(old->exec);
+            P->graphs.erase(old);
+        }
+        P->graphs.push_back(SnGraph{storage, w, up, dn, exec, 0});
+        hit = &P->graphs.back();
+    }
+    hit->last_use = ++P->graph_clock;
+    NWCCH_CUDA_TRY(cudaGraphLaunch(hit->exec, s));
+    return NWCCH_OK;
+}
+
+template int launch_supernodal<int32_t>(nwcch_topology*, SnPlan*, const int32_t*, int32_t*, int32_t*, cudaStream_t);
+template int launch_supernodal<int64_t>(nwcch_topology*, SnPlan*, const int32_t*, int64_t*, int64_t*, cudaStream_t);
 template int run_supernodal<int32_t>(nwcch_topology*, SnPlan*, const int32_t*, int32_t*, int32_t*, cudaStream_t);
 template int run_supernodal<int64_t>(nwcch_topology*, SnPlan*, const int32_t*, int64_t*, int64_t*, cudaStream_t);
 

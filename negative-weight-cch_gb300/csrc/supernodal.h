@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <mutex>
 #include <vector>
 
 struct nwcch_topology;
@@ -39,7 +40,20 @@ struct SnLaunch {
     int64_t count;  // items
 };
 
+// A captured customization for one (storage, w, up, dn) binding.
+struct SnGraph {
+    int storage;
+    const void* w;
+    void* up;
+    void* dn;
+    cudaGraphExec_t exec;
+    uint64_t last_use;
+};
+
 struct SnPlan {
+    std::vector<SnGraph> graphs;  // small cache, most recently used kept
+    uint64_t graph_clock = 0;
+    std::mutex graph_mu;
     int64_t nsn = 0;
     int32_t levels = 0;
     int64_t items = 0;
@@ -58,5 +72,11 @@ void free_supernodal_plan(SnPlan* p);
 // Enqueues a full customization on stream s (base values + every launch).
 template <class T>
 int run_supernodal(nwcch_topology* t, SnPlan* P, const int32_t* w, T* up, T* dn, cudaStream_t s);
+
+// The same through a CUDA graph captured once per (w, up, dn) binding and
+// replayed afterwards; when s is itself being captured the launches are
+// simply enqueued into the caller's capture.
+template <class T>
+int launch_supernodal(nwcch_topology* t, SnPlan* P, const int32_t* w, T* up, T* dn, cudaStream_t s);
 
 }  // namespace nwcch

@@ -118,6 +118,25 @@ def test_delaunay_negative_cycles(gpu):
         assert m.saturated and T.negative_cycle_arcs(m) > 0
 
 
+def test_large_weights_take_the_exact_path(gpu, oracle):
+    """Weights near 2^27: sums leave the +-2^28 window of the DPX fast path,
+    so blocks recompute exactly; results stay equal to the oracle."""
+    from nwcch import graphs as G
+    from nwcch import topology as TT
+    from nwcch.device import DeviceTopology
+    g = G.grid(10, seed=5)
+    w = (g["w"].astype(np.int64) << 20).astype(np.int32)
+    top = TT.build_topology(g, leaf=8)
+    T = DeviceTopology.from_dict(top)
+    oup, odn = oracle.customize(oracle.Topo.from_dict(top), w)
+    assert np.abs(oup[oup != INF]).max() > (1 << 28)
+    for storage in ("int32", "int64"):
+        m = T.customize(w, storage)
+        up, dn = m.to_numpy()
+        assert not m.saturated
+        assert np.array_equal(up, oup) and np.array_equal(dn, odn)
+
+
 def _seeded(kind, n, seed):
     from nwcch import graphs as G
     from nwcch import topology as TT
