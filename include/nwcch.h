@@ -191,6 +191,25 @@ int nwcch_query_batch_i64(nwcch_topology* t, const int64_t* up_dev, const int64_
                           const int32_t* s_rank_dev, const int32_t* t_rank_dev, int64_t nq,
                           int64_t* dist_dev, void* stream);
 
+/* Allocation-free form of nwcch_query_batch (int32 storage); it has no
+ * counterpart in the reference. For callers that must not allocate device
+ * memory: a serving loop that has already given all device memory to
+ * resident metrics, an application whose own allocator owns the device, or a
+ * latency-critical path that cannot risk an allocator call. Instead of
+ * cudaMallocAsync it uses a fixed 32 MiB label scratch compiled into the
+ * library (held by every GPU that loads it until the process exits); it
+ * calls no allocation routine. Limit: the per-warp scratch is
+ * 8 * (2.5 * (depth + 1) + 1) bytes and whole blocks of 4 warps must fit, so
+ * an elimination tree deeper than about 419,000 returns NWCCH_ERR_CAPACITY;
+ * deeper trees just run fewer queries at a time. The first call on a device
+ * looks up the scratch's device address (make it before any stream capture).
+ * All calls on a device share the scratch: calls that overlap on the GPU
+ * (other streams, other threads) race and must be serialized by the caller.
+ * Synchronous; same results as nwcch_query_batch. */
+int nwcch_query_batch_noalloc(nwcch_topology* t, const int32_t* up_dev, const int32_t* dn_dev,
+                              const int32_t* s_rank_dev, const int32_t* t_rank_dev, int64_t nq,
+                              int64_t* dist_dev, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -10,6 +10,7 @@
 // heads, no conflicts); the warp walks the chain in order.
 
 #include <algorithm>
+#include <mutex>
 
 #include "common.cuh"
 #include "topology.h"
@@ -125,4 +126,72 @@ extern "C" int nwcch_query_batch_i64(nwcch_topology* t, const int64_t* up_dev, c
         return NWCCH_ERR_ARG;
     if (nq == 0) return NWCCH_OK;
     return query_plain<int64_t>(t, up_dev, dn_dev, s_rank_dev, t_rank_dev, nq, dist_dev, (cudaStream_t)stream);
+}
+
+// ---------------------------------------------------------------------------
+// Allocation-free query entry point.
+//
+// nwcch_query_batch takes its per-warp label scratch from cudaMallocAsync.
+// Some callers cannot allocate at all: a serving loop whose admission control
+// has already handed every byte of device memory to resident metrics, an
+// embedding application whose own allocator owns the device and forbids
+// direct CUDA allocations, or a latency-critical path that must not risk an
+// allocator call stalling behind other work. nwcch_query_batch_noalloc serves
+// them: the same query kernel, with its scratch in the fixed array below,
+// which every GPU that loads this library holds until the process exits.
+
+namespace nwcch {
+
+// 32 MiB of label scratch, shared by every call on a device.
+constexpr int64_t kStaticQueryWords = (int64_t)4 << 20;
+static __device__ __align__(256) int64_t g_query_scratch[kStaticQueryWords];
+
+namespace {
+std::mutex g_scratch_mu;
+int64_t* g_scratch_addr[256];  // device address of g_query_scratch, per device
+}  // namespace
+
+// The host cannot name a __device__ array directly (its host-side symbol is
+// only a stand-in), so its device address is looked up once per device, with
+// that device current, and cached.
+static int static_query_scratch(int64_t** out) {
+    int dev = 0;
+    NWCCH_CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 256) return NWCCH_ERR_ARG;
+    std::lock_guard<std::mutex> lock(g_scratch_mu);
+    if (!g_scratch_addr[dev]) {
+        void* p = nullptr;
+        if (cudaGetSymbolAddress(&p, g_query_scratch) != cudaSuccess || !p) return NWCCH_ERR_CUDA;
+        g_scratch_addr[dev] = static_cast<int64_t*>(p);
+    }
+    *out = g_scratch_addr[dev];
+    return NWCCH_OK;
+}
+
+}  // namespace nwcch
+
+extern "C" int nwcch_query_batch_noalloc(nwcch_topology* t, const int32_t* up_dev, const int32_t* dn_dev,
+                                         const int32_t* s_rank_dev, const int32_t* t_rank_dev, int64_t nq,
+                                         int64_t* dist_dev, void* stream) {
+    if (!t || nq < 0 || (nq > 0 && (!up_dev || !dn_dev || !s_rank_dev || !t_rank_dev || !dist_dev)))
+        return NWCCH_ERR_ARG;
+    if (nq == 0) return NWCCH_OK;
+    const int64_t Dp = t->d.max_depth + 1;
+    const int64_t per_warp = 2 * Dp + (Dp + 1) / 2 + 1;  // int64 words: F, R, chain
+    const int block = 128, warps_per_block = block / 32;
+    // whole blocks of warps must fit in the fixed scratch
+    const int64_t max_blocks = kStaticQueryWords / (per_warp * warps_per_block);
+    if (max_blocks < 1) return NWCCH_ERR_CAPACITY;  // elimination tree too deep for the fixed scratch
+    int64_t* scratch = nullptr;
+    const int rc = static_query_scratch(&scratch);
+    if (rc) return rc;
+    const int64_t want_blocks = (std::min<int64_t>(nq, 152 * 32) + warps_per_block - 1) / warps_per_block;
+    const int64_t blocks = std::min(want_blocks, max_blocks);
+    cudaStream_t s = (cudaStream_t)stream;
+    // no state in the scratch survives between queries: every label and chain
+    // slot a query reads it writes first, so nothing needs clearing
+    k_query_plain<int32_t><<<(unsigned)blocks, block, 0, s>>>(t->d, up_dev, dn_dev, s_rank_dev, t_rank_dev, nq,
+                                                             dist_dev, scratch, t->err);
+    NWCCH_CUDA_TRY(cudaGetLastError());
+    return consume_error(t, s);
 }
