@@ -152,6 +152,10 @@ int nwcch_negative_cycle_arcs(nwcch_topology* t, const int32_t* up_dev, const in
 /* int64 storage (python/cch_nb.py:566-572). */
 int nwcch_negative_cycle_arcs_i64(nwcch_topology* t, const int64_t* up_dev, const int64_t* dn_dev,
                                   int64_t* count, void* stream);
+/* Enqueue-only form (int32 storage): the count lands in count_dev (one
+ * int64 of device memory) in stream order (python/cch_nb.py:566-572). */
+int nwcch_negative_cycle_arcs_async(nwcch_topology* t, const int32_t* up_dev, const int32_t* dn_dev,
+                                    int64_t* count_dev, void* stream);
 
 /* Number of self-loop original arcs with a negative weight (loops never
  * enter the contracted graph). Replaces CCH._negative_loop
@@ -190,6 +194,21 @@ int nwcch_query_batch(nwcch_topology* t, const int32_t* up_dev, const int32_t* d
 int nwcch_query_batch_i64(nwcch_topology* t, const int64_t* up_dev, const int64_t* dn_dev,
                           const int32_t* s_rank_dev, const int32_t* t_rank_dev, int64_t nq,
                           int64_t* dist_dev, void* stream);
+/* Enqueue-only batch (python/cch_nb.py:577-615), for CUDA-graph capture and
+ * pipelines: labels in shared memory, no allocation, no synchronization
+ * (argument errors in the rank arrays surface at nwcch_check). Returns
+ * NWCCH_ERR_CAPACITY when the elimination tree is too deep for shared-memory
+ * labels (about 10,000 levels); nwcch_query_batch then falls back to the
+ * plain kernel. */
+int nwcch_query_batch_async(nwcch_topology* t, const int32_t* up_dev, const int32_t* dn_dev,
+                            const int32_t* s_rank_dev, const int32_t* t_rank_dev, int64_t nq,
+                            int64_t* dist_dev, void* stream);
+/* The plain per-query form (one warp per query, one ancestor at a time,
+ * labels in global scratch): the same sweeps as Query::run
+ * (cpp/cch.cpp:549-575), kept as the baseline of the batched form. */
+int nwcch_query_batch_plain(nwcch_topology* t, const int32_t* up_dev, const int32_t* dn_dev,
+                            const int32_t* s_rank_dev, const int32_t* t_rank_dev, int64_t nq,
+                            int64_t* dist_dev, void* stream);
 
 /* Allocation-free form of nwcch_query_batch (int32 storage); it has no
  * counterpart in the reference. For callers that must not allocate device

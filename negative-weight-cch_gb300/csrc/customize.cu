@@ -241,6 +241,17 @@ extern "C" int nwcch_negative_cycle_arcs_i64(nwcch_topology* t, const int64_t* u
     return negative_cycle_arcs<int64_t>(t, up_dev, dn_dev, count, (cudaStream_t)stream);
 }
 
+extern "C" int nwcch_negative_cycle_arcs_async(nwcch_topology* t, const int32_t* up_dev, const int32_t* dn_dev,
+                                               int64_t* count_dev, void* stream) {
+    if (!t || !up_dev || !dn_dev || !count_dev) return NWCCH_ERR_ARG;
+    cudaStream_t s = (cudaStream_t)stream;
+    NWCCH_CUDA_TRY(cudaMemsetAsync(count_dev, 0, sizeof(int64_t), s));
+    k_negcycle<int32_t><<<grid_for(t->d.m_plus, 256), 256, 0, s>>>(
+        up_dev, dn_dev, t->d.m_plus, reinterpret_cast<unsigned long long*>(count_dev));
+    NWCCH_CUDA_TRY(cudaGetLastError());
+    return NWCCH_OK;
+}
+
 extern "C" int nwcch_negative_loops(nwcch_topology* t, const int32_t* w_dev, int64_t* count, void* stream) {
     if (!t || !count || (t->nloops > 0 && !w_dev)) return NWCCH_ERR_ARG;
     *count = 0;

@@ -17,6 +17,8 @@
 
 #include <algorithm>
 #include <atomic>
+#include <chrono>
+#include <cstdio>
 #include <condition_variable>
 #include <cstdint>
 #include <cstdlib>
@@ -314,7 +316,17 @@ class Dissector {
     const int32_t* nbr_;
     const double *x_, *y_;
     int64_t leaf_;
-    int64_t band_min_ = 250000;
+    int64_t band_min_ = env_int("NWCCH_ND_BAND_MIN", 20000);
+    int64_t band_div_ = env_int("NWCCH_ND_BAND_DIV", 100);
+    // the middle-half band is also tried on cells up to this size (smaller
+    // on huge graphs, where the narrow band alone keeps the order fast)
+    int64_t wide_max_ = env_int("NWCCH_ND_WIDE_MAX", n_ <= 2000000 ? 300000 : 60000);
+    bool verbose_ = env_int("NWCCH_ND_VERBOSE", 0) != 0;
+
+    static int64_t env_int(const char* name, int64_t dflt) {
+        const char* v = getenv(name);
+        return v ? atoll(v) : dflt;
+    }
     int threads_;
     std::unique_ptr<std::atomic<int64_t>[]> owner_;  // cell stamp currently holding a vertex
     vector<int32_t> local_;               // local id inside that cell
@@ -404,19 +416,27 @@ class Dissector {
         g.edges = e;
     }
 
-    CutResult flow_cut(const Cell& c, const LocalGraph& g, int dir) const {
+    // Band of the projection's middle in which a cut is searched: inertial
+    // flow's middle half (sources and sinks the first and last quarter), or a
+    // narrow band (m / band_div_, at least band_min_ vertices) that bounds the
+    // flow work on big cells and forces balanced halves.
+    int64_t narrow_band(int64_t m) const {
+        if (m <= band_min_ * 2) return m / 2;
+        return std::max<int64_t>(band_min_, m / std::max<int64_t>(2, band_div_));
+    }
+
+    CutResult flow_cut(const Cell& c, const LocalGraph& g, int dir, int64_t band) const {
         const int32_t m = g.m;
+        const int32_t k = std::max<int32_t>(1, (int32_t)((m - band) / 2));
+        // only the k lowest and k highest projections matter: two selections
+        // instead of a sort (ties broken by local id, so the result is fixed)
+        vector<double> kv(m);
+        for (int32_t i = 0; i < m; i++) kv[i] = key(c.verts[i], dir);
+        const auto less = [&](int32_t a, int32_t b) { return kv[a] < kv[b] || (kv[a] == kv[b] && a < b); };
         vector<int32_t> perm(m);
         std::iota(perm.begin(), perm.end(), 0);
-        std::stable_sort(perm.begin(), perm.end(), [&](int32_t a, int32_t b) {
-            return key(c.verts[a], dir) < key(c.verts[b], dir);
-        });
-        // inertial flow takes the first and last quarter as sources and sinks;
-        // on very large cells the cut is searched in a narrower middle band
-        // (10% of the cell, at least band_min_ vertices) to bound the flow work
-        int64_t band = m / 2;
-        if (m > band_min_ * 2) band = std::max<int64_t>(band_min_, m / 10);
-        const int32_t k = std::max<int32_t>(1, (int32_t)((m - band) / 2));
+        std::nth_element(perm.begin(), perm.begin() + k, perm.end(), less);
+        std::nth_element(perm.begin() + k, perm.end() - k, perm.end(), less);
         vector<int8_t> role(m, NORMAL);
         for (int32_t i = 0; i < k; i++) {
             role[perm[i]] = SOURCE;
@@ -476,26 +496,45 @@ class Dissector {
             return;
         }
         const int64_t stamp = ++stamp_;
+        const auto t_start = std::chrono::steady_clock::now();
         LocalGraph g;
         build_local(c, stamp, g);
         CutResult best;
         int64_t best_sep = -1, best_bal = 0;
-        CutResult cuts[4];
+        // candidates: 4 directions x (narrow band, and the middle half on
+        // cells small enough for it)
+        vector<std::pair<int, int64_t>> cand;
+        for (int d = 0; d < 4; d++) cand.push_back({d, narrow_band(m)});
+        if (m <= wide_max_ && narrow_band(m) != m / 2)
+            for (int d = 0; d < 4; d++) cand.push_back({d, m / 2});
+        vector<CutResult> cuts(cand.size());
         if (m >= 20000 && threads_ > 1) {
             vector<std::thread> ts;
-            for (int d = 0; d < 4; d++) ts.emplace_back([&, d] { cuts[d] = flow_cut(c, g, d); });
+            for (size_t i = 0; i < cand.size(); i++)
+                ts.emplace_back([&, i] { cuts[i] = flow_cut(c, g, cand[i].first, cand[i].second); });
             for (auto& t : ts) t.join();
         } else {
-            for (int d = 0; d < 4; d++) cuts[d] = flow_cut(c, g, d);
+            for (size_t i = 0; i < cand.size(); i++) cuts[i] = flow_cut(c, g, cand[i].first, cand[i].second);
         }
-        for (int d = 0; d < 4; d++) {
-            if (!cuts[d].ok) continue;
-            const int64_t ns = (int64_t)cuts[d].sep.size();
-            const int64_t bal = std::llabs((int64_t)cuts[d].a.size() - (int64_t)cuts[d].b.size());
-            if (best_sep < 0 || ns < best_sep || (ns == best_sep && bal < best_bal)) {
+        if (verbose_ && m >= 100000) {
+            const double secs =
+                std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
+            fprintf(stderr, "[nd] cell %lld: %.2fs, %zu candidates\n", (long long)m, secs, cand.size());
+        }
+        // smallest separator per vertex of the smaller half (ties: smaller
+        // separator, then better balance)
+        double best_ratio = 0;
+        for (size_t i = 0; i < cuts.size(); i++) {
+            if (!cuts[i].ok) continue;
+            const int64_t ns = (int64_t)cuts[i].sep.size();
+            const int64_t na = (int64_t)cuts[i].a.size(), nb = (int64_t)cuts[i].b.size();
+            const int64_t bal = std::llabs(na - nb);
+            const double ratio = (double)ns / (double)(std::min(na, nb) + 1);
+            if (best_sep < 0 || ratio < best_ratio || (ratio == best_ratio && (ns < best_sep || (ns == best_sep && bal < best_bal)))) {
+                best_ratio = ratio;
                 best_sep = ns;
                 best_bal = bal;
-                best = std::move(cuts[d]);
+                best = std::move(cuts[i]);
             }
         }
         if (best_sep < 0) best = geometric_cut(c, g);

@@ -13,6 +13,7 @@
 #include <mutex>
 
 #include "common.cuh"
+#include "supernodal.h"
 #include "topology.h"
 
 namespace nwcch {
@@ -116,6 +117,33 @@ extern "C" int nwcch_query_batch(nwcch_topology* t, const int32_t* up_dev, const
     if (!t || nq < 0 || (nq > 0 && (!up_dev || !dn_dev || !s_rank_dev || !t_rank_dev || !dist_dev)))
         return NWCCH_ERR_ARG;
     if (nq == 0) return NWCCH_OK;
+    bool used = false;
+    const int rc = query_sn_async<int32_t>(t, up_dev, dn_dev, s_rank_dev, t_rank_dev, nq, dist_dev,
+                                           (cudaStream_t)stream, &used);
+    if (rc) return rc;
+    if (used) return consume_error(t, (cudaStream_t)stream);
+    return query_plain<int32_t>(t, up_dev, dn_dev, s_rank_dev, t_rank_dev, nq, dist_dev, (cudaStream_t)stream);
+}
+
+extern "C" int nwcch_query_batch_async(nwcch_topology* t, const int32_t* up_dev, const int32_t* dn_dev,
+                                       const int32_t* s_rank_dev, const int32_t* t_rank_dev, int64_t nq,
+                                       int64_t* dist_dev, void* stream) {
+    if (!t || nq < 0 || (nq > 0 && (!up_dev || !dn_dev || !s_rank_dev || !t_rank_dev || !dist_dev)))
+        return NWCCH_ERR_ARG;
+    if (nq == 0) return NWCCH_OK;
+    bool used = false;
+    const int rc = query_sn_async<int32_t>(t, up_dev, dn_dev, s_rank_dev, t_rank_dev, nq, dist_dev,
+                                           (cudaStream_t)stream, &used);
+    if (rc || used) return rc;
+    return NWCCH_ERR_CAPACITY;  // elimination tree too deep for the shared-memory labels
+}
+
+extern "C" int nwcch_query_batch_plain(nwcch_topology* t, const int32_t* up_dev, const int32_t* dn_dev,
+                                       const int32_t* s_rank_dev, const int32_t* t_rank_dev, int64_t nq,
+                                       int64_t* dist_dev, void* stream) {
+    if (!t || nq < 0 || (nq > 0 && (!up_dev || !dn_dev || !s_rank_dev || !t_rank_dev || !dist_dev)))
+        return NWCCH_ERR_ARG;
+    if (nq == 0) return NWCCH_OK;
     return query_plain<int32_t>(t, up_dev, dn_dev, s_rank_dev, t_rank_dev, nq, dist_dev, (cudaStream_t)stream);
 }
 
@@ -125,6 +153,11 @@ extern "C" int nwcch_query_batch_i64(nwcch_topology* t, const int64_t* up_dev, c
     if (!t || nq < 0 || (nq > 0 && (!up_dev || !dn_dev || !s_rank_dev || !t_rank_dev || !dist_dev)))
         return NWCCH_ERR_ARG;
     if (nq == 0) return NWCCH_OK;
+    bool used = false;
+    const int rc = query_sn_async<int64_t>(t, up_dev, dn_dev, s_rank_dev, t_rank_dev, nq, dist_dev,
+                                           (cudaStream_t)stream, &used);
+    if (rc) return rc;
+    if (used) return consume_error(t, (cudaStream_t)stream);
     return query_plain<int64_t>(t, up_dev, dn_dev, s_rank_dev, t_rank_dev, nq, dist_dev, (cudaStream_t)stream);
 }
 

@@ -206,15 +206,15 @@ SnPlan* build_supernodal_plan(int64_t n, const int64_t* first, const int32_t* he
         add(SN_OUT_BIG, l, 0, out_big[l]);
     }
     P->items = (int64_t)items.size() / 3;
-    int32_t *d_s0, *d_k, *d_b, *d_rel;
+    int32_t *d_s0, *d_k, *d_b, *d_rel, *d_sid;
     int64_t* d_rel_off;
     if ((*rc = upload_vec(P, s0v, &d_s0)) || (*rc = upload_vec(P, kv, &d_k)) || (*rc = upload_vec(P, bv, &d_b)) ||
         (*rc = upload_vec(P, rel_off, &d_rel_off)) || (*rc = upload_vec(P, rel, &d_rel)) ||
-        (*rc = upload_vec(P, items, &P->d_items))) {
+        (*rc = upload_vec(P, items, &P->d_items)) || (*rc = upload_vec(P, sid, &d_sid))) {
         free_supernodal_plan(P);
         return nullptr;
     }
-    P->dev = SnDev{d_s0, d_k, d_b, d_rel_off, d_rel};
+    P->dev = SnDev{d_s0, d_k, d_b, d_rel_off, d_rel, d_sid};
     return P;
 }
 

@@ -22,6 +22,7 @@ struct SnDev {
     const int32_t* b;        // [nsn]
     const int64_t* rel_off;  // [nsn] start of the supernode's outgoing arc ids
     const int32_t* rel;      // arc id of (B[p], B[q]) for p < q, packed upper triangle
+    const int32_t* sn_id;    // [n] supernode of every vertex
 };
 
 enum SnKind : int {
@@ -72,6 +73,12 @@ void free_supernodal_plan(SnPlan* p);
 // Enqueues a full customization on stream s (base values + every launch).
 template <class T>
 int run_supernodal(nwcch_topology* t, SnPlan* P, const int32_t* w, T* up, T* dn, cudaStream_t s);
+
+// Enqueues the supernodal query kernel (labels in shared memory); sets *used
+// to false, enqueuing nothing, when the elimination tree is too deep for it.
+template <class T>
+int query_sn_async(nwcch_topology* t, const T* up, const T* dn, const int32_t* s_rank, const int32_t* t_rank,
+                   int64_t nq, int64_t* dist, cudaStream_t s, bool* used);
 
 // The same through a CUDA graph captured once per (w, up, dn) binding and
 // replayed afterwards; when s is itself being captured the launches are

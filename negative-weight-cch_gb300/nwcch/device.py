@@ -31,6 +31,10 @@ for _name, _args in {
     "nwcch_customize_plain_async": [P, P, P, P, P],
     "nwcch_negative_cycle_arcs": [P, P, P, PI64, P],
     "nwcch_negative_cycle_arcs_i64": [P, P, P, PI64, P],
+    "nwcch_negative_cycle_arcs_async": [P, P, P, P, P],
+    "nwcch_query_batch_noalloc": [P, P, P, P, P, I64, P, P],
+    "nwcch_query_batch_async": [P, P, P, P, P, I64, P, P],
+    "nwcch_query_batch_plain": [P, P, P, P, P, I64, P, P],
     "nwcch_negative_loops": [P, P, PI64, P],
     "nwcch_update": [P, P, P, P, P, P, I64, P, P, P],
     "nwcch_update_i64": [P, P, P, P, P, P, I64, P, P, P],
@@ -215,6 +219,14 @@ class DeviceTopology:
                    "negative_cycle_arcs")
         return int(c.value)
 
+    def negative_cycle_arcs_async(self, m: Metric, out):
+        """Enqueue the scan; the count lands in `out` (int64 CUDA tensor)."""
+        if m.storage != "int32":
+            raise ValueError("the enqueue-only scan reads int32 storage")
+        _lib.check(_lib.lib().nwcch_negative_cycle_arcs_async(self.handle, m.up.data_ptr(), m.dn.data_ptr(),
+                                                              out.data_ptr(), _stream(self._torch)),
+                   "negative_cycle_arcs_async")
+
     def negative_loops(self, m: Metric) -> int:
         c = C.c_int64()
         _lib.check(_lib.lib().nwcch_negative_loops(self.handle, m.w.data_ptr(), C.byref(c), _stream(self._torch)),
@@ -247,8 +259,11 @@ class DeviceTopology:
         return int(stats[0])
 
     # ------------------------------------------------------------ queries
-    def query_batch(self, m: Metric, s_rank, t_rank):
-        """int64 device tensor of distances (INT64_MAX = unreachable)."""
+    def query_batch(self, m: Metric, s_rank, t_rank, method: str = "supernodal", out=None, sync: bool = True):
+        """int64 device tensor of distances (INT64_MAX = unreachable).
+        method "supernodal" (batched kernel, shared-memory labels) or "plain"
+        (one ancestor at a time, int32 storage only). sync=False only
+        enqueues (supernodal, int32)."""
         torch = self._torch
         lib = _lib.lib()
         s = torch.as_tensor(np.asarray(s_rank) if not isinstance(s_rank, torch.Tensor) else s_rank)
@@ -257,8 +272,18 @@ class DeviceTopology:
         t = t.to(device="cuda", dtype=torch.int32).contiguous()
         if s.numel() != t.numel():
             raise ValueError("s and t differ in length")
-        out = torch.empty(s.numel(), dtype=torch.int64, device="cuda")
-        fn = lib.nwcch_query_batch if m.storage == "int32" else lib.nwcch_query_batch_i64
+        if out is None:
+            out = torch.empty(s.numel(), dtype=torch.int64, device="cuda")
+        if method == "plain":
+            if m.storage != "int32":
+                raise ValueError("the plain query reads int32 storage")
+            fn = lib.nwcch_query_batch_plain
+        elif not sync:
+            if m.storage != "int32":
+                raise ValueError("the enqueue-only query reads int32 storage")
+            fn = lib.nwcch_query_batch_async
+        else:
+            fn = lib.nwcch_query_batch if m.storage == "int32" else lib.nwcch_query_batch_i64
         _status(fn(self.handle, m.up.data_ptr(), m.dn.data_ptr(), s.data_ptr(), t.data_ptr(), s.numel(),
                    out.data_ptr(), _stream(torch)), "query_batch")
         return out

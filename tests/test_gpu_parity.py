@@ -118,6 +118,33 @@ def test_delaunay_negative_cycles(gpu):
         assert m.saturated and T.negative_cycle_arcs(m) > 0
 
 
+@pytest.mark.parametrize("kind,n", [("delaunay", 40_000), ("road", 60_000)])
+def test_query_forms_agree(gpu, oracle, kind, n):
+    """Batched (supernodal, sync and enqueue-only) and plain queries give the
+    oracle's distances, with int32 and int64 storage."""
+    from nwcch import graphs as G
+    from nwcch import topology as TT
+    from nwcch.device import DeviceTopology
+    g = {"delaunay": G.delaunay, "road": G.road_like}[kind](n, seed=33)
+    top = TT.build_topology(g)
+    T = DeviceTopology.from_dict(top)
+    OT = oracle.Topo.from_dict(top)
+    oup, odn = oracle.customize(OT, g["w"])
+    s, t = G.random_pairs(g["n"], 4000, seed=8)
+    s, t = top["rank"][s], top["rank"][t]
+    s[:50] = t[:50]  # s == t as well
+    want = oracle.query_batch(OT, oup, odn, s, t)
+    m = T.customize(g["w"], "int32")
+    assert np.array_equal(T.query_batch(m, s, t).cpu().numpy(), want)
+    assert np.array_equal(T.query_batch(m, s, t, method="plain").cpu().numpy(), want)
+    out = T.query_batch(m, s, t, sync=False)
+    gpu.cuda.synchronize()
+    assert not T.check()
+    assert np.array_equal(out.cpu().numpy(), want)
+    m64 = T.customize(g["w"], "int64")
+    assert np.array_equal(T.query_batch(m64, s, t).cpu().numpy(), want)
+
+
 def test_large_weights_take_the_exact_path(gpu, oracle):
     """Weights near 2^27: sums leave the +-2^28 window of the DPX fast path,
     so blocks recompute exactly; results stay equal to the oracle."""
