@@ -220,15 +220,28 @@ def run_ours(args, W, world):
     neg_k = int(count.item())
     # the plain per-level form of the same customization
     plain_ms = []
-    plain = T.customize(w_dev, "int32", method="plain")
-    for _ in range(args.plain_steps):
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        T.customize(w_dev, "int32", out=plain, sync=False, method="plain")
-        e1.record(stream)
-        torch.cuda.synchronize()
-        plain_ms.append(e0.elapsed_time(e1))
-    same = bool(torch.equal(plain.up, metric.up) and torch.equal(plain.dn, metric.dn))
+    same = None
+    plain_steps = args.plain_steps if args.plain_steps >= 0 else (0 if T.n > 5_000_000 else 1)
+    if plain_steps:
+        plain = T.customize(w_dev, "int32", method="plain")
+        for _ in range(plain_steps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            T.customize(w_dev, "int32", out=plain, sync=False, method="plain")
+            e1.record(stream)
+            torch.cuda.synchronize()
+            plain_ms.append(e0.elapsed_time(e1))
+        same = bool(torch.equal(plain.up, metric.up) and torch.equal(plain.dn, metric.dn))
+        del plain
+    # the plain per-query form on the same batch (one ancestor at a time)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ref_d = T.query_batch(good, qs, qt)
+    e0.record(stream)
+    plain_d = T.query_batch(good, qs, qt, method="plain")
+    e1.record(stream)
+    torch.cuda.synchronize()
+    plain_q_ms = e0.elapsed_time(e1)
+    assert torch.equal(ref_d, plain_d), "batched and plain queries differ"
     # end to end through the public API: weights from pinned host memory,
     # customization, scan, count read back
     e2e_ms = []
@@ -249,7 +262,117 @@ def run_ours(args, W, world):
         T.query_batch(good, qs[i:i + 1], qt[i:i + 1])
         lat.append((time.perf_counter() - t0) * 1e6)
     return dict(T=T, cust_ms=cust_ms, q_ms=q_ms, wall=wall, plain_ms=plain_ms, plain_equal=same, e2e_ms=e2e_ms,
+                plain_q_ms=plain_q_ms,
                 lat_us=lat, clocks=clocks.summary(), neg=neg_k, saturated=bool(sat))
+
+
+def batched_bytes(n, m, m_plus, triangles, k, s_w=4):
+    """Per batched customization of k metrics: the topology (heads, first,
+    arc map) is read once, weights and up/dn once per metric."""
+    return (triangles * (4 * s_w * k + 4) + m_plus * (4 * s_w * k + 4) + 8 * (n + 1)
+            + m * (8 + 1 + 4 + 4 * k))
+
+
+def run_batch(args, Wd, K):
+    """K metrics of one topology customized in one batched launch sequence,
+    against K single customizations of the same metrics; then partial
+    re-customizations of 1, 100 and 1000 changed arcs, each checked equal to a
+    full recompute."""
+    import torch
+
+    from nwcch import graphs as G
+    from nwcch.device import DeviceTopology
+    g, top = Wd["g"], Wd["top"]
+    T = DeviceTopology.from_dict(top)
+    stream = torch.cuda.current_stream()
+    Wk = G.scaled_metrics(g, K, seed=11)
+    w_dev = torch.from_numpy(Wk).cuda()
+    b = T.customize_batch(w_dev)
+    counts = T.negative_cycle_arcs_batch(b)
+    torch.cuda.synchronize()
+    assert int(counts.sum()) == 0, "conservative metrics reported negative cycles"
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    fits_l2 = K * T.m_plus * 8 < 129e6
+
+    def timed(fn, steps):
+        out = []
+        for _ in range(steps):
+            if fits_l2:
+                flush.fill_(1)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            out.append(e0.elapsed_time(e1))
+        return out
+
+    def batch_step():
+        T.customize_batch(w_dev, out=b, sync=False)
+        T.negative_cycle_arcs_batch(b, out=counts)
+
+    w1 = torch.empty(T.m, dtype=torch.int32, device="cuda")
+    single = T.customize(w1.copy_(w_dev[0]), "int32")
+    c1 = torch.zeros(1, dtype=torch.int64, device="cuda")
+
+    def singles_step():
+        for k in range(K):
+            w1.copy_(w_dev[k])
+            T.customize(w1, "int32", out=single, sync=False)
+            T.negative_cycle_arcs_async(single, c1)
+
+    for _ in range(max(3, args.warmup)):
+        batch_step()
+        singles_step()
+    torch.cuda.synchronize()
+    batch_ms = timed(batch_step, max(3, args.steps))
+    singles_ms = timed(singles_step, 3)
+    assert not T.check()
+    # every metric of the batch equals its single customization
+    equal = True
+    for k in range(K):
+        T.customize(w1.copy_(w_dev[k]), "int32", out=single, sync=False)
+        equal &= bool(torch.equal(single.up, b.up[k]) and torch.equal(single.dn, b.dn[k]))
+    assert equal, "batched customization differs from single customization"
+    # partial re-customization of metric 0: new lengths L' in [1, 2L] keep the
+    # metric conservative (w' = w + L' - L)
+    rng = np.random.default_rng(5)
+    m0 = b.metric(0)
+    w_cur = Wk[0].astype(np.int64).copy()
+    L = g["L"].astype(np.int64)
+    full = T.customize(m0.w, "int32")
+    updates = {}
+    for size in (1, 100, 1000):
+        wall, dev_ms, ev = [], [], []
+        for rep in range(5):
+            idx = rng.choice(T.m, size=size, replace=False)
+            val = w_cur[idx] + rng.integers(1, 2 * L[idx] + 1) - L[idx]
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            t0 = time.perf_counter()
+            e0.record(stream)
+            ev.append(T.update(m0, idx, val))
+            e1.record(stream)
+            torch.cuda.synchronize()
+            wall.append((time.perf_counter() - t0) * 1000)
+            dev_ms.append(e0.elapsed_time(e1))
+            w_cur[idx] = val
+            T.customize(m0.w, "int32", out=full)
+            assert torch.equal(full.up, m0.up) and torch.equal(full.dn, m0.dn), "partial != full recompute"
+            assert m0.stats["changed_negative"] == 0
+        updates[str(size)] = {"ms_median": round(statistics.median(wall), 3),
+                              "device_ms_median": round(statistics.median(dev_ms), 3),
+                              "evaluated_median": int(statistics.median(ev)), "reps": 5,
+                              "equal_full_recompute": True}
+    bm = statistics.median(batch_ms)
+    B = batched_bytes(top["n"], top["e_arc"].size, T.m_plus, T.triangles, K)
+    return {"workload": Wd["name"], "metrics": K, "batch_ms": round(bm, 3), "ms_per_metric": round(bm / K, 4),
+            "singles_ms": round(statistics.median(singles_ms), 3),
+            "speedup_vs_singles": round(statistics.median(singles_ms) / bm, 2),
+            "equal_to_singles": equal, "achieved_gbs": round(B / (bm / 1000) / 1e9, 1),
+            "algorithmic_bytes": int(B),
+            "l2": "flushed between steps" if fits_l2 else "inputs larger than L2",
+            "partial_updates": updates}
 
 
 def cpu_baseline(W, budget_s: float):
@@ -277,7 +400,11 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default=os.environ.get("NWCCH_BENCH_WORKLOAD", "usa24m"), choices=list(WORKLOADS))
     ap.add_argument("--cpu-budget", type=float, default=20.0)
-    ap.add_argument("--plain-steps", type=int, default=1)
+    ap.add_argument("--batch-metrics", type=int, default=64,
+                    help="metrics of the batched customization (0: skip it)")
+    ap.add_argument("--batch-workload", default="delaunay264k", choices=list(WORKLOADS))
+    ap.add_argument("--plain-steps", type=int, default=-1,
+                    help="plain per-level customizations to time (-1: one, none above 5M vertices)")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -303,6 +430,11 @@ def main():
         torch.distributed.init_process_group("nccl")
     W = make_workload(args.workload, seed=0)
     R = run_ours(args, W, world)
+    batch = None
+    if args.batch_metrics > 0 and rank == 0:
+        Wd = W if args.batch_workload == args.workload else make_workload(args.batch_workload, seed=0)
+        batch = run_batch(args, Wd, args.batch_metrics)
+        log(f"batched: {batch}")
     wall = R["wall"]
     cust_total = sum(R["cust_ms"]) / 1000.0
     if world > 1:
@@ -337,6 +469,7 @@ def main():
         "plain_customize_ms": round(statistics.median(R["plain_ms"]), 3) if R["plain_ms"] else None,
         "plain_equals_supernodal": R["plain_equal"],
         "queries_per_s": round(nq / (qms / 1000) * world, 1), "query_batch_ms": round(qms, 4),
+        "plain_queries_per_s": round(nq / (R["plain_q_ms"] / 1000) * world, 1),
         "query_latency_us": {"p50": round(lat[len(lat) // 2], 2), "p99": round(lat[max(0, int(len(lat) * 0.99) - 1)], 2),
                              "mode": "one query per call, host-timed"},
         "e2e": {"value": round(statistics.median(R["e2e_ms"]), 4), "unit": "ms",
@@ -349,6 +482,7 @@ def main():
         "cpu_baseline": {"value": round(cb["value"], 3), "unit": "ms", "cores": cb["cores"], "kind": "port",
                          "sample": f"{cb['runs']} level-parallel customizations + scans of the same metric"},
         "clocks": R["clocks"],
+        "batched_customization": batch,
     }
     print(json.dumps(line), flush=True)
 

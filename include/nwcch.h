@@ -135,6 +135,19 @@ int nwcch_customize_i64(nwcch_topology* t, const int32_t* w_dev, int64_t* up_dev
                         void* stream);
 int nwcch_customize_i64_async(nwcch_topology* t, const int32_t* w_dev, int64_t* up_dev,
                               int64_t* dn_dev, void* stream);
+/* Batched customization of `metrics` metrics over one topology (vehicle or
+ * battery variants), in one launch sequence whose kernels take the metric
+ * as a grid dimension: w_dev is metrics x m (metric-major), up_dev/dn_dev
+ * metrics x m+. Same per-metric results as nwcch_customize
+ * (python/cch_nb.py:529-563 applied to every metric). 1 <= metrics <= 65535. */
+int nwcch_customize_batch(nwcch_topology* t, int64_t metrics, const int32_t* w_dev, int32_t* up_dev,
+                          int32_t* dn_dev, void* stream);
+int nwcch_customize_batch_async(nwcch_topology* t, int64_t metrics, const int32_t* w_dev, int32_t* up_dev,
+                                int32_t* dn_dev, void* stream);
+/* Negative-cycle counts of a batch: counts_dev[k] = arcs of metric k with
+ * up + dn < 0 (python/cch_nb.py:566-572), enqueue only. */
+int nwcch_negative_cycle_arcs_batch_async(nwcch_topology* t, int64_t metrics, const int32_t* up_dev,
+                                          const int32_t* dn_dev, int64_t* counts_dev, void* stream);
 /* The plain form of the same computation: one launch per elimination level,
  * a block per row pulling its lower triangles (the level structure of
  * CCH::levels / customize_parallel, cpp/cch.cpp:465-529). Same results; kept

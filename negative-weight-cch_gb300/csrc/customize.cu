@@ -37,6 +37,10 @@ __global__ void k_fill2(T* __restrict__ a, T* __restrict__ b, int64_t count, T v
 template <class T>
 __global__ void k_base(DevTopo D, const int32_t* __restrict__ w, T* __restrict__ up, T* __restrict__ dn,
                        int* __restrict__ err) {
+    // metric blockIdx.y of a metric-major batch (weights m apart, arcs m+ apart)
+    w += blockIdx.y * D.m;
+    up += blockIdx.y * D.m_plus;
+    dn += blockIdx.y * D.m_plus;
     int bad = 0;
     for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < D.m;
          k += (int64_t)gridDim.x * blockDim.x) {
@@ -120,6 +124,9 @@ __global__ void __launch_bounds__(128) k_pull_rows(DevTopo D, const int32_t* __r
 template <class T>
 __global__ void k_negcycle(const T* __restrict__ up, const T* __restrict__ dn, int64_t count,
                            unsigned long long* __restrict__ out) {
+    up += blockIdx.y * count;  // metric blockIdx.y of a metric-major batch
+    dn += blockIdx.y * count;
+    out += blockIdx.y;
     unsigned long long c = 0;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < count;
          i += (int64_t)gridDim.x * blockDim.x)
@@ -141,16 +148,17 @@ int grid_for(int64_t count, int block) {
 }
 
 template <class T>
-int base_init(nwcch_topology* t, const int32_t* w, T* up, T* dn, cudaStream_t s) {
+int base_init(nwcch_topology* t, const int32_t* w, T* up, T* dn, cudaStream_t s, int* err, int metrics) {
     const DevTopo& D = t->d;
-    k_fill2<T><<<grid_for(D.m_plus, 256), 256, 0, s>>>(up, dn, D.m_plus, Lim<T>::INF);
-    if (D.m > 0) k_base<T><<<grid_for(D.m, 256), 256, 0, s>>>(D, w, up, dn, t->err);
+    k_fill2<T><<<grid_for(D.m_plus * metrics, 256), 256, 0, s>>>(up, dn, D.m_plus * metrics, Lim<T>::INF);
+    if (D.m > 0) k_base<T><<<dim3(grid_for(D.m, 256), metrics), 256, 0, s>>>(D, w, up, dn, err);
     return cudaGetLastError() == cudaSuccess ? NWCCH_OK : NWCCH_ERR_CUDA;
 }
 
 template <class T>
 int customize_plain(nwcch_topology* t, const int32_t* w, T* up, T* dn, cudaStream_t s) {
-    int rc = base_init<T>(t, w, up, dn, s);
+    int* err = stream_slot(t, s).err;
+    int rc = base_init<T>(t, w, up, dn, s, err);
     if (rc) return rc;
     const int max_smem = 227 * 1024;
     NWCCH_CUDA_TRY(cudaFuncSetAttribute(k_pull_rows<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
@@ -159,25 +167,26 @@ int customize_plain(nwcch_topology* t, const int32_t* w, T* up, T* dn, cudaStrea
         const int64_t v0 = t->level_off[l], nv = t->level_off[l + 1] - v0;
         const size_t smem = (2 * sizeof(T) + sizeof(int32_t)) * (size_t)t->level_maxdeg[l];
         if (smem > (size_t)max_smem) return NWCCH_ERR_CAPACITY;
-        k_pull_rows<T><<<(unsigned)nv, 128, smem, s>>>(t->d, t->level_verts + v0, up, dn, t->err);
+        k_pull_rows<T><<<(unsigned)nv, 128, smem, s>>>(t->d, t->level_verts + v0, up, dn, err);
     }
     return cudaGetLastError() == cudaSuccess ? NWCCH_OK : NWCCH_ERR_CUDA;
 }
 
 template <class T>
 int negative_cycle_arcs(nwcch_topology* t, const T* up, const T* dn, int64_t* count, cudaStream_t s) {
-    NWCCH_CUDA_TRY(cudaMemsetAsync(t->counters, 0, sizeof(unsigned long long), s));
-    k_negcycle<T><<<grid_for(t->d.m_plus, 256), 256, 0, s>>>(up, dn, t->d.m_plus, t->counters);
+    unsigned long long* c = stream_slot(t, s).counters;
+    NWCCH_CUDA_TRY(cudaMemsetAsync(c, 0, sizeof(unsigned long long), s));
+    k_negcycle<T><<<grid_for(t->d.m_plus, 256), 256, 0, s>>>(up, dn, t->d.m_plus, c);
     NWCCH_CUDA_TRY(cudaGetLastError());
     unsigned long long h = 0;
-    NWCCH_CUDA_TRY(cudaMemcpyAsync(&h, t->counters, sizeof(h), cudaMemcpyDeviceToHost, s));
+    NWCCH_CUDA_TRY(cudaMemcpyAsync(&h, c, sizeof(h), cudaMemcpyDeviceToHost, s));
     NWCCH_CUDA_TRY(cudaStreamSynchronize(s));
     *count = (int64_t)h;
     return NWCCH_OK;
 }
 
-template int base_init<int32_t>(nwcch_topology*, const int32_t*, int32_t*, int32_t*, cudaStream_t);
-template int base_init<int64_t>(nwcch_topology*, const int32_t*, int64_t*, int64_t*, cudaStream_t);
+template int base_init<int32_t>(nwcch_topology*, const int32_t*, int32_t*, int32_t*, cudaStream_t, int*, int);
+template int base_init<int64_t>(nwcch_topology*, const int32_t*, int64_t*, int64_t*, cudaStream_t, int*, int);
 
 }  // namespace nwcch
 
@@ -241,6 +250,31 @@ extern "C" int nwcch_negative_cycle_arcs_i64(nwcch_topology* t, const int64_t* u
     return negative_cycle_arcs<int64_t>(t, up_dev, dn_dev, count, (cudaStream_t)stream);
 }
 
+extern "C" int nwcch_customize_batch_async(nwcch_topology* t, int64_t metrics, const int32_t* w_dev,
+                                           int32_t* up_dev, int32_t* dn_dev, void* stream) {
+    if (!t || metrics < 1 || metrics > 65535 || !up_dev || !dn_dev || (t->d.m > 0 && !w_dev)) return NWCCH_ERR_ARG;
+    return launch_supernodal<int32_t>(t, static_cast<SnPlan*>(t->sn_plan), w_dev, up_dev, dn_dev,
+                                      (cudaStream_t)stream, (int)metrics);
+}
+
+extern "C" int nwcch_customize_batch(nwcch_topology* t, int64_t metrics, const int32_t* w_dev, int32_t* up_dev,
+                                     int32_t* dn_dev, void* stream) {
+    const int rc = nwcch_customize_batch_async(t, metrics, w_dev, up_dev, dn_dev, stream);
+    if (rc) return rc;
+    return consume_error(t, (cudaStream_t)stream);
+}
+
+extern "C" int nwcch_negative_cycle_arcs_batch_async(nwcch_topology* t, int64_t metrics, const int32_t* up_dev,
+                                                     const int32_t* dn_dev, int64_t* counts_dev, void* stream) {
+    if (!t || metrics < 1 || metrics > 65535 || !up_dev || !dn_dev || !counts_dev) return NWCCH_ERR_ARG;
+    cudaStream_t s = (cudaStream_t)stream;
+    NWCCH_CUDA_TRY(cudaMemsetAsync(counts_dev, 0, sizeof(int64_t) * metrics, s));
+    k_negcycle<int32_t><<<dim3(grid_for(t->d.m_plus, 256), (unsigned)metrics), 256, 0, s>>>(
+        up_dev, dn_dev, t->d.m_plus, reinterpret_cast<unsigned long long*>(counts_dev));
+    NWCCH_CUDA_TRY(cudaGetLastError());
+    return NWCCH_OK;
+}
+
 extern "C" int nwcch_negative_cycle_arcs_async(nwcch_topology* t, const int32_t* up_dev, const int32_t* dn_dev,
                                                int64_t* count_dev, void* stream) {
     if (!t || !up_dev || !dn_dev || !count_dev) return NWCCH_ERR_ARG;
@@ -257,11 +291,12 @@ extern "C" int nwcch_negative_loops(nwcch_topology* t, const int32_t* w_dev, int
     *count = 0;
     if (t->nloops == 0) return NWCCH_OK;
     cudaStream_t s = (cudaStream_t)stream;
-    NWCCH_CUDA_TRY(cudaMemsetAsync(t->counters + 1, 0, sizeof(unsigned long long), s));
-    k_negloops<<<grid_for(t->nloops, 256), 256, 0, s>>>(t->loops, t->nloops, w_dev, t->counters + 1);
+    unsigned long long* c = stream_slot(t, s).counters + 1;
+    NWCCH_CUDA_TRY(cudaMemsetAsync(c, 0, sizeof(unsigned long long), s));
+    k_negloops<<<grid_for(t->nloops, 256), 256, 0, s>>>(t->loops, t->nloops, w_dev, c);
     NWCCH_CUDA_TRY(cudaGetLastError());
     unsigned long long h = 0;
-    NWCCH_CUDA_TRY(cudaMemcpyAsync(&h, t->counters + 1, sizeof(h), cudaMemcpyDeviceToHost, s));
+    NWCCH_CUDA_TRY(cudaMemcpyAsync(&h, c, sizeof(h), cudaMemcpyDeviceToHost, s));
     NWCCH_CUDA_TRY(cudaStreamSynchronize(s));
     *count = (int64_t)h;
     return NWCCH_OK;

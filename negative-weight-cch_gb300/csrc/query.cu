@@ -100,7 +100,7 @@ int query_plain(nwcch_topology* t, const T* up, const T* dn, const int32_t* s_ra
     void* scratch = nullptr;
     NWCCH_CUDA_TRY(cudaMallocAsync(&scratch, (size_t)(blocks * (block / 32)) * per_warp * sizeof(int64_t), s));
     k_query_plain<T><<<(unsigned)blocks, block, 0, s>>>(t->d, up, dn, s_rank, t_rank, nq, dist, (int64_t*)scratch,
-                                                       t->err);
+                                                       stream_slot(t, s).err);
     const cudaError_t launch = cudaGetLastError();
     NWCCH_CUDA_TRY(cudaFreeAsync(scratch, s));
     NWCCH_CUDA_TRY(launch);
@@ -119,7 +119,7 @@ extern "C" int nwcch_query_batch(nwcch_topology* t, const int32_t* up_dev, const
     if (nq == 0) return NWCCH_OK;
     bool used = false;
     const int rc = query_sn_async<int32_t>(t, up_dev, dn_dev, s_rank_dev, t_rank_dev, nq, dist_dev,
-                                           (cudaStream_t)stream, &used);
+                                           (cudaStream_t)stream, true, &used);
     if (rc) return rc;
     if (used) return consume_error(t, (cudaStream_t)stream);
     return query_plain<int32_t>(t, up_dev, dn_dev, s_rank_dev, t_rank_dev, nq, dist_dev, (cudaStream_t)stream);
@@ -133,7 +133,7 @@ extern "C" int nwcch_query_batch_async(nwcch_topology* t, const int32_t* up_dev,
     if (nq == 0) return NWCCH_OK;
     bool used = false;
     const int rc = query_sn_async<int32_t>(t, up_dev, dn_dev, s_rank_dev, t_rank_dev, nq, dist_dev,
-                                           (cudaStream_t)stream, &used);
+                                           (cudaStream_t)stream, false, &used);
     if (rc || used) return rc;
     return NWCCH_ERR_CAPACITY;  // elimination tree too deep for the shared-memory labels
 }
@@ -155,7 +155,7 @@ extern "C" int nwcch_query_batch_i64(nwcch_topology* t, const int64_t* up_dev, c
     if (nq == 0) return NWCCH_OK;
     bool used = false;
     const int rc = query_sn_async<int64_t>(t, up_dev, dn_dev, s_rank_dev, t_rank_dev, nq, dist_dev,
-                                           (cudaStream_t)stream, &used);
+                                           (cudaStream_t)stream, true, &used);
     if (rc) return rc;
     if (used) return consume_error(t, (cudaStream_t)stream);
     return query_plain<int64_t>(t, up_dev, dn_dev, s_rank_dev, t_rank_dev, nq, dist_dev, (cudaStream_t)stream);
@@ -224,7 +224,7 @@ extern "C" int nwcch_query_batch_noalloc(nwcch_topology* t, const int32_t* up_de
     // no state in the scratch survives between queries: every label and chain
     // slot a query reads it writes first, so nothing needs clearing
     k_query_plain<int32_t><<<(unsigned)blocks, block, 0, s>>>(t->d, up_dev, dn_dev, s_rank_dev, t_rank_dev, nq,
-                                                             dist_dev, scratch, t->err);
+                                                             dist_dev, scratch, stream_slot(t, s).err);
     NWCCH_CUDA_TRY(cudaGetLastError());
     return consume_error(t, s);
 }

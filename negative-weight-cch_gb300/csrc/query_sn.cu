@@ -14,6 +14,7 @@
 // Labels are indexed by chain position: depth(start) - depth(v).
 
 #include <algorithm>
+#include <cstdlib>
 
 #include "common.cuh"
 #include "supernodal.h"
@@ -217,19 +218,23 @@ __device__ void sn_sweep32(const DevTopo& D, const SnDev& S, const int32_t* __re
     }
 }
 
+// Labels live in shared memory, or - for trees so deep that shared memory
+// would leave only a few warps per SM - in a global scratch (`gscratch`,
+// 12 * (depth + 1) + 16 bytes per warp, L1/L2-resident while in use).
 __global__ void k_query_sn32(DevTopo D, SnDev S, const int32_t* __restrict__ up, const int32_t* __restrict__ dn,
                              const int32_t* __restrict__ s_rank, const int32_t* __restrict__ t_rank, int64_t nq,
                              int64_t* __restrict__ dist, const unsigned int* __restrict__ maxabs,
-                             int* __restrict__ err) {
+                             unsigned char* __restrict__ gscratch, int* __restrict__ err) {
     if (!small_labels(D, maxabs)) return;  // the 64-bit kernel answers this batch
     extern __shared__ __align__(16) unsigned char smraw[];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const int64_t Dp = D.max_depth + 1;
     const int64_t per_warp = ((12 * Dp + 16) + 15) & ~15LL;
-    int32_t* F = reinterpret_cast<int32_t*>(smraw + wib * per_warp);
+    const int64_t warp = blockIdx.x * (int64_t)(blockDim.x >> 5) + wib;
+    unsigned char* mine = gscratch ? gscratch + warp * per_warp : smraw + wib * per_warp;
+    int32_t* F = reinterpret_cast<int32_t*>(mine);
     int32_t* R = F + Dp;
     int32_t* chain = R + Dp;
-    const int64_t warp = blockIdx.x * (int64_t)(blockDim.x >> 5) + wib;
     const int64_t nwarps = (int64_t)gridDim.x * (blockDim.x >> 5);
     int e = 0;
     for (int64_t q = warp; q < nq; q += nwarps) {
@@ -334,13 +339,15 @@ static int launch_shape(K kernel, int warps, size_t smem, int64_t nq, int64_t* b
 
 template <class T>
 int query_sn_async(nwcch_topology* t, const T* up, const T* dn, const int32_t* s_rank, const int32_t* t_rank,
-                   int64_t nq, int64_t* dist, cudaStream_t s, bool* used) {
+                   int64_t nq, int64_t* dist, cudaStream_t s, bool allow_alloc, bool* used) {
     int w64 = 0;
     size_t smem64 = 0;
     *used = false;
     if (!t->sn_plan || !sn_query_shape(t, 20, &w64, &smem64)) return NWCCH_OK;
     const SnDev& S = static_cast<SnPlan*>(t->sn_plan)->dev;
-    unsigned int* maxabs = reinterpret_cast<unsigned int*>(t->counters + 3);
+    const StreamSlot slot = stream_slot(t, s);
+    unsigned int* maxabs = reinterpret_cast<unsigned int*>(slot.counters + 3);
+    int* err = slot.err;
     if (sizeof(T) == 4) {
         // 32-bit labels when the metric's values allow them (decided on the
         // device: each kernel returns at once when the batch is not its own)
@@ -348,30 +355,48 @@ int query_sn_async(nwcch_topology* t, const T* up, const T* dn, const int32_t* s
         k_maxabs<<<grid_for_queries(t->d.m_plus), 256, 0, s>>>(reinterpret_cast<const int32_t*>(up),
                                                                reinterpret_cast<const int32_t*>(dn), t->d.m_plus,
                                                                maxabs);
-        int w32 = 0;
-        size_t smem32 = 0;
-        if (sn_query_shape(t, 12, &w32, &smem32)) {
+        const int64_t Dp = t->d.max_depth + 1;
+        const int64_t per_warp = ((12 * Dp + 16) + 15) & ~15LL;
+        const auto* u32 = reinterpret_cast<const int32_t*>(up);
+        const auto* d32 = reinterpret_cast<const int32_t*>(dn);
+        const bool force_global = getenv("NWCCH_QUERY_GLOBAL_LABELS") != nullptr;  // for tests
+        if (allow_alloc && (force_global || per_warp > 8 * 1024)) {
+            // deep tree: labels in global scratch, occupancy set by registers
             int64_t blocks = 0;
-            int rc = launch_shape(k_query_sn32, w32, smem32, nq, &blocks);
+            int rc = launch_shape(k_query_sn32, 4, 0, nq, &blocks);
             if (rc) return rc;
-            k_query_sn32<<<(unsigned)blocks, 32 * w32, smem32, s>>>(t->d, S, reinterpret_cast<const int32_t*>(up),
-                                                                    reinterpret_cast<const int32_t*>(dn), s_rank,
-                                                                    t_rank, nq, dist, maxabs, t->err);
+            void* scratch = nullptr;
+            NWCCH_CUDA_TRY(cudaMallocAsync(&scratch, (size_t)(blocks * 4 * per_warp), s));
+            k_query_sn32<<<(unsigned)blocks, 128, 0, s>>>(t->d, S, u32, d32, s_rank, t_rank, nq, dist, maxabs,
+                                                          static_cast<unsigned char*>(scratch), err);
+            const cudaError_t launch = cudaGetLastError();
+            NWCCH_CUDA_TRY(cudaFreeAsync(scratch, s));
+            NWCCH_CUDA_TRY(launch);
+        } else {
+            int w32 = 0;
+            size_t smem32 = 0;
+            if (sn_query_shape(t, 12, &w32, &smem32)) {
+                int64_t blocks = 0;
+                int rc = launch_shape(k_query_sn32, w32, smem32, nq, &blocks);
+                if (rc) return rc;
+                k_query_sn32<<<(unsigned)blocks, 32 * w32, smem32, s>>>(t->d, S, u32, d32, s_rank, t_rank, nq, dist,
+                                                                        maxabs, nullptr, err);
+            }
         }
     }
     int64_t blocks = 0;
     int rc = launch_shape(k_query_sn<T>, w64, smem64, nq, &blocks);
     if (rc) return rc;
     k_query_sn<T><<<(unsigned)blocks, 32 * w64, smem64, s>>>(t->d, S, up, dn, s_rank, t_rank, nq, dist, maxabs,
-                                                             t->err);
+                                                             err);
     NWCCH_CUDA_TRY(cudaGetLastError());
     *used = true;
     return NWCCH_OK;
 }
 
 template int query_sn_async<int32_t>(nwcch_topology*, const int32_t*, const int32_t*, const int32_t*,
-                                     const int32_t*, int64_t, int64_t*, cudaStream_t, bool*);
+                                     const int32_t*, int64_t, int64_t*, cudaStream_t, bool, bool*);
 template int query_sn_async<int64_t>(nwcch_topology*, const int64_t*, const int64_t*, const int32_t*,
-                                     const int32_t*, int64_t, int64_t*, cudaStream_t, bool*);
+                                     const int32_t*, int64_t, int64_t*, cudaStream_t, bool, bool*);
 
 }  // namespace nwcch

@@ -182,6 +182,8 @@ __global__ void __launch_bounds__(CT) k_sn_panel(DevTopo D, SnDev S, const int32
                                                  T* __restrict__ up, T* __restrict__ dn, int* __restrict__ err) {
     using E = Exact<T>;
     __shared__ PanelSmem<T, CT> sm;
+    up += blockIdx.y * D.m_plus;  // metric blockIdx.y of a metric-major batch
+    dn += blockIdx.y * D.m_plus;
     const int32_t s = items[3 * blockIdx.x], ct = items[3 * blockIdx.x + 1];
     const int32_t s0 = S.s0[s], k = S.k[s], cols = k + S.b[s];
     const int i0 = panel * SN_P;
@@ -367,6 +369,8 @@ __global__ void __launch_bounds__((TILE / MT) * (TILE / MT))
     constexpr int CH = sizeof(T) == 4 ? 32 : 16;
     using E = Exact<T>;
     __shared__ TileSmem<T, TILE, CH> sm;
+    up += blockIdx.y * D.m_plus;  // metric blockIdx.y of a metric-major batch
+    dn += blockIdx.y * D.m_plus;
     const auto c = tile_ctx<T, TILE, MT, OUT>(S, items, panel);
     int e = 0;
     bool done = false;

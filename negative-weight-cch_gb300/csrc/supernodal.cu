@@ -226,8 +226,9 @@ SnPlan* build_supernodal_plan(int64_t n, const int64_t* first, const int32_t* he
 namespace nwcch {
 
 template <class T>
-int run_supernodal(nwcch_topology* t, SnPlan* P, const int32_t* w, T* up, T* dn, cudaStream_t s) {
-    int rc = base_init<T>(t, w, up, dn, s);
+int run_supernodal(nwcch_topology* t, SnPlan* P, const int32_t* w, T* up, T* dn, cudaStream_t s, int* err,
+                   int metrics) {
+    int rc = base_init<T>(t, w, up, dn, s, err, metrics);
     if (rc) return rc;
     const DevTopo& D = t->d;
     constexpr int CT = sizeof(T) == 4 ? 128 : 32;
@@ -235,16 +236,16 @@ int run_supernodal(nwcch_topology* t, SnPlan* P, const int32_t* w, T* up, T* dn,
         const int32_t* it = P->d_items + 3 * la.off;
         switch (la.kind) {
             case SN_PANEL:
-                k_sn_panel<T, CT><<<(unsigned)la.count, CT, 0, s>>>(D, P->dev, it, la.panel, up, dn, t->err);
+                k_sn_panel<T, CT><<<dim3((unsigned)la.count, metrics), CT, 0, s>>>(D, P->dev, it, la.panel, up, dn, err);
                 break;
             case SN_TRAIL:
-                k_sn_tile<T, 64, 4, false><<<(unsigned)la.count, 256, 0, s>>>(D, P->dev, it, la.panel, up, dn, t->err);
+                k_sn_tile<T, 64, 4, false><<<dim3((unsigned)la.count, metrics), 256, 0, s>>>(D, P->dev, it, la.panel, up, dn, err);
                 break;
             case SN_OUT_BIG:
-                k_sn_tile<T, 64, 4, true><<<(unsigned)la.count, 256, 0, s>>>(D, P->dev, it, 0, up, dn, t->err);
+                k_sn_tile<T, 64, 4, true><<<dim3((unsigned)la.count, metrics), 256, 0, s>>>(D, P->dev, it, 0, up, dn, err);
                 break;
             case SN_OUT_SMALL:
-                k_sn_tile<T, 16, 2, true><<<(unsigned)la.count, 64, 0, s>>>(D, P->dev, it, 0, up, dn, t->err);
+                k_sn_tile<T, 16, 2, true><<<dim3((unsigned)la.count, metrics), 64, 0, s>>>(D, P->dev, it, 0, up, dn, err);
                 break;
             default:
                 return NWCCH_ERR_TOPOLOGY;
@@ -254,23 +255,25 @@ int run_supernodal(nwcch_topology* t, SnPlan* P, const int32_t* w, T* up, T* dn,
 }
 
 template <class T>
-int launch_supernodal(nwcch_topology* t, SnPlan* P, const int32_t* w, T* up, T* dn, cudaStream_t s) {
+int launch_supernodal(nwcch_topology* t, SnPlan* P, const int32_t* w, T* up, T* dn, cudaStream_t s, int metrics) {
     static const bool no_graph = getenv("NWCCH_NO_GRAPH") != nullptr;
     cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
     NWCCH_CUDA_TRY(cudaStreamIsCapturing(s, &cap));
-    if (no_graph || cap != cudaStreamCaptureStatusNone) return run_supernodal<T>(t, P, w, up, dn, s);
+    int* err = stream_slot(t, s).err;
+    if (no_graph || cap != cudaStreamCaptureStatusNone) return run_supernodal<T>(t, P, w, up, dn, s, err, metrics);
     std::lock_guard<std::mutex> lock(P->graph_mu);
     const int storage = (int)sizeof(T);
     SnGraph* hit = nullptr;
     for (auto& g : P->graphs)
-        if (g.storage == storage && g.w == w && g.up == up && g.dn == dn) hit = &g;
+        if (g.storage == storage && g.metrics == metrics && g.err == err && g.w == w && g.up == up && g.dn == dn)
+            hit = &g;
     if (!hit) {
         cudaStream_t cs;
         NWCCH_CUDA_TRY(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
         cudaGraph_t graph = nullptr;
         int rc = NWCCH_OK;
         if (cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal) != cudaSuccess) rc = NWCCH_ERR_CUDA;
-        if (!rc) rc = run_supernodal<T>(t, P, w, up, dn, cs);
+        if (!rc) rc = run_supernodal<T>(t, P, w, up, dn, cs, err, metrics);
         if (cudaStreamEndCapture(cs, &graph) != cudaSuccess && !rc) rc = NWCCH_ERR_CUDA;
         cudaGraphExec_t exec = nullptr;
         if (!rc && cudaGraphInstantiate(&exec, graph, 0) != cudaSuccess) rc = NWCCH_ERR_CUDA;
@@ -283,7 +286,7 @@ int launch_supernodal(nwcch_topology* t, SnPlan* P, const int32_t* w, T* up, T* 
             cudaGraphExecDestroy(old->exec);
             P->graphs.erase(old);
         }
-        P->graphs.push_back(SnGraph{storage, w, up, dn, exec, 0});
+        P->graphs.push_back(SnGraph{storage, metrics, err, w, up, dn, exec, 0});
         hit = &P->graphs.back();
     }
     hit->last_use = ++P->graph_clock;
@@ -291,9 +294,11 @@ int launch_supernodal(nwcch_topology* t, SnPlan* P, const int32_t* w, T* up, T* 
     return NWCCH_OK;
 }
 
-template int launch_supernodal<int32_t>(nwcch_topology*, SnPlan*, const int32_t*, int32_t*, int32_t*, cudaStream_t);
-template int launch_supernodal<int64_t>(nwcch_topology*, SnPlan*, const int32_t*, int64_t*, int64_t*, cudaStream_t);
-template int run_supernodal<int32_t>(nwcch_topology*, SnPlan*, const int32_t*, int32_t*, int32_t*, cudaStream_t);
-template int run_supernodal<int64_t>(nwcch_topology*, SnPlan*, const int32_t*, int64_t*, int64_t*, cudaStream_t);
+template int launch_supernodal<int32_t>(nwcch_topology*, SnPlan*, const int32_t*, int32_t*, int32_t*, cudaStream_t, int);
+template int launch_supernodal<int64_t>(nwcch_topology*, SnPlan*, const int32_t*, int64_t*, int64_t*, cudaStream_t, int);
+template int run_supernodal<int32_t>(nwcch_topology*, SnPlan*, const int32_t*, int32_t*, int32_t*, cudaStream_t, int*,
+                                     int);
+template int run_supernodal<int64_t>(nwcch_topology*, SnPlan*, const int32_t*, int64_t*, int64_t*, cudaStream_t, int*,
+                                     int);
 
 }  // namespace nwcch

@@ -41,9 +41,11 @@ struct SnLaunch {
     int64_t count;  // items
 };
 
-// A captured customization for one (storage, w, up, dn) binding.
+// A captured customization for one (storage, metrics, w, up, dn, err) binding.
 struct SnGraph {
     int storage;
+    int metrics;
+    int* err;
     const void* w;
     void* up;
     void* dn;
@@ -70,20 +72,25 @@ struct SnPlan {
 SnPlan* build_supernodal_plan(int64_t n, const int64_t* first, const int32_t* head, const int32_t* parent, int* rc);
 void free_supernodal_plan(SnPlan* p);
 
-// Enqueues a full customization on stream s (base values + every launch).
+// Enqueues a full customization on stream s (base values + every launch) of
+// `metrics` metrics stored metric-major (w: metrics x m, up/dn: metrics x m+);
+// every launch gets the metric as its second grid dimension. Range errors go
+// to the device word err.
 template <class T>
-int run_supernodal(nwcch_topology* t, SnPlan* P, const int32_t* w, T* up, T* dn, cudaStream_t s);
+int run_supernodal(nwcch_topology* t, SnPlan* P, const int32_t* w, T* up, T* dn, cudaStream_t s, int* err,
+                   int metrics = 1);
 
 // Enqueues the supernodal query kernel (labels in shared memory); sets *used
 // to false, enqueuing nothing, when the elimination tree is too deep for it.
 template <class T>
 int query_sn_async(nwcch_topology* t, const T* up, const T* dn, const int32_t* s_rank, const int32_t* t_rank,
-                   int64_t nq, int64_t* dist, cudaStream_t s, bool* used);
+                   int64_t nq, int64_t* dist, cudaStream_t s, bool allow_alloc, bool* used);
 
 // The same through a CUDA graph captured once per (w, up, dn) binding and
-// replayed afterwards; when s is itself being captured the launches are
-// simply enqueued into the caller's capture.
+// error word (the slot of stream s) and replayed afterwards; when s is itself
+// being captured the launches are simply enqueued into the caller's capture.
 template <class T>
-int launch_supernodal(nwcch_topology* t, SnPlan* P, const int32_t* w, T* up, T* dn, cudaStream_t s);
+int launch_supernodal(nwcch_topology* t, SnPlan* P, const int32_t* w, T* up, T* dn, cudaStream_t s,
+                      int metrics = 1);
 
 }  // namespace nwcch

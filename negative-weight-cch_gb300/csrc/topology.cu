@@ -40,11 +40,24 @@ void release(nwcch_topology* t) {
 
 }  // namespace
 
+StreamSlot stream_slot(nwcch_topology* t, cudaStream_t stream) {
+    std::lock_guard<std::mutex> lock(t->slot_mu);
+    const size_t used = t->slot_stream.size();
+    for (size_t i = 0; i < used; i++)
+        if (t->slot_stream[i] == stream) return t->slots[i];
+    if (used < t->slots.size()) {
+        t->slot_stream.push_back(stream);
+        return t->slots[used];
+    }
+    return t->slots.back();
+}
+
 int consume_error(nwcch_topology* t, cudaStream_t stream) {
+    const StreamSlot slot = stream_slot(t, stream);
     int h = 0;
-    NWCCH_CUDA_TRY(cudaMemcpyAsync(&h, t->err, sizeof(int), cudaMemcpyDeviceToHost, stream));
+    NWCCH_CUDA_TRY(cudaMemcpyAsync(&h, slot.err, sizeof(int), cudaMemcpyDeviceToHost, stream));
     NWCCH_CUDA_TRY(cudaStreamSynchronize(stream));
-    if (h) NWCCH_CUDA_TRY(cudaMemsetAsync(t->err, 0, sizeof(int), stream));
+    if (h) NWCCH_CUDA_TRY(cudaMemsetAsync(slot.err, 0, sizeof(int), stream));
     if (h & ERR_TIMEOUT) return NWCCH_ERR_TIMEOUT;
     if (h & ERR_CAPACITY) return NWCCH_ERR_CAPACITY;
     if (h & ERR_TOPOLOGY) return NWCCH_ERR_TOPOLOGY;
@@ -197,12 +210,16 @@ extern "C" int nwcch_topology_create(int64_t n, const int64_t* first, const int3
         t->level_verts = p32;
         if ((rc = upload(t, t->level_arc_off.data(), t->level_arc_off.size(), &p64))) break;
         t->d_level_arc_off = p64;
-        const int zero = 0;
-        if ((rc = upload(t, &zero, 1, &p32))) break;
-        t->err = reinterpret_cast<int*>(p32);
-        const int64_t zeros[16] = {0};
-        if ((rc = upload(t, zeros, 16, &p64))) break;
-        t->counters = reinterpret_cast<unsigned long long*>(p64);
+        // per-stream slots: 256 bytes each, the error word first and the
+        // 16 counters from byte 128
+        const std::vector<int64_t> zeros((size_t)kStreamSlots * 32, 0);
+        if ((rc = upload(t, zeros.data(), zeros.size(), &p64))) break;
+        for (int i = 0; i < kStreamSlots; i++) {
+            StreamSlot slot;
+            slot.err = reinterpret_cast<int*>(p64 + 32 * i);
+            slot.counters = reinterpret_cast<unsigned long long*>(p64 + 32 * i + 16);
+            t->slots.push_back(slot);
+        }
     } while (false);
     if (rc != NWCCH_OK) {
         release(t);

@@ -30,6 +30,14 @@ struct DevTopo {
     const int32_t* aeidx;   // [...]     ... as original arc ids
 };
 
+// Device words private to the calls enqueued on one stream: the error word
+// and 16 scratch counters (scan results, query range flags). Calls on
+// different streams of one handle never share them, so they may overlap.
+struct StreamSlot {
+    int* err = nullptr;
+    unsigned long long* counters = nullptr;
+};
+
 }  // namespace nwcch
 
 struct nwcch_topology {
@@ -45,8 +53,9 @@ struct nwcch_topology {
     int32_t* level_verts = nullptr;           // device: vertices sorted by (level, rank)
     std::vector<int64_t> level_arc_off;       // [levels+1]: arcs bucketed by tail level
     int64_t* d_level_arc_off = nullptr;       // device copy
-    int* err = nullptr;                       // device error word
-    unsigned long long* counters = nullptr;   // device: 16 scratch counters (scan results)
+    std::mutex slot_mu;                       // guards the stream slot table
+    std::vector<cudaStream_t> slot_stream;    // stream bound to each slot in use
+    std::vector<nwcch::StreamSlot> slots;     // device words, preallocated at create
     std::vector<void*> allocations;           // every cudaMalloc of this handle
     size_t device_bytes = 0;
     void* sn_plan = nullptr;                  // nwcch::SnPlan (supernodal customization)
@@ -57,7 +66,15 @@ struct nwcch_topology {
 
 namespace nwcch {
 
-// Reads and clears the device error word (synchronizes `stream`).
+// Slots preallocated per handle (one per stream that enqueues work on it).
+constexpr int kStreamSlots = 64;
+
+// The slot of `stream` (bound on first use); error words of the calls on a
+// stream beyond the first kStreamSlots streams fall back to the last slot,
+// shared, which only merges their status reports.
+StreamSlot stream_slot(nwcch_topology* t, cudaStream_t stream);
+
+// Reads and clears the error word of `stream`'s slot (synchronizes `stream`).
 int consume_error(nwcch_topology* t, cudaStream_t stream);
 
 }  // namespace nwcch

@@ -351,7 +351,7 @@ int update(nwcch_topology* t, int32_t* w_dev, T* up_dev, T* dn_dev, const int64_
     A.levels = t->levels;
     A.k = kk;
     A.ws = *ws;
-    A.err = t->err;
+    A.err = stream_slot(t, s).err;
     void* args[] = {&A};
     const int blocks = sizeof(T) == 4 ? ws->blocks32 : ws->blocks64;
     NWCCH_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k_update<T>, dim3(blocks), dim3(256), args, 0, s));

@@ -32,6 +32,9 @@ for _name, _args in {
     "nwcch_negative_cycle_arcs": [P, P, P, PI64, P],
     "nwcch_negative_cycle_arcs_i64": [P, P, P, PI64, P],
     "nwcch_negative_cycle_arcs_async": [P, P, P, P, P],
+    "nwcch_customize_batch": [P, I64, P, P, P, P],
+    "nwcch_customize_batch_async": [P, I64, P, P, P, P],
+    "nwcch_negative_cycle_arcs_batch_async": [P, I64, P, P, P, P],
     "nwcch_query_batch_noalloc": [P, P, P, P, P, I64, P, P],
     "nwcch_query_batch_async": [P, P, P, P, P, I64, P, P],
     "nwcch_query_batch_plain": [P, P, P, P, P, I64, P, P],
@@ -113,6 +116,23 @@ class Metric:
             f[a == _lib.INF64] = np.inf
             out.append(f)
         return tuple(out)
+
+
+@dataclass
+class MetricBatch:
+    """K customized metrics of one topology, metric-major on the device."""
+    topo: "DeviceTopology"
+    w: object        # torch int32 [K, m]
+    up: object       # torch int32 [K, m+]
+    dn: object
+    saturated: bool = False
+
+    def __len__(self) -> int:
+        return int(self.up.shape[0])
+
+    def metric(self, k: int) -> Metric:
+        """Metric k as a view: queries and updates on it act on the batch."""
+        return Metric(self.topo, self.w[k], self.up[k], self.dn[k], saturated=self.saturated)
 
 
 class DeviceTopology:
@@ -206,6 +226,48 @@ class DeviceTopology:
             warnings.warn(f"customization ({storage}) saturated: some values left the storage range",
                           SaturationWarning, stacklevel=2)
         return m
+
+    def customize_batch(self, w, out: "MetricBatch | None" = None, sync: bool = True) -> "MetricBatch":
+        """Customizes K metrics of this topology at once (int32 storage).
+
+        w: K x m original weights (host array or device tensor). The result
+        keeps the K metrics metric-major in two K x m+ tensors; every row is
+        the metric nwcch_customize would produce for that row of w."""
+        torch = self._torch
+        if isinstance(w, torch.Tensor):
+            wt = w.to(device="cuda", dtype=torch.int32).contiguous()
+        else:
+            rows = [self.weights(r) for r in np.asarray(w).reshape(-1, self.m)]
+            wt = torch.stack(rows) if rows else torch.empty(0, self.m, dtype=torch.int32, device="cuda")
+        wt = wt.reshape(-1, self.m)
+        k = wt.shape[0]
+        if k < 1:
+            raise ValueError("need at least one metric")
+        if out is not None and tuple(out.up.shape) == (k, self.m_plus):
+            up, dn = out.up, out.dn
+        else:
+            up = torch.empty(k, self.m_plus, dtype=torch.int32, device="cuda")
+            dn = torch.empty(k, self.m_plus, dtype=torch.int32, device="cuda")
+        lib = _lib.lib()
+        fn = lib.nwcch_customize_batch if sync else lib.nwcch_customize_batch_async
+        sat = _status(fn(self.handle, k, wt.data_ptr(), up.data_ptr(), dn.data_ptr(), _stream(torch)),
+                      "customize_batch")
+        if sat:
+            warnings.warn("batched customization saturated: some values left the int32 range",
+                          SaturationWarning, stacklevel=2)
+        return MetricBatch(self, wt, up, dn, saturated=sat)
+
+    def negative_cycle_arcs_batch(self, b: "MetricBatch", out=None):
+        """Per-metric negative-cycle arc counts of a batch (int64 CUDA tensor
+        of K entries, enqueued on the current stream)."""
+        torch = self._torch
+        k = b.up.shape[0]
+        if out is None:
+            out = torch.empty(k, dtype=torch.int64, device="cuda")
+        _lib.check(_lib.lib().nwcch_negative_cycle_arcs_batch_async(self.handle, k, b.up.data_ptr(), b.dn.data_ptr(),
+                                                                    out.data_ptr(), _stream(torch)),
+                   "negative_cycle_arcs_batch")
+        return out
 
     def check(self) -> bool:
         """Status of asynchronous calls since the last check (True = saturated)."""

@@ -143,6 +143,13 @@ def test_query_forms_agree(gpu, oracle, kind, n):
     assert np.array_equal(out.cpu().numpy(), want)
     m64 = T.customize(g["w"], "int64")
     assert np.array_equal(T.query_batch(m64, s, t).cpu().numpy(), want)
+    # the deep-tree variant (labels in global scratch), forced
+    import os
+    os.environ["NWCCH_QUERY_GLOBAL_LABELS"] = "1"
+    try:
+        assert np.array_equal(T.query_batch(m, s, t).cpu().numpy(), want)
+    finally:
+        del os.environ["NWCCH_QUERY_GLOBAL_LABELS"]
 
 
 def test_large_weights_take_the_exact_path(gpu, oracle):
@@ -250,3 +257,53 @@ def test_cch_class_workflow(gpu, oracle):
         bf, neg = oracle.bellman_ford(g["n"], g["off"], g["tgt"], g["w"], int(s[i]))
         want = np.inf if bf[t[i]] == INF else float(bf[t[i]])
         assert d[i] == want
+
+
+def test_customize_batch(gpu, oracle):
+    """K metrics in one batched launch sequence equal K single customizations
+    and the oracle; per-metric scan counts; queries and partial updates on a
+    metric of the batch leave the other metrics untouched."""
+    from nwcch import graphs as G
+    from nwcch import topology as TT
+    from nwcch.device import DeviceTopology
+    g = G.delaunay(30_000, seed=17)
+    top = TT.build_topology(g)
+    T = DeviceTopology.from_dict(top)
+    OT = oracle.Topo.from_dict(top)
+    W = G.scaled_metrics(g, 6, seed=3)
+    neg, _ = G.inject_negative_triangle(dict(g, w=W[4].copy()), seed=2)
+    W[4] = neg["w"]
+    b = T.customize_batch(W)
+    assert len(b) == 6
+    counts = T.negative_cycle_arcs_batch(b).cpu().numpy()
+    for k in range(6):
+        m = T.customize(W[k], "int32")
+        up, dn = m.to_numpy()
+        bu, bd = b.metric(k).to_numpy()
+        assert np.array_equal(up, bu) and np.array_equal(dn, bd)
+        if k != 4:  # (metric 4 has a negative cycle: its values saturate)
+            oup, odn = oracle.customize(OT, W[k])
+            assert np.array_equal(up, oup) and np.array_equal(dn, odn)
+        assert counts[k] == T.negative_cycle_arcs(m)
+        assert (counts[k] > 0) == (k == 4)
+    # replay into the same buffers (captured launch graph reused)
+    b2 = T.customize_batch(W, out=b)
+    assert b2.up.data_ptr() == b.up.data_ptr()
+    for k in (0, 5):
+        assert np.array_equal(b.metric(k).to_numpy()[0], oracle.customize(OT, W[k])[0])
+    s, t = G.random_pairs(g["n"], 2000, seed=4)
+    s, t = top["rank"][s], top["rank"][t]
+    oup, odn = oracle.customize(OT, W[1])
+    assert np.array_equal(T.query_batch(b.metric(1), s, t).cpu().numpy(), oracle.query_batch(OT, oup, odn, s, t))
+    before = b.up.clone(), b.dn.clone()
+    rng = np.random.default_rng(1)
+    idx = rng.choice(T.m, size=100, replace=False)
+    w2 = W[2].copy()
+    val = (w2[idx] + 50).astype(np.int32)
+    T.update(b.metric(2), idx, val)
+    w2[idx] = val
+    fu, fd = T.customize(w2, "int32").to_numpy()
+    bu, bd = b.metric(2).to_numpy()
+    assert np.array_equal(fu, bu) and np.array_equal(fd, bd)
+    for k in (0, 1, 3, 4, 5):
+        assert gpu.equal(b.up[k], before[0][k]) and gpu.equal(b.dn[k], before[1][k])
