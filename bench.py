@@ -49,6 +49,8 @@ WORKLOADS = {
     "usa24m": dict(kind="road", n=24_000_000, arcs=58_333_344, queries=100_000, inject=True),
     # plain GPU configuration: 264k-vertex Delaunay graph
     "delaunay264k": dict(kind="delaunay", n=264_000, queries=10_000, inject=False),
+    # serving configuration: 1.1M-vertex Delaunay graph, 8 resident metrics
+    "delaunay1m": dict(kind="delaunay", n=1_100_000, queries=10_000, inject=False),
     # CPU configuration: 64x64 grid
     "grid64": dict(kind="grid", n=4096, queries=1_000, inject=False),
 }
@@ -335,18 +337,19 @@ def run_batch(args, Wd, K):
         equal &= bool(torch.equal(single.up, b.up[k]) and torch.equal(single.dn, b.dn[k]))
     assert equal, "batched customization differs from single customization"
     # partial re-customization of metric 0: new lengths L' in [1, 2L] keep the
-    # metric conservative (w' = w + L' - L)
+    # metric conservative (w' = height difference + L')
     rng = np.random.default_rng(5)
     m0 = b.metric(0)
     w_cur = Wk[0].astype(np.int64).copy()
     L = g["L"].astype(np.int64)
+    heights = w_cur - L  # w = length + height difference; lengths change, heights stay
     full = T.customize(m0.w, "int32")
     updates = {}
     for size in (1, 100, 1000):
         wall, dev_ms, ev = [], [], []
         for rep in range(5):
             idx = rng.choice(T.m, size=size, replace=False)
-            val = w_cur[idx] + rng.integers(1, 2 * L[idx] + 1) - L[idx]
+            val = heights[idx] + rng.integers(1, 2 * L[idx] + 1)
             torch.cuda.synchronize()
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             t0 = time.perf_counter()
@@ -373,6 +376,44 @@ def run_batch(args, Wd, K):
             "algorithmic_bytes": int(B),
             "l2": "flushed between steps" if fits_l2 else "inputs larger than L2",
             "partial_updates": updates}
+
+
+def run_serving(args, Ws, loads):
+    """8 resident metrics of one topology behind the serving loop: an open
+    Poisson stream of queries (uniform s, t, metric) at each offered load,
+    with update batches of 1-1000 arcs every 0.1 s on average; batched
+    (supernodal) against plain per-query kernels."""
+    from nwcch import graphs as G
+    from nwcch.device import DeviceTopology
+    from nwcch.serve import ServingLoop, poisson_trace, run_trace, summarize
+    g, top = Ws["g"], Ws["top"]
+    T = DeviceTopology.from_dict(top)
+    W8 = G.scaled_metrics(g, 8, seed=21)
+    keys = list(range(8))
+    runs = []
+    for method in ("supernodal", "plain"):
+        for rate in loads:
+            if method == "plain" and rate > 1e5:
+                continue  # the plain kernels saturate far below this load
+            duration = min(args.serve_seconds, 200_000 / rate)
+            shadow = {k: W8[k].copy() for k in keys}
+            trace = poisson_trace(T, keys, rate, duration, update_every=0.1, update_sizes=(1, 10, 100, 1000),
+                                  weights=shadow, L=g["L"], seed=int(rate) % 100_003)
+            with ServingLoop(T, method=method) as loop:
+                for k in keys:
+                    loop.add_metric(k, W8[k])
+                for b in [loop.submit_query(k, 0, 0) for k in keys]:  # admit + customize before the clock
+                    b.wait(300)
+                b0, q0 = loop.batches, loop.batched_queries
+                res = run_trace(loop, trace)
+                st = summarize(res)
+                nb = loop.batches - b0
+                st.update(method=method, offered_qps=rate, seconds=round(duration, 3), batches=nb,
+                          mean_batch=round((loop.batched_queries - q0) / max(1, nb), 1))
+            log(f"serving: {st}")
+            runs.append(st)
+    return {"workload": Ws["name"], "n": top["n"], "metrics": 8, "update_sizes": [1, 10, 100, 1000],
+            "updates_per_s": 10, "latency": "scheduled arrival to answer on the host", "runs": runs}
 
 
 def cpu_baseline(W, budget_s: float):
@@ -403,6 +444,9 @@ def main():
     ap.add_argument("--batch-metrics", type=int, default=64,
                     help="metrics of the batched customization (0: skip it)")
     ap.add_argument("--batch-workload", default="delaunay264k", choices=list(WORKLOADS))
+    ap.add_argument("--serve-workload", default="delaunay1m", choices=list(WORKLOADS) + ["none"])
+    ap.add_argument("--serve-loads", default="1e4,1e5,1e6", help="offered query loads (queries/s)")
+    ap.add_argument("--serve-seconds", type=float, default=1.0)
     ap.add_argument("--plain-steps", type=int, default=-1,
                     help="plain per-level customizations to time (-1: one, none above 5M vertices)")
     args = ap.parse_args()
@@ -430,11 +474,6 @@ def main():
         torch.distributed.init_process_group("nccl")
     W = make_workload(args.workload, seed=0)
     R = run_ours(args, W, world)
-    batch = None
-    if args.batch_metrics > 0 and rank == 0:
-        Wd = W if args.batch_workload == args.workload else make_workload(args.batch_workload, seed=0)
-        batch = run_batch(args, Wd, args.batch_metrics)
-        log(f"batched: {batch}")
     wall = R["wall"]
     cust_total = sum(R["cust_ms"]) / 1000.0
     if world > 1:
@@ -443,6 +482,17 @@ def main():
         cust_total, wall = float(t[0]), float(t[1])
     if rank != 0:
         return
+    # rank 0 only, after the timed replicas: the batched and serving sections
+    batch = serving = None
+    if args.batch_metrics > 0:
+        Wd = W if args.batch_workload == args.workload else make_workload(args.batch_workload, seed=0)
+        batch = run_batch(args, Wd, args.batch_metrics)
+        log(f"batched: {batch}")
+        del Wd
+    if args.serve_workload != "none":
+        Ws = W if args.serve_workload == args.workload else make_workload(args.serve_workload, seed=0)
+        serving = run_serving(args, Ws, [float(x) for x in args.serve_loads.split(",") if x])
+        del Ws
     T = R["T"]
     nq = int(W["qs"].size)
     qms = statistics.median(R["q_ms"])
@@ -483,6 +533,7 @@ def main():
                          "sample": f"{cb['runs']} level-parallel customizations + scans of the same metric"},
         "clocks": R["clocks"],
         "batched_customization": batch,
+        "serving": serving,
     }
     print(json.dumps(line), flush=True)
 

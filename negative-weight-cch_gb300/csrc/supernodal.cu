@@ -102,6 +102,7 @@ SnPlan* build_supernodal_plan(int64_t n, const int64_t* first, const int32_t* he
     }
     P->nsn = ns;
     P->levels = L;
+    for (int64_t s = 0; s < ns; s++) P->max_b = std::max(P->max_b, bv[s]);
     // arc ids of (B[p], B[q]) for every supernode, found by merging B's tail
     // into the row of B[p] (chordality puts it there)
     std::vector<int64_t> rel_off(ns + 1, 0);
@@ -280,7 +281,7 @@ int launch_supernodal(nwcch_topology* t, SnPlan* P, const int32_t* w, T* up, T* 
         if (graph) cudaGraphDestroy(graph);
         cudaStreamDestroy(cs);
         if (rc) return rc;
-        if (P->graphs.size() >= 8) {
+        if (P->graphs.size() >= 16) {
             auto old = std::min_element(P->graphs.begin(), P->graphs.end(),
                                         [](const SnGraph& a, const SnGraph& b) { return a.last_use < b.last_use; });
             cudaGraphExecDestroy(old->exec);

@@ -54,13 +54,14 @@ struct SnGraph {
 };
 
 struct SnPlan {
-    std::vector<SnGraph> graphs;  // small cache, most recently used kept
+    std::vector<SnGraph> graphs;  // up to 16, least recently used dropped first
     uint64_t graph_clock = 0;
     std::mutex graph_mu;
     int64_t nsn = 0;
     int32_t levels = 0;
     int64_t items = 0;
     int64_t rel_entries = 0;
+    int32_t max_b = 0;            // longest boundary of any supernode
     std::vector<SnLaunch> launches;
     SnDev dev{};
     int32_t* d_items = nullptr;

@@ -14,13 +14,30 @@
 // and a level ends with a grid barrier whose spin is bounded (on timeout the
 // kernel records ERR_TIMEOUT and every block returns). The kernel cleans its
 // workspace (queued flags, bucket counts, pending bits) before it exits.
+//
+// The level sweep pays a barrier per level and a row search per lower
+// triangle, so a change that spreads through the top separators costs more
+// than customizing from scratch. The sweep therefore runs under a budget
+// (about half the time of a full customization): past it, the sweep stops at
+// its next pending level L and the update is finished densely with the same
+// results and statistics: the whole metric is re-customized into scratch by
+// the supernodal kernels, the arcs whose values differ are the changed ones,
+// and an arc of level >= L counts as evaluated if it was queued before the
+// stop or one of its lower triangles has a changed side (the set the sweep
+// would have queued). Lower triangles are found through the supernode
+// layout: a triangle inside a supernode through its trapezoid columns, one
+// below it through the boundary pairs of a descendant supernode.
 
 #include <algorithm>
+#include <climits>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 #include <vector>
 
 #include "common.cuh"
+#include "customize.h"
+#include "supernodal.h"
 #include "topology.h"
 
 namespace nwcch {
@@ -35,8 +52,14 @@ struct UpdateWorkspace {
     int64_t* edge_idx = nullptr;      // [cap] staged changes
     int32_t* new_w = nullptr;         // [cap]
     int64_t cap = 0;
+    uint8_t* chg = nullptr;           // [m+]  arc changed in this update
+    uint8_t* dq = nullptr;            // [m+]  dense finish: a lower triangle has a changed side
+    uint8_t* acol = nullptr;          // [n]   dense finish: per supernode row, a changed arc above it
+    void* up2 = nullptr;              // [m+]  dense finish: full re-customization (8-byte slots)
+    void* dn2 = nullptr;
     // [0] evaluated [1] changed [2] changed with up+dn<0 [3] levels done
-    // [5] barrier arrivals [6] barrier generation
+    // [5] barrier arrivals [6] barrier generation [7] stop level + 1
+    // [8], [9] stop requests by level parity
     unsigned long long* stats = nullptr;
     int blocks32 = 0, blocks64 = 0;
 };
@@ -52,7 +75,17 @@ struct UpdateArgs {
     int64_t k;
     UpdateWorkspace ws;
     int* err;
+    long long budget_ns;  // sweep time before the dense finish (0: dense from the start)
+    int64_t max_arcs;     // evaluated arcs before the dense finish
 };
+
+static constexpr int kStatWords = 16;
+
+__device__ __forceinline__ unsigned long long globaltimer_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
 
 __device__ __forceinline__ int32_t ldcg(const int32_t* p) { return __ldcg(p); }
 __device__ __forceinline__ int64_t ldcg(const int64_t* p) {
@@ -120,6 +153,11 @@ __global__ void __launch_bounds__(256) k_update(UpdateArgs<T> A) {
     const int64_t gthreads = (int64_t)gridDim.x * blockDim.x;
     const int64_t gwarp = gtid >> 5, gwarps = gthreads >> 5;
     int e = 0;
+    unsigned long long t_start = 0;
+    if (gtid == 0) {
+        t_start = globaltimer_ns();
+        if (A.budget_ns <= 0) A.ws.stats[8] = 1;  // dense from the first level
+    }
     // 1. new weights (python/cch.py:357-360)
     for (int64_t j = gtid; j < A.k; j += gthreads) A.w[A.ws.edge_idx[j]] = A.ws.new_w[j];
     if (!grid_sync(A)) return;
@@ -132,7 +170,10 @@ __global__ void __launch_bounds__(256) k_update(UpdateArgs<T> A) {
     // 3. levels, lowest first (python/cch.py:376-401)
     __shared__ int32_t next_level;
     int32_t L = -1;
-    while (true) {
+    bool stopped = false;
+    // a stop request for iteration i is written during iteration i-1 into
+    // word 8 + (i & 1), so no block reads a word while it is being written
+    for (int iter = 0;; iter++) {
         if (threadIdx.x < 32) {
             int32_t found = -1;
             const int32_t words = (A.levels + 31) >> 5;
@@ -152,6 +193,24 @@ __global__ void __launch_bounds__(256) k_update(UpdateArgs<T> A) {
         __syncthreads();
         L = next_level;
         if (L < 0) break;
+        if (__ldcg(A.ws.stats + 8 + (iter & 1))) {
+            stopped = true;
+            if (gtid == 0) {
+                A.ws.stats[7] = (unsigned long long)L + 1;
+                // the pending levels from L up join the cleanup list
+                unsigned long long d = A.ws.stats[3];
+                for (int32_t wi = L >> 5; wi < ((A.levels + 31) >> 5); wi++) {
+                    uint32_t bits = __ldcg(A.ws.pending + wi);
+                    if (wi == (L >> 5)) bits &= ~((1u << (L & 31)) - 1u);
+                    while (bits) {
+                        A.ws.done_levels[d++] = wi * 32 + __ffs(bits) - 1;
+                        bits &= bits - 1;
+                    }
+                }
+                A.ws.stats[3] = d;
+            }
+            break;
+        }
         const int64_t base = A.level_arc_off[L];
         const int32_t cnt = __ldcg(A.ws.bcount + L);
         if (gtid == 0) {
@@ -188,6 +247,7 @@ __global__ void __launch_bounds__(256) k_update(UpdateArgs<T> A) {
             if (lane == 0) {
                 A.up[c] = nu;
                 A.dn[c] = nd;
+                A.ws.chg[c] = 1;
                 const unsigned long long p = atomicAdd(A.ws.stats + 1, 1ull);
                 A.ws.changed[p] = c;
                 if (negative_pair(nu, nd)) atomicAdd(A.ws.stats + 2, 1ull);
@@ -205,9 +265,19 @@ __global__ void __launch_bounds__(256) k_update(UpdateArgs<T> A) {
                 enqueue(A, (int32_t)r);
             }
         }
+        if (gtid == 0 && ((long long)(globaltimer_ns() - t_start) > A.budget_ns ||
+                          (long long)A.ws.stats[0] > A.max_arcs)) {
+            A.ws.stats[8 + ((iter + 1) & 1)] = 1;
+        }
         if (!grid_sync(A)) return;
     }
+    if (stopped) {  // the host finishes densely and cleans the workspace
+        if (e) atomicOr(A.err, e);
+        return;
+    }
     // 4. clean the workspace for the next call
+    const int64_t nchanged = (int64_t)__ldcg(A.ws.stats + 1);
+    for (int64_t j = gtid; j < nchanged; j += gthreads) A.ws.chg[__ldcg(A.ws.changed + j)] = 0;
     const int32_t nd_levels = (int32_t)__ldcg(A.ws.stats + 3);
     for (int32_t li = 0; li < nd_levels; li++) {
         const int32_t l = __ldcg(A.ws.done_levels + li);
@@ -224,8 +294,134 @@ __global__ void __launch_bounds__(256) k_update(UpdateArgs<T> A) {
     if (e) atomicOr(A.err, e);
 }
 
+// ---------------------------------------------------------------- dense finish
+
+// Arcs whose full re-customization differs are changed: new values written,
+// appended to the changed list, flagged, negative pairs counted.
+template <class T>
+__global__ void __launch_bounds__(256) k_dense_diff(int64_t m_plus, T* __restrict__ up, T* __restrict__ dn,
+                                                    const T* __restrict__ up2, const T* __restrict__ dn2,
+                                                    uint8_t* __restrict__ chg, int32_t* __restrict__ changed,
+                                                    unsigned long long* __restrict__ stats) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t base = warp * 32; base < m_plus; base += nwarps * 32) {
+        const int64_t c = base + lane;
+        T nu = 0, nd = 0;
+        bool d = false;
+        if (c < m_plus) {
+            nu = up2[c];
+            nd = dn2[c];
+            d = nu != up[c] || nd != dn[c];
+        }
+        const unsigned mask = __ballot_sync(0xffffffffu, d);
+        if (!mask) continue;
+        const unsigned neg = __ballot_sync(0xffffffffu, d && negative_pair(nu, nd));
+        unsigned long long p0 = 0;
+        if (lane == 0) {
+            p0 = atomicAdd(stats + 1, (unsigned long long)__popc(mask));
+            if (neg) atomicAdd(stats + 2, (unsigned long long)__popc(neg));
+        }
+        p0 = __shfl_sync(0xffffffffu, p0, 0);
+        if (d) {
+            up[c] = nu;
+            dn[c] = nd;
+            chg[c] = 1;
+            const unsigned long long pos = p0 + __popc(mask & ((1u << lane) - 1u));
+            if (pos < (unsigned long long)m_plus) changed[pos] = (int32_t)c;
+        }
+    }
+}
+
+// dq[a] = 1 for every arc a with a lower triangle that has a changed side.
+// Supernode S (rows s0..s0+k-1, columns j of row i for i < j < k+b; column j
+// is vertex s0+j below k and boundary vertex B[j-k] from k on):
+//  - the triangles below target (p, j) inside S are (i; p, j) for i < p: the
+//    target is marked if a side (i, p) or (i, j) changed, a column flag
+//    above row p in column p or in column j;
+//  - every row of S holds all of B, so S is the bottom of a triangle below
+//    every boundary pair (B[p], B[q]): marked if column k+p or k+q of S
+//    has a changed arc. Every lower triangle is one of the two kinds.
+__global__ void __launch_bounds__(256) k_dense_mark(DevTopo D, SnDev S, int64_t nsn, const uint8_t* __restrict__ chg,
+                                                    uint8_t* __restrict__ dq, uint8_t* __restrict__ acol) {
+    extern __shared__ uint8_t anyc[];  // [b]: column of the boundary has a changed arc
+    for (int64_t sn = blockIdx.x; sn < nsn; sn += gridDim.x) {
+        const int32_t s0 = S.s0[sn], k = S.k[sn], b = S.b[sn];
+        const int32_t width = k + b;
+        for (int32_t p = 1 + threadIdx.x; p < k; p += blockDim.x) {
+            uint8_t a = 0;
+            for (int32_t i = 0; i < p && !a; i++) a = chg[D.first[s0 + i] + (p - i - 1)];
+            acol[s0 + p] = a;
+        }
+        __syncthreads();
+        int any = 0;
+        for (int32_t j = 1 + threadIdx.x; j < width; j += blockDim.x) {
+            uint8_t r = 0;
+            const int32_t rows = min(j, k);
+            for (int32_t p = 0; p < rows; p++) {
+                const int64_t a = D.first[s0 + p] + (j - p - 1);
+                if (r || (p > 0 && acol[s0 + p])) dq[a] = 1;
+                r |= chg[a];
+            }
+            if (j >= k) {
+                anyc[j - k] = r;
+                any |= r;
+            }
+        }
+        if (__syncthreads_or(any)) {
+            const int64_t ro = S.rel_off[sn];
+            for (int32_t p = 0; p + 1 < b; p++) {
+                const uint8_t ap = anyc[p];
+                const int64_t row = ro + (int64_t)p * (2 * b - p - 1) / 2 - p - 1;  // + q: pair (p, q)
+                for (int32_t q = p + 1 + threadIdx.x; q < b; q += blockDim.x)
+                    if (ap | anyc[q]) dq[S.rel[row + q]] = 1;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// Arcs of level >= L queued by the sweep before it stopped or marked above.
+__global__ void __launch_bounds__(256) k_dense_count(DevTopo D, int32_t L, const uint8_t* __restrict__ queued,
+                                                     const uint8_t* __restrict__ dq,
+                                                     unsigned long long* __restrict__ stats) {
+    unsigned long long c = 0;
+    for (int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; a < D.m_plus;
+         a += (int64_t)gridDim.x * blockDim.x)
+        if ((queued[a] | dq[a]) && D.vlevel[D.tail[a]] >= L) c++;
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+    if ((threadIdx.x & 31) == 0 && c) atomicAdd(stats + 0, c);
+}
+
+// The workspace cleanup of the sweep, for a stopped sweep.
+__global__ void __launch_bounds__(256) k_update_clean(UpdateWorkspace ws, const int64_t* __restrict__ level_arc_off,
+                                                      int64_t m_plus) {
+    const int64_t nchanged = min((int64_t)ws.stats[1], m_plus);
+    const int32_t nd_levels = (int32_t)ws.stats[3];
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < nchanged;
+         j += (int64_t)gridDim.x * blockDim.x)
+        ws.chg[ws.changed[j]] = 0;
+    for (int32_t li = blockIdx.x; li < nd_levels; li += gridDim.x) {
+        const int32_t l = ws.done_levels[li];
+        const int64_t base = level_arc_off[l];
+        const int32_t cnt = ws.bcount[l];
+        for (int32_t i = threadIdx.x; i < cnt; i += blockDim.x) ws.queued[ws.bucket[base + i]] = 0;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            ws.bcount[l] = 0;
+            ws.pending[l >> 5] = 0;
+        }
+    }
+}
+
 static void free_workspace(UpdateWorkspace* ws) {
     if (!ws) return;
+    cudaFree(ws->chg);
+    cudaFree(ws->dq);
+    cudaFree(ws->acol);
+    cudaFree(ws->up2);
+    cudaFree(ws->dn2);
     cudaFree(ws->queued);
     cudaFree(ws->bucket);
     cudaFree(ws->bcount);
@@ -280,11 +476,14 @@ int get_workspace(nwcch_topology* t, int64_t k, UpdateWorkspace** out) {
                   cudaMalloc(&ws->pending, ((L + 31) / 32) * 4) == cudaSuccess &&
                   cudaMalloc(&ws->done_levels, L * 4) == cudaSuccess &&
                   cudaMalloc(&ws->changed, std::max<int64_t>(1, mp) * 4) == cudaSuccess &&
-                  cudaMalloc(&ws->stats, 8 * sizeof(unsigned long long)) == cudaSuccess;
+                  cudaMalloc(&ws->chg, qbytes) == cudaSuccess && cudaMalloc(&ws->dq, qbytes) == cudaSuccess &&
+                  cudaMalloc(&ws->acol, std::max<int64_t>(1, t->d.n)) == cudaSuccess &&
+                  cudaMalloc(&ws->stats, kStatWords * sizeof(unsigned long long)) == cudaSuccess;
         if (ok)
             ok = cudaMemset(ws->queued, 0, qbytes) == cudaSuccess && cudaMemset(ws->bcount, 0, L * 4) == cudaSuccess &&
                  cudaMemset(ws->pending, 0, ((L + 31) / 32) * 4) == cudaSuccess &&
-                 cudaMemset(ws->stats, 0, 8 * sizeof(unsigned long long)) == cudaSuccess;
+                 cudaMemset(ws->chg, 0, qbytes) == cudaSuccess && cudaMemset(ws->dq, 0, qbytes) == cudaSuccess &&
+                 cudaMemset(ws->stats, 0, kStatWords * sizeof(unsigned long long)) == cudaSuccess;
         if (ok) ok = cooperative_blocks((const void*)k_update<int32_t>, &ws->blocks32) == NWCCH_OK &&
                      cooperative_blocks((const void*)k_update<int64_t>, &ws->blocks64) == NWCCH_OK;
         if (!ok) {
@@ -311,6 +510,48 @@ int get_workspace(nwcch_topology* t, int64_t k, UpdateWorkspace** out) {
 }
 
 }  // namespace
+
+// Time the level sweep may take before the update is finished densely: about
+// half a full customization (which runs near 1e11 triangles/s), at least
+// 0.2 ms. NWCCH_UPDATE_MODE=dense or =incremental forces one form.
+long long sweep_budget_ns(const nwcch_topology* t) {
+    const char* mode = getenv("NWCCH_UPDATE_MODE");
+    if (mode && !strcmp(mode, "dense")) return 0;
+    if (mode && !strcmp(mode, "incremental")) return LLONG_MAX;
+    return std::max<long long>(200000, (long long)(t->triangles / 200));
+}
+
+template <class T>
+int finish_dense(nwcch_topology* t, UpdateWorkspace* ws, const int32_t* w_dev, T* up_dev, T* dn_dev, int32_t L,
+                 cudaStream_t s) {
+    auto* P = static_cast<SnPlan*>(t->sn_plan);
+    const int64_t mp = t->d.m_plus;
+    if (!P) return NWCCH_ERR_TOPOLOGY;
+    if (!ws->up2) {
+        if (cudaMalloc(&ws->up2, std::max<int64_t>(1, mp) * 8) != cudaSuccess) return NWCCH_ERR_NOMEM;
+        if (cudaMalloc(&ws->dn2, std::max<int64_t>(1, mp) * 8) != cudaSuccess) {
+            cudaFree(ws->up2);
+            ws->up2 = nullptr;
+            return NWCCH_ERR_NOMEM;
+        }
+    }
+    T* up2 = static_cast<T*>(ws->up2);
+    T* dn2 = static_cast<T*>(ws->dn2);
+    int rc = launch_supernodal<T>(t, P, w_dev, up2, dn2, s);
+    if (rc) return rc;
+    k_dense_diff<T><<<grid_for(mp, 256), 256, 0, s>>>(mp, up_dev, dn_dev, up2, dn2, ws->chg, ws->changed, ws->stats);
+    const size_t smem = (size_t)std::max(1, P->max_b);
+    if (smem > 227 * 1024) return NWCCH_ERR_CAPACITY;
+    if (smem > 48 * 1024)
+        NWCCH_CUDA_TRY(cudaFuncSetAttribute(k_dense_mark, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const unsigned blocks = (unsigned)std::max<int64_t>(1, std::min<int64_t>(P->nsn, 152 * 8));
+    k_dense_mark<<<blocks, 256, smem, s>>>(t->d, P->dev, P->nsn, ws->chg, ws->dq, ws->acol);
+    k_dense_count<<<grid_for(mp, 256), 256, 0, s>>>(t->d, L, ws->queued, ws->dq, ws->stats);
+    k_update_clean<<<152 * 4, 256, 0, s>>>(*ws, t->d_level_arc_off, mp);
+    NWCCH_CUDA_TRY(cudaGetLastError());
+    NWCCH_CUDA_TRY(cudaMemsetAsync(ws->dq, 0, (size_t)mp, s));
+    return NWCCH_OK;
+}
 
 template <class T>
 int update(nwcch_topology* t, int32_t* w_dev, T* up_dev, T* dn_dev, const int64_t* edge_idx, const int32_t* new_w,
@@ -341,7 +582,7 @@ int update(nwcch_topology* t, int32_t* w_dev, T* up_dev, T* dn_dev, const int64_
         NWCCH_CUDA_TRY(cudaMemcpyAsync(ws->edge_idx, idx.data(), kk * 8, cudaMemcpyHostToDevice, s));
         NWCCH_CUDA_TRY(cudaMemcpyAsync(ws->new_w, val.data(), kk * 4, cudaMemcpyHostToDevice, s));
     }
-    NWCCH_CUDA_TRY(cudaMemsetAsync(ws->stats, 0, 8 * sizeof(unsigned long long), s));
+    NWCCH_CUDA_TRY(cudaMemsetAsync(ws->stats, 0, kStatWords * sizeof(unsigned long long), s));
     UpdateArgs<T> A;
     A.D = t->d;
     A.w = w_dev;
@@ -352,12 +593,21 @@ int update(nwcch_topology* t, int32_t* w_dev, T* up_dev, T* dn_dev, const int64_
     A.k = kk;
     A.ws = *ws;
     A.err = stream_slot(t, s).err;
+    A.budget_ns = sweep_budget_ns(t);
+    A.max_arcs = std::max<int64_t>(4096, t->d.m_plus / 8);
     void* args[] = {&A};
     const int blocks = sizeof(T) == 4 ? ws->blocks32 : ws->blocks64;
     NWCCH_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k_update<T>, dim3(blocks), dim3(256), args, 0, s));
-    unsigned long long h[8];
+    unsigned long long h[kStatWords];
     NWCCH_CUDA_TRY(cudaMemcpyAsync(h, ws->stats, sizeof(h), cudaMemcpyDeviceToHost, s));
     NWCCH_CUDA_TRY(cudaStreamSynchronize(s));
+    if (h[7]) {  // the sweep stopped at level h[7] - 1: finish densely
+        rc = finish_dense<T>(t, ws, w_dev, up_dev, dn_dev, (int32_t)(h[7] - 1), s);
+        if (rc) return rc;
+        NWCCH_CUDA_TRY(cudaMemcpyAsync(h, ws->stats, sizeof(h), cudaMemcpyDeviceToHost, s));
+        NWCCH_CUDA_TRY(cudaStreamSynchronize(s));
+    }
+    if (h[1] > (unsigned long long)t->d.m_plus) return NWCCH_ERR_TOPOLOGY;  // an arc changed twice: inconsistent state
     if (changed_dev && h[1])
         NWCCH_CUDA_TRY(cudaMemcpyAsync(changed_dev, ws->changed, h[1] * 4, cudaMemcpyDeviceToDevice, s));
     rc = consume_error(t, s);

@@ -3,6 +3,8 @@ vectors of the reference and against the pinned CPU oracle. Integer work, so
 every comparison is exact."""
 from __future__ import annotations
 
+import functools
+
 import numpy as np
 import pytest
 
@@ -47,9 +49,15 @@ def test_family_customize_query(gpu, storage, i):
     assert np.array_equal(d, c["ans"]) and np.array_equal(d, c["truth"])
 
 
+@pytest.mark.parametrize("mode", ["auto", "dense"])
 @pytest.mark.parametrize("storage", ["int32", "int64"])
 @pytest.mark.parametrize("i", range(12))
-def test_family_updates(gpu, storage, i):
+def test_family_updates(gpu, storage, i, mode, monkeypatch):
+    """Partial re-customization against the reference's recorded updates:
+    evaluated count, changed set and values. "dense" stops the level sweep
+    at once, so the update is finished by the dense form."""
+    if mode != "auto":
+        monkeypatch.setenv("NWCCH_UPDATE_MODE", mode)
     c = family_case(load_golden("family.npz"), i)
     T = dev_topo(c)
     m = T.customize(c["w"], storage)
@@ -171,6 +179,7 @@ def test_large_weights_take_the_exact_path(gpu, oracle):
         assert np.array_equal(up, oup) and np.array_equal(dn, odn)
 
 
+@functools.lru_cache(maxsize=4)
 def _seeded(kind, n, seed):
     from nwcch import graphs as G
     from nwcch import topology as TT
@@ -178,8 +187,11 @@ def _seeded(kind, n, seed):
     return g, TT.build_topology(g)
 
 
+@pytest.mark.parametrize("mode", ["auto", "incremental", "dense"])
 @pytest.mark.parametrize("kind,n", [("delaunay", 50_000), ("road", 80_000)])
-def test_against_oracle(gpu, oracle, kind, n):
+def test_against_oracle(gpu, oracle, kind, n, mode, monkeypatch):
+    if mode != "auto":
+        monkeypatch.setenv("NWCCH_UPDATE_MODE", mode)
     from nwcch import graphs as G
     from nwcch.device import DeviceTopology
     g, top = _seeded(kind, n, seed=21)
