@@ -242,6 +242,23 @@ int nwcch_query_batch_noalloc(nwcch_topology* t, const int32_t* up_dev, const in
                               const int32_t* s_rank_dev, const int32_t* t_rank_dev, int64_t nq,
                               int64_t* dist_dev, void* stream);
 
+/* ------------------------------------------------------------------------
+ * CCH potential
+ * ---------------------------------------------------------------------- */
+
+/* p(v) = min(0, min_u dist(u, v)), the virtual-source distances of
+ * Johnson's algorithm, read off a customized metric by an upward and a
+ * downward sweep. Replaces cch_potential (cpp/cch.cpp:631-655) and
+ * CCH.potential (python/cch.py:734-755). p_dev: int64[n] in RANK space (the
+ * reference returns p[rank[v]] per vertex v). Meaningful for metrics without
+ * a negative cycle; NWCCH_SATURATED if a sum left the int64 range. */
+int nwcch_potential(nwcch_topology* t, const int32_t* up_dev, const int32_t* dn_dev, int64_t* p_dev,
+                    void* stream);
+int nwcch_potential_async(nwcch_topology* t, const int32_t* up_dev, const int32_t* dn_dev, int64_t* p_dev,
+                          void* stream);
+int nwcch_potential_i64(nwcch_topology* t, const int64_t* up_dev, const int64_t* dn_dev, int64_t* p_dev,
+                        void* stream);
+
 #ifdef __cplusplus
 }
 #endif

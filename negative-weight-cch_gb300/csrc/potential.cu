@@ -1,0 +1,266 @@
+// CCH potential on the device: p(v) = min(0, min_u dist(u, v)) read off a
+// customized metric (cpp/cch.cpp:631-655, python/cch.py:734-755), the
+// virtual-source distances Johnson's algorithm gets from Bellman-Ford.
+//
+// The reference sweeps every vertex upward in rank order (pushing p(x) +
+// up(x, y) to the heads of x's row), then downward in reverse rank order
+// (p(x) = min(p(x), p(y) + dn(x, y)) over the row). Here both sweeps go by
+// supernode level, so a whole level runs at once:
+//
+// upward (levels from the bottom): a vertex's lower neighbours lie in its own
+// supernode or in descendant supernodes, which pushed their candidates into
+// p with atomicMin when their level ran. Inside a supernode the rows i < j
+// form a triangular (min,+) solve, done 32 rows at a time: the 32x32 diagonal
+// block by shuffles, the rest of the chunk's columns as a (min,+) product.
+// The boundary columns (ancestors) are pushed at the end.
+//
+// downward (levels from the top): the boundary values are final, so every
+// row first takes its (min,+) product with them; then the rows are solved
+// from the bottom, 32 at a time, against the rows below them.
+//
+// Small supernodes take one warp each, large ones a CTA of 256 threads.
+
+#include <algorithm>
+
+#include "common.cuh"
+#include "customize.h"
+#include "supernodal.h"
+#include "topology.h"
+
+namespace nwcch {
+
+namespace {
+
+constexpr unsigned FULL = 0xffffffffu;
+
+__device__ __forceinline__ int64_t warp_min64(int64_t v) {
+    for (int o = 16; o > 0; o >>= 1) v = min(v, (int64_t)__shfl_xor_sync(FULL, (long long)v, o));
+    return v;
+}
+
+// arc of supernode row i (vertex s0+i), column j (j > i): first[s0+i] + (j-i-1)
+__device__ __forceinline__ int64_t arc_at(const DevTopo& D, int32_t s0, int32_t i, int32_t j) {
+    return D.first[s0 + i] + (j - i - 1);
+}
+
+// ---------------------------------------------------------------- upward
+
+// Rows [i0, i0+rows) of a supernode: the diagonal block, by one warp.
+template <class T>
+__device__ void up_diagonal(const DevTopo& D, int32_t s0, int32_t i0, int rows, const T* __restrict__ up,
+                            int64_t* p, int& e) {
+    const int lane = threadIdx.x & 31;
+    int64_t pj = lane < rows ? p[s0 + i0 + lane] : 0;
+    for (int r = 0; r + 1 < rows; r++) {
+        const int64_t pr = __shfl_sync(FULL, (long long)pj, r);
+        if (lane > r && lane < rows) {
+            const int64_t c = label_plus(pr, up[arc_at(D, s0, i0 + r, i0 + lane)], e);
+            if (c < pj) pj = c;
+        }
+    }
+    if (lane < rows) p[s0 + i0 + lane] = pj;
+}
+
+// Column j of the supernode against rows [i0, i1): min over the rows.
+template <class T>
+__device__ __forceinline__ int64_t up_column(const DevTopo& D, int32_t s0, int32_t i0, int32_t i1, int32_t j,
+                                             const T* __restrict__ up, const int64_t* p, int& e) {
+    int64_t acc = INF64;
+    for (int32_t i = i0; i < i1; i++) acc = min(acc, label_plus(p[s0 + i], up[arc_at(D, s0, i, j)], e));
+    return acc;
+}
+
+template <class T>
+__global__ void __launch_bounds__(128) k_pot_up_warp(DevTopo D, SnDev S, const int32_t* __restrict__ sns,
+                                                     int64_t count, const T* __restrict__ up, int64_t* p, int* err) {
+    const int lane = threadIdx.x & 31;
+    const int64_t w = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    int e = 0;
+    for (int64_t it = w; it < count; it += nw) {
+        const int32_t sn = sns[it];
+        const int32_t s0 = S.s0[sn], k = S.k[sn], b = S.b[sn];
+        // k <= 32: one diagonal block holds every internal row
+        up_diagonal<T>(D, s0, 0, k, up, p, e);
+        __syncwarp();
+        const int64_t brow = D.first[s0 + k - 1];  // the last row lists the boundary
+        for (int32_t q = lane; q < b; q += 32) {
+            const int64_t acc = up_column<T>(D, s0, 0, k, k + q, up, p, e);
+            if (acc < 0) atomicMin(reinterpret_cast<long long*>(p + D.head[brow + q]), (long long)acc);
+        }
+        __syncwarp();
+    }
+    if (e) atomicOr(err, e);
+}
+
+template <class T>
+__global__ void __launch_bounds__(256) k_pot_up_cta(DevTopo D, SnDev S, const int32_t* __restrict__ sns,
+                                                    int64_t count, const T* __restrict__ up, int64_t* p, int* err) {
+    const int warp = threadIdx.x >> 5;
+    int e = 0;
+    for (int64_t it = blockIdx.x; it < count; it += gridDim.x) {
+        const int32_t sn = sns[it];
+        const int32_t s0 = S.s0[sn], k = S.k[sn], b = S.b[sn];
+        for (int32_t i0 = 0; i0 < k; i0 += 32) {
+            const int rows = min(32, k - i0);
+            if (warp == 0) up_diagonal<T>(D, s0, i0, rows, up, p, e);
+            __syncthreads();
+            for (int32_t j = i0 + rows + threadIdx.x; j < k; j += blockDim.x) {
+                const int64_t acc = up_column<T>(D, s0, i0, i0 + rows, j, up, p, e);
+                if (acc < p[s0 + j]) p[s0 + j] = acc;
+            }
+            __syncthreads();
+        }
+        const int64_t brow = D.first[s0 + k - 1];
+        for (int32_t q = threadIdx.x; q < b; q += blockDim.x) {
+            const int64_t acc = up_column<T>(D, s0, 0, k, k + q, up, p, e);
+            if (acc < 0) atomicMin(reinterpret_cast<long long*>(p + D.head[brow + q]), (long long)acc);
+        }
+        __syncthreads();
+    }
+    if (e) atomicOr(err, e);
+}
+
+// ---------------------------------------------------------------- downward
+
+// Row i against columns [j0, j1) (vertices final): min over the columns, by
+// one warp; column j's vertex value comes from `val`.
+template <class T, class V>
+__device__ __forceinline__ int64_t down_row(const DevTopo& D, int32_t s0, int32_t i, int32_t j0, int32_t j1,
+                                            const T* __restrict__ dn, V val, int& e) {
+    const int lane = threadIdx.x & 31;
+    int64_t acc = INF64;
+    for (int32_t j = j0 + lane; j < j1; j += 32) acc = min(acc, label_plus(val(j), dn[arc_at(D, s0, i, j)], e));
+    return warp_min64(acc);
+}
+
+// Rows [i0, i0+rows), bottom-up, against each other: the diagonal block.
+template <class T>
+__device__ void down_diagonal(const DevTopo& D, int32_t s0, int32_t i0, int rows, const T* __restrict__ dn,
+                              int64_t* p, int& e) {
+    const int lane = threadIdx.x & 31;
+    int64_t mine = lane < rows ? p[s0 + i0 + lane] : INF64;
+    for (int r = rows - 2; r >= 0; r--) {
+        int64_t c = INF64;
+        if (lane > r && lane < rows) c = label_plus(mine, dn[arc_at(D, s0, i0 + r, i0 + lane)], e);
+        c = warp_min64(c);
+        if (lane == r && c < mine) mine = c;
+    }
+    if (lane < rows) p[s0 + i0 + lane] = mine;
+}
+
+template <class T>
+__global__ void __launch_bounds__(128) k_pot_down_warp(DevTopo D, SnDev S, const int32_t* __restrict__ sns,
+                                                       int64_t count, const T* __restrict__ dn, int64_t* p,
+                                                       int* err) {
+    const int lane = threadIdx.x & 31;
+    const int64_t w = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    int e = 0;
+    for (int64_t it = w; it < count; it += nw) {
+        const int32_t sn = sns[it];
+        const int32_t s0 = S.s0[sn], k = S.k[sn], b = S.b[sn];
+        const int32_t* B = D.head + D.first[s0 + k - 1];
+        auto bval = [&](int32_t j) { return p[B[j - k]]; };
+        for (int32_t i = 0; i < k; i++) {
+            const int64_t c = down_row<T>(D, s0, i, k, k + b, dn, bval, e);
+            if (lane == 0 && c < p[s0 + i]) p[s0 + i] = c;
+        }
+        __syncwarp();
+        down_diagonal<T>(D, s0, 0, k, dn, p, e);
+        __syncwarp();
+    }
+    if (e) atomicOr(err, e);
+}
+
+template <class T>
+__global__ void __launch_bounds__(256) k_pot_down_cta(DevTopo D, SnDev S, const int32_t* __restrict__ sns,
+                                                      int64_t count, const T* __restrict__ dn, int64_t* p, int* err) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    int e = 0;
+    for (int64_t it = blockIdx.x; it < count; it += gridDim.x) {
+        const int32_t sn = sns[it];
+        const int32_t s0 = S.s0[sn], k = S.k[sn], b = S.b[sn];
+        const int32_t* B = D.head + D.first[s0 + k - 1];
+        auto bval = [&](int32_t j) { return p[B[j - k]]; };
+        for (int32_t i = warp; i < k; i += nwarps) {
+            const int64_t c = down_row<T>(D, s0, i, k, k + b, dn, bval, e);
+            if (lane == 0 && c < p[s0 + i]) p[s0 + i] = c;
+        }
+        __syncthreads();
+        auto ival = [&](int32_t j) { return p[s0 + j]; };
+        for (int32_t i1 = k; i1 > 0; i1 -= 32) {
+            const int32_t i0 = max(0, i1 - 32);
+            // the chunk's rows against the final rows [i1, k)
+            for (int32_t i = i0 + warp; i < i1; i += nwarps) {
+                const int64_t c = down_row<T>(D, s0, i, i1, k, dn, ival, e);
+                if (lane == 0 && c < p[s0 + i]) p[s0 + i] = c;
+            }
+            __syncthreads();
+            if (warp == 0) down_diagonal<T>(D, s0, i0, i1 - i0, dn, p, e);
+            __syncthreads();
+        }
+    }
+    if (e) atomicOr(err, e);
+}
+
+int warp_grid(int64_t count) {
+    return (int)std::max<int64_t>(1, std::min<int64_t>((count + 3) / 4, 152 * 64));
+}
+
+}  // namespace
+
+template <class T>
+int potential(nwcch_topology* t, const T* up, const T* dn, int64_t* p, cudaStream_t s) {
+    auto* P = static_cast<SnPlan*>(t->sn_plan);
+    if (!P) return NWCCH_ERR_TOPOLOGY;
+    int* err = stream_slot(t, s).err;
+    const DevTopo& D = t->d;
+    NWCCH_CUDA_TRY(cudaMemsetAsync(p, 0, sizeof(int64_t) * std::max<int64_t>(1, D.n), s));
+    const int32_t L = P->levels;
+    for (int32_t l = 0; l < L; l++) {
+        const int64_t off = P->sn_level_off[l], big = P->sn_level_big[l], cnt = P->sn_level_off[l + 1] - off;
+        if (big)
+            k_pot_up_cta<T><<<(unsigned)std::min<int64_t>(big, 152 * 8), 256, 0, s>>>(D, P->dev, P->d_sn_order + off,
+                                                                                   big, up, p, err);
+        if (cnt > big)
+            k_pot_up_warp<T><<<warp_grid(cnt - big), 128, 0, s>>>(D, P->dev, P->d_sn_order + off + big, cnt - big, up,
+                                                                  p, err);
+    }
+    for (int32_t l = L - 1; l >= 0; l--) {
+        const int64_t off = P->sn_level_off[l], big = P->sn_level_big[l], cnt = P->sn_level_off[l + 1] - off;
+        if (big)
+            k_pot_down_cta<T><<<(unsigned)std::min<int64_t>(big, 152 * 8), 256, 0, s>>>(
+                D, P->dev, P->d_sn_order + off, big, dn, p, err);
+        if (cnt > big)
+            k_pot_down_warp<T><<<warp_grid(cnt - big), 128, 0, s>>>(D, P->dev, P->d_sn_order + off + big, cnt - big,
+                                                                    dn, p, err);
+    }
+    NWCCH_CUDA_TRY(cudaGetLastError());
+    return NWCCH_OK;
+}
+
+}  // namespace nwcch
+
+using namespace nwcch;
+
+extern "C" int nwcch_potential_async(nwcch_topology* t, const int32_t* up_dev, const int32_t* dn_dev, int64_t* p_dev,
+                                     void* stream) {
+    if (!t || !p_dev || (t->d.m_plus > 0 && (!up_dev || !dn_dev))) return NWCCH_ERR_ARG;
+    return potential<int32_t>(t, up_dev, dn_dev, p_dev, (cudaStream_t)stream);
+}
+
+extern "C" int nwcch_potential(nwcch_topology* t, const int32_t* up_dev, const int32_t* dn_dev, int64_t* p_dev,
+                               void* stream) {
+    const int rc = nwcch_potential_async(t, up_dev, dn_dev, p_dev, stream);
+    if (rc) return rc;
+    return consume_error(t, (cudaStream_t)stream);
+}
+
+extern "C" int nwcch_potential_i64(nwcch_topology* t, const int64_t* up_dev, const int64_t* dn_dev, int64_t* p_dev,
+                                   void* stream) {
+    if (!t || !p_dev || (t->d.m_plus > 0 && (!up_dev || !dn_dev))) return NWCCH_ERR_ARG;
+    const int rc = potential<int64_t>(t, up_dev, dn_dev, p_dev, (cudaStream_t)stream);
+    if (rc) return rc;
+    return consume_error(t, (cudaStream_t)stream);
+}

@@ -207,11 +207,30 @@ SnPlan* build_supernodal_plan(int64_t n, const int64_t* first, const int32_t* he
         add(SN_OUT_BIG, l, 0, out_big[l]);
     }
     P->items = (int64_t)items.size() / 3;
+    // supernodes by level, whole-CTA ones first within a level
+    std::vector<int32_t> order;
+    order.reserve(ns);
+    P->sn_level_off.assign(L + 1, 0);
+    P->sn_level_big.assign(L, 0);
+    {
+        std::vector<std::vector<int32_t>> by_level(L);
+        for (int64_t s = 0; s < ns; s++) by_level[lvl[s]].push_back((int32_t)s);
+        for (int32_t l = 0; l < L; l++) {
+            P->sn_level_off[l] = (int64_t)order.size();
+            for (int32_t s : by_level[l])
+                if (sn_sweep_big(kv[s], bv[s])) order.push_back(s);
+            P->sn_level_big[l] = (int64_t)order.size() - P->sn_level_off[l];
+            for (int32_t s : by_level[l])
+                if (!sn_sweep_big(kv[s], bv[s])) order.push_back(s);
+        }
+        P->sn_level_off[L] = (int64_t)order.size();
+    }
     int32_t *d_s0, *d_k, *d_b, *d_rel, *d_sid;
     int64_t* d_rel_off;
     if ((*rc = upload_vec(P, s0v, &d_s0)) || (*rc = upload_vec(P, kv, &d_k)) || (*rc = upload_vec(P, bv, &d_b)) ||
         (*rc = upload_vec(P, rel_off, &d_rel_off)) || (*rc = upload_vec(P, rel, &d_rel)) ||
-        (*rc = upload_vec(P, items, &P->d_items)) || (*rc = upload_vec(P, sid, &d_sid))) {
+        (*rc = upload_vec(P, items, &P->d_items)) || (*rc = upload_vec(P, sid, &d_sid)) ||
+        (*rc = upload_vec(P, order, &P->d_sn_order))) {
         free_supernodal_plan(P);
         return nullptr;
     }

@@ -62,6 +62,12 @@ struct SnPlan {
     int64_t items = 0;
     int64_t rel_entries = 0;
     int32_t max_b = 0;            // longest boundary of any supernode
+    // supernodes grouped by level (the vertex sweeps of the potential):
+    // level l is sn_order[sn_level_off[l] .. sn_level_off[l+1]), its first
+    // sn_level_big[l] entries taking a whole CTA each, the rest a warp each
+    std::vector<int64_t> sn_level_off;
+    std::vector<int64_t> sn_level_big;
+    int32_t* d_sn_order = nullptr;
     std::vector<SnLaunch> launches;
     SnDev dev{};
     int32_t* d_items = nullptr;
@@ -80,6 +86,9 @@ void free_supernodal_plan(SnPlan* p);
 template <class T>
 int run_supernodal(nwcch_topology* t, SnPlan* P, const int32_t* w, T* up, T* dn, cudaStream_t s, int* err,
                    int metrics = 1);
+
+// A supernode swept by a whole CTA rather than one warp.
+inline bool sn_sweep_big(int64_t k, int64_t b) { return k > 32 || k * (k + b) > 32 * 1024; }
 
 // Enqueues the supernodal query kernel (labels in shared memory); sets *used
 // to false, enqueuing nothing, when the elimination tree is too deep for it.

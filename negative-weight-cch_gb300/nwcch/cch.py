@@ -92,6 +92,13 @@ class CCH:
         """Checks only the arcs the last update changed (python/cch.py:666-671)."""
         return self.dev.negative_loops(self.metric) > 0 or self.metric.stats.get("changed_negative", 0) > 0
 
+    def potential(self) -> np.ndarray:
+        """python/cch.py:734-755: the feasible potential p(v) = min(0,
+        min_u dist(u, v)) read off the customized metric, per ORIGINAL vertex
+        (float64, as the reference)."""
+        p = self.dev.potential(self.metric).cpu().numpy()
+        return p[self.rank].astype(np.float64)
+
     # ------------------------------------------------------------ queries
     def query(self, s, t) -> float:
         """Distance between ORIGINAL vertex ids s and t (inf if unreachable)."""

@@ -43,6 +43,8 @@ for _name, _args in {
     "nwcch_update_i64": [P, P, P, P, P, P, I64, P, P, P],
     "nwcch_query_batch": [P, P, P, P, P, I64, P, P],
     "nwcch_query_batch_i64": [P, P, P, P, P, I64, P, P],
+    "nwcch_potential": [P, P, P, P, P],
+    "nwcch_potential_i64": [P, P, P, P, P],
 }.items():
     _lib.register(_name, _args)
 
@@ -349,6 +351,19 @@ class DeviceTopology:
         _status(fn(self.handle, m.up.data_ptr(), m.dn.data_ptr(), s.data_ptr(), t.data_ptr(), s.numel(),
                    out.data_ptr(), _stream(torch)), "query_batch")
         return out
+
+    # ------------------------------------------------------------ potential
+    def potential(self, m: Metric, out=None):
+        """CCH potential p(v) = min(0, min_u dist(u, v)) (cpp/cch.cpp:631-655),
+        int64 CUDA tensor in RANK space."""
+        torch = self._torch
+        if out is None:
+            out = torch.empty(max(self.n, 1), dtype=torch.int64, device="cuda")
+        lib = _lib.lib()
+        fn = lib.nwcch_potential if m.storage == "int32" else lib.nwcch_potential_i64
+        if _status(fn(self.handle, m.up.data_ptr(), m.dn.data_ptr(), out.data_ptr(), _stream(torch)), "potential"):
+            warnings.warn("potential saturated: some sums left the int64 range", SaturationWarning, stacklevel=2)
+        return out[:self.n]
 
 
 def distances_to_float(d) -> np.ndarray:

@@ -386,6 +386,50 @@ int orc_bellman_ford(int64_t n, const int64_t* off, const int32_t* tgt, const in
     return r;
 }
 
+void orc_potential(int64_t n, const int64_t* first, const int32_t* head, const int64_t* up, const int64_t* dn,
+                   int64_t* p) {
+    /* cpp/cch.cpp:636-644: upward pass, increasing rank */
+    for (int64_t x = 0; x < n; x++) p[x] = 0;
+    for (int64_t x = 0; x < n; x++) {
+        const int64_t px = p[x];
+        for (int64_t a = first[x]; a < first[x + 1]; a++) {
+            int64_t v;
+            if (add_ok(px, up[a], &v) && v < p[head[a]]) p[head[a]] = v;
+        }
+    }
+    /* cpp/cch.cpp:645-652: downward pass, decreasing rank */
+    for (int64_t x = n - 1; x >= 0; x--) {
+        int64_t best = p[x];
+        for (int64_t a = first[x]; a < first[x + 1]; a++) {
+            int64_t v;
+            if (add_ok(p[head[a]], dn[a], &v) && v < best) best = v;
+        }
+        p[x] = best;
+    }
+}
+
+int orc_virtual_source_potential(int64_t n, const int64_t* off, const int32_t* tgt, const int32_t* w,
+                                 int64_t* p) {
+    unsigned char* inq = (unsigned char*)calloc((size_t)n, 1);
+    int64_t* queue = (int64_t*)malloc((size_t)(n + 1) * sizeof(int64_t));
+    int64_t* count = (int64_t*)calloc((size_t)n, sizeof(int64_t));
+    int64_t* src = (int64_t*)malloc((size_t)(n > 0 ? n : 1) * sizeof(int64_t));
+    for (int64_t v = 0; v < n; v++) {
+        src[v] = v;
+        p[v] = 0;
+    }
+    int r = 0;
+    for (int64_t u = 0; u < n && !r; u++)
+        for (int64_t k = off[u]; k < off[u + 1]; k++)
+            if (tgt[k] == u && w[k] < 0) r = 1;
+    if (!r) r = spfa(n, off, tgt, w, p, inq, queue, count, n, src);
+    free(inq);
+    free(queue);
+    free(count);
+    free(src);
+    return r;
+}
+
 int orc_has_negative_cycle(int64_t n, const int64_t* off, const int32_t* tgt, const int32_t* w) {
     int64_t* dist = (int64_t*)calloc((size_t)n, sizeof(int64_t));
     unsigned char* inq = (unsigned char*)calloc((size_t)n, 1);

@@ -67,4 +67,17 @@ int orc_bellman_ford(int64_t n, const int64_t* off, const int32_t* tgt, const in
  * exists. */
 int orc_has_negative_cycle(int64_t n, const int64_t* off, const int32_t* tgt, const int32_t* w);
 
+/* cpp/cch.cpp:631-655 (= python/cch.py:734-755): the potential
+ * p(v) = min(0, min_u dist(u, v)) read off a customized CCH, rank space:
+ * an upward pass in increasing rank, then a downward pass in decreasing rank.
+ * p int64[n]. */
+void orc_potential(int64_t n, const int64_t* first, const int32_t* head, const int64_t* up, const int64_t* dn,
+                   int64_t* p);
+
+/* The same potential by Bellman-Ford from a virtual source with 0-arcs to
+ * every vertex (the role of cpp/cch.cpp:608-629 johnson_potential), original
+ * vertex ids. Returns 1 if a negative cycle exists (p then undefined). */
+int orc_virtual_source_potential(int64_t n, const int64_t* off, const int32_t* tgt, const int32_t* w,
+                                 int64_t* p);
+
 #endif

@@ -51,6 +51,10 @@ def lib():
             L.orc_bellman_ford.argtypes = [I64, P, P, P, I64, P]
             L.orc_bellman_ford.restype = C.c_int
             L.orc_has_negative_cycle.argtypes = [I64, P, P, P]
+            L.orc_potential.argtypes = [I64, P, P, P, P, P]
+            L.orc_potential.restype = None
+            L.orc_virtual_source_potential.argtypes = [I64, P, P, P, P]
+            L.orc_virtual_source_potential.restype = C.c_int
             L.orc_has_negative_cycle.restype = C.c_int
             _lib = L
     return _lib
@@ -135,6 +139,22 @@ def bellman_ford(n, off, tgt, w, s):
 def has_negative_cycle(n, off, tgt, w) -> bool:
     off, tgt, w = _c(off, np.int64), _c(tgt, np.int32), _c(w, np.int32)
     return bool(lib().orc_has_negative_cycle(n, _p(off), _p(tgt), _p(w)))
+
+
+def potential(T: Topo, up, dn):
+    """cpp/cch.cpp:631-655: the CCH potential, rank space (int64[n])."""
+    up, dn = _c(up, np.int64), _c(dn, np.int64)
+    p = np.empty(T.n, np.int64)
+    lib().orc_potential(T.n, _p(T.first), _p(T.head), _p(up), _p(dn), _p(p))
+    return p
+
+
+def virtual_source_potential(n, off, tgt, w):
+    """Bellman-Ford from a virtual source (0-arcs to every vertex), original
+    ids; None if a negative cycle exists."""
+    off, tgt, w = _c(off, np.int64), _c(tgt, np.int32), _c(w, np.int32)
+    p = np.empty(n, np.int64)
+    return None if lib().orc_virtual_source_potential(n, _p(off), _p(tgt), _p(w), _p(p)) else p
 
 
 def to_float(a):

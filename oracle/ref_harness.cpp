@@ -144,6 +144,15 @@ void ref_johnson_potential(void* p, const double* w, double* pot) {
     std::copy(pv.begin(), pv.end(), pot);
 }
 
+// Reference CCH potential (two sweeps over the customized CCH), original ids.
+void ref_cch_potential(void* p, const double* up, const double* dn, double* pot) {
+    auto* h = static_cast<RefHandle*>(p);
+    const size_t m = h->c.head.size();
+    vector<double> u(up, up + m), d(dn, dn + m);
+    auto pv = cch_potential(h->c, u, d);
+    std::copy(pv.begin(), pv.end(), pot);
+}
+
 void ref_dijkstra_batch(void* p, const double* w, const double* pot, int64_t nq, const int64_t* s,
                         const int64_t* t, double* out) {
     auto* h = static_cast<RefHandle*>(p);

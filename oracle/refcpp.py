@@ -52,6 +52,8 @@ def lib():
         L.ref_query_batch.argtypes = [P, P, P, I64, P, P, P]
         L.ref_johnson_potential.argtypes = [P, P, P]
         L.ref_dijkstra_batch.argtypes = [P, P, P, I64, P, P, P]
+        L.ref_cch_potential.argtypes = [P, P, P, P]
+        L.ref_cch_potential.restype = None
         _lib = L
     return _lib
 
@@ -124,6 +126,12 @@ class RefCCH:
         secs = lib().ref_query_batch(self.h, _p(np.ascontiguousarray(up)), _p(np.ascontiguousarray(dn)), s.size,
                                      _p(s), _p(t), _p(out))
         return out, secs
+
+    def cch_potential(self, up, dn):
+        """The reference's CCH potential, original vertex ids (float64)."""
+        pot = np.empty(self.n)
+        lib().ref_cch_potential(self.h, _p(np.ascontiguousarray(up)), _p(np.ascontiguousarray(dn)), _p(pot))
+        return pot
 
     def johnson_dijkstra(self, w, s, t):
         w = np.ascontiguousarray(w, np.float64)

@@ -28,7 +28,14 @@ Fixtures (np.savez_compressed):
   reference C++ nested-dissection order, customized arcs, negative-cycle
   count and 1,000 query answers;
 * delaunay_negcycle.npz - a 3,000-point Delaunay graph with one injected
-  3-cycle of total weight -1: customized arcs and the scan count.
+  3-cycle of total weight -1: customized arcs and the scan count;
+* potential.npz   - the reference's CCH potential: CCH.potential
+  (python/cch.py:734-755) on every family.npz graph rebuilt in the
+  reference with the fixture's order, and cch_potential (cpp/cch.cpp:631-655)
+  on grid64.npz; original vertex ids.
+
+`--only NAME[,NAME]` regenerates some fixtures (techniques, family, grid64,
+delaunay_negcycle, potential); potential reads family.npz and grid64.npz.
 """
 from __future__ import annotations
 
@@ -349,15 +356,47 @@ def make_delaunay_negcycle(R):
     np.savez_compressed(HERE / "delaunay_negcycle.npz", **out)
 
 
+def make_potential(R):
+    from refcpp import RefCCH
+    gm, CCH = R["graphs"], R["cch"].CCH
+    fam = np.load(HERE / "family.npz")
+    out = {}
+    for ci in range(int(fam["cases"])):
+        pre = f"c{ci}_"
+        n = int(fam[pre + "n"])
+        off, tgt, w = fam[pre + "off"], fam[pre + "tgt"], fam[pre + "w"]
+        g = gm.Graph(n)
+        for u in range(n):
+            for k in range(off[u], off[u + 1]):
+                g.add_edge(u, int(tgt[k]), float(w[k]))
+        c = CCH(g, order=[int(r) for r in fam[pre + "rank"]], log=lambda *_: None)
+        assert list(c.first) == fam[pre + "first"].tolist() and list(c.head) == fam[pre + "head"].tolist()
+        assert not c.customize(g)
+        assert np.array_equal(to_i32(c.up), fam[pre + "up"])
+        out[pre + "p"] = to_i64(c.potential())
+    z = np.load(HERE / "grid64.npz")
+    ref = RefCCH(dict(n=int(z["n"]), off=z["off"], tgt=z["tgt"], x=z["x"], y=z["y"]))
+    ref.set_order(z["rank"])
+    ref.symbolic()
+    up, dn, _ = ref.customize(z["w"].astype(np.float64))
+    assert np.array_equal(to_i32(up), z["up"])
+    out["grid64_p"] = to_i64(ref.cch_potential(up, dn))
+    out["cases"] = fam["cases"]
+    np.savez_compressed(HERE / "potential.npz", **out)
+    print(f"potential.npz: {int(fam['cases'])} family graphs + grid64, min p {out['grid64_p'].min()}")
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--only", default="")
     args = ap.parse_args()
     R = import_reference(Path(args.reference))
-    make_techniques(R)
-    make_family(R)
-    make_grid64(R)
-    make_delaunay_negcycle(R)
+    makers = dict(techniques=make_techniques, family=make_family, grid64=make_grid64,
+                  delaunay_negcycle=make_delaunay_negcycle, potential=make_potential)
+    only = [s for s in args.only.split(",") if s] or list(makers)
+    for name in only:
+        makers[name](R)
 
 
 if __name__ == "__main__":

@@ -319,3 +319,40 @@ def test_customize_batch(gpu, oracle):
     assert np.array_equal(fu, bu) and np.array_equal(fd, bd)
     for k in (0, 1, 3, 4, 5):
         assert gpu.equal(b.up[k], before[0][k]) and gpu.equal(b.dn[k], before[1][k])
+
+
+@pytest.mark.parametrize("storage", ["int32", "int64"])
+def test_potential_golden(gpu, storage):
+    """The device potential equals the reference's cch_potential / CCH.potential
+    (golden) on every family graph and grid64."""
+    P = load_golden("potential.npz")
+    F = load_golden("family.npz")
+    for i in range(int(P["cases"])):
+        c = family_case(F, i)
+        T = dev_topo(c)
+        m = T.customize(c["w"], storage)
+        p = T.potential(m).cpu().numpy()[c["rank"]]
+        assert np.array_equal(p, P[f"c{i}_p"])
+    z = load_golden("grid64.npz")
+    T = dev_topo(z)
+    p = T.potential(T.customize(z["w"], storage)).cpu().numpy()[z["rank"]]
+    assert np.array_equal(p, P["grid64_p"])
+
+
+@pytest.mark.parametrize("kind,n", [("delaunay", 50_000), ("road", 80_000)])
+def test_potential_against_oracle(gpu, oracle, kind, n):
+    """Larger graphs (big supernodes take the CTA kernels): equal to the
+    oracle's two sweeps and to Bellman-Ford from a virtual source; reduced
+    weights w(u,v) + p(u) - p(v) are non-negative."""
+    from nwcch.device import DeviceTopology
+    g, top = _seeded(kind, n, seed=21)
+    T = DeviceTopology.from_dict(top)
+    OT = oracle.Topo.from_dict(top)
+    oup, odn = oracle.customize(OT, g["w"])
+    m = T.customize(g["w"], "int32")
+    p = T.potential(m).cpu().numpy()
+    assert np.array_equal(p, oracle.potential(OT, oup, odn))
+    pv = p[top["rank"]]
+    assert np.array_equal(pv, oracle.virtual_source_potential(g["n"], g["off"], g["tgt"], g["w"]))
+    src = np.repeat(np.arange(g["n"]), np.diff(g["off"]))
+    assert np.all(g["w"].astype(np.int64) + pv[src] - pv[g["tgt"]] >= 0)

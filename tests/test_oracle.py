@@ -119,3 +119,21 @@ def test_bellman_ford_pins_queries(oracle):
         sel = np.nonzero(z["qs"] == s)[0]
         for q in sel:
             assert dist[z["qt"][q]] == z["ans"][q]
+
+
+def test_potential_against_reference(oracle):
+    """cpp/cch.cpp:631-655 / python/cch.py:734-755: the oracle's two-sweep
+    potential equals the reference's on every family graph and grid64, and
+    the Bellman-Ford potential from a virtual source."""
+    P = load_golden("potential.npz")
+    F = load_golden("family.npz")
+    for i in range(int(P["cases"])):
+        c = family_case(F, i)
+        T = topo(oracle, c)
+        p = oracle.potential(T, i32_to_i64(c["up"]), i32_to_i64(c["dn"]))[c["rank"]]
+        assert np.array_equal(p, P[f"c{i}_p"])
+        assert np.array_equal(p, oracle.virtual_source_potential(int(c["n"]), c["off"], c["tgt"], c["w"]))
+    z = load_golden("grid64.npz")
+    p = oracle.potential(topo(oracle, z), i32_to_i64(z["up"]), i32_to_i64(z["dn"]))[z["rank"]]
+    assert np.array_equal(p, P["grid64_p"])
+    assert np.array_equal(p, oracle.virtual_source_potential(int(z["n"]), z["off"], z["tgt"], z["w"]))
