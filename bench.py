@@ -203,6 +203,16 @@ def run_ours(args, W, world):
     if W["w_bad"] is not None:
         assert neg > 0, "injected negative cycle not detected"
     assert T.negative_cycle_arcs(good) == 0
+    # the autotuner picks the query schedule on a sample of this workload
+    tuned = None
+    if not args.no_tune:
+        from nwcch import tune
+        k = min(W["qs"].size, 8192)
+        r = tune.tune_queries(T, good, W["qs"][:k], W["qt"][:k], reps=2)
+        tuned = {"sample_queries": k, **r["best"], "sample_ms": r["ms"],
+                 "default_ms": next(x["ms"] for x in r["trials"] if x["query_dense_rows"] == 16
+                                    and x["query_occupancy"] == 1 and x["labels"] == "auto")}
+        log(f"query schedule: {tuned}")
 
     def step(ev0=None, ev1=None):
         if ev0 is not None:
@@ -281,9 +291,31 @@ def run_ours(args, W, world):
         t0 = time.perf_counter()
         T.query_batch(good, qs[i:i + 1], qt[i:i + 1])
         lat.append((time.perf_counter() - t0) * 1e6)
-    return dict(T=T, cust_ms=cust_ms, q_ms=q_ms, wall=wall, plain_ms=plain_ms, plain_equal=same, e2e_ms=e2e_ms,
-                plain_q_ms=plain_q_ms,
+    # the CCH potential of the conservative metric (two sweeps)
+    pot_ms = []
+    for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        pot = T.potential(good)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        pot_ms.append(e0.elapsed_time(e1))
+    good_host = good.to_numpy()
+    return dict(T=T, tuned=tuned, cust_ms=cust_ms, q_ms=q_ms, wall=wall, plain_ms=plain_ms, plain_equal=same,
+                e2e_ms=e2e_ms,
+                plain_q_ms=plain_q_ms, pot_ms=pot_ms, pot=pot.cpu().numpy(), good_host=good_host,
                 lat_us=lat, clocks=clocks.summary(), neg=neg_k, saturated=bool(sat))
+
+
+def cpu_potential(W, good_host, pot_dev):
+    """The oracle's two-sweep potential (single thread, like the reference's
+    cch_potential) on the same customized metric; equal to the device's."""
+    import oracle as orc
+    OT = orc.Topo.from_dict(W["top"])
+    t0 = time.perf_counter()
+    p = orc.potential(OT, *good_host)
+    ms = (time.perf_counter() - t0) * 1000
+    return dict(ms=ms, equal=bool(np.array_equal(p, pot_dev)))
 
 
 def batched_bytes(n, m, m_plus, triangles, k, s_w=4):
@@ -465,6 +497,7 @@ def main():
     ap.add_argument("--serve-workload", default="delaunay1m", choices=list(WORKLOADS) + ["none"])
     ap.add_argument("--serve-loads", default="1e4,1e5,1e6", help="offered query loads (queries/s)")
     ap.add_argument("--serve-seconds", type=float, default=1.0)
+    ap.add_argument("--no-tune", action="store_true", help="keep the default query schedule")
     ap.add_argument("--plain-steps", type=int, default=-1,
                     help="plain per-level customizations to time (-1: one, none above 5M vertices)")
     args = ap.parse_args()
@@ -519,6 +552,7 @@ def main():
     B = algorithmic_bytes(top["n"], top["e_arc"].size, T.m_plus, T.triangles)
     achieved = B / (cust / 1000) / 1e9
     cb = cpu_baseline(W, args.cpu_budget)
+    cp = cpu_potential(W, R["good_host"], R["pot"])
     line = {
         "metric": METRIC, "value": round(cust_total * 1000 / replica_units(args.steps, world), 4), "unit": UNIT,
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -535,12 +569,15 @@ def main():
         "plain_customize_ms": round(statistics.median(R["plain_ms"]), 3) if R["plain_ms"] else None,
         "plain_equals_supernodal": R["plain_equal"],
         "queries_per_s": round(nq / (qms / 1000) * world, 1), "query_batch_ms": round(qms, 4),
+        "query_schedule": R["tuned"],
         "plain_queries_per_s": round(nq / (R["plain_q_ms"] / 1000) * world, 1),
         "query_latency_us": {"p50": round(lat[len(lat) // 2], 2), "p99": round(lat[max(0, int(len(lat) * 0.99) - 1)], 2),
                              "mode": "one query per call, host-timed"},
         "e2e": {"value": round(statistics.median(R["e2e_ms"]), 4), "unit": "ms",
                 "h2d_bytes_per_step": int(W["w"].size * 4), "d2h_bytes_per_step": 8},
-        "gpu_launches": (2 + T.sn_launches + 1 + 1) * args.steps,
+        # per timed step: k_fill2 + k_base + the supernodal launches, the
+        # scan, and the query batch's k_maxabs + k_query_sn32 + k_query_sn
+        "gpu_launches": (2 + T.sn_launches + 1 + 3) * args.steps,
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "peak_source": peak_src,
                      "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": None,
                      "algorithmic_bytes_per_launch": int(B),
@@ -548,6 +585,9 @@ def main():
         "cpu_baseline": {"value": round(cb["value"], 3), "unit": "ms", "cores": cb["cores"], "kind": "port",
                          "sample": f"{cb['runs']} level-parallel customizations + scans of the same metric"},
         "clocks": R["clocks"],
+        "potential": {"gpu_ms": round(statistics.median(R["pot_ms"]), 3),
+                      "cpu_ms": round(cp["ms"], 1), "cpu_cores": 1, "cpu_kind": "port of cpp/cch.cpp:631-655",
+                      "equal": cp["equal"], "metric": "conservative (no injected cycle)"},
         "batched_customization": batch,
         "serving": serving,
     }

@@ -25,8 +25,9 @@
  *   - Pointers named *_dev are device pointers (cudaMalloc / torch CUDA
  *     tensors); all others are host pointers. `stream` is a cudaStream_t
  *     (NULL = legacy default stream).
- *   - A topology handle is immutable after creation and may be shared by
- *     calls on different streams; its error word is shared by those calls.
+ *   - A topology handle is immutable after creation (but for its tuned
+ *     schedules, nwcch_tune_set) and may be shared by calls on different
+ *     streams; each stream gets its own error word.
  */
 #ifndef NWCCH_H
 #define NWCCH_H
@@ -114,9 +115,22 @@ int nwcch_topology_destroy(nwcch_topology* t);
  * arc ids stored. */
 int nwcch_topology_info(const nwcch_topology* t, int64_t* info, int64_t len);
 
-/* Reads and clears the error word of `t` after asynchronous calls
- * (synchronizes `stream`). */
+/* Reads and clears the error word of `stream`'s calls on `t` (synchronizes
+ * `stream`). Each stream that enqueues work on a handle gets its own error
+ * word and scratch counters (64 per handle), so calls on different streams
+ * may overlap. */
 int nwcch_check(nwcch_topology* t, void* stream);
+
+/* Schedules picked by measurement (no counterpart in the reference: the
+ * autotuner of this library, python nwcch.tune, sets them per topology).
+ * Results never depend on them. */
+#define NWCCH_TUNE_QUERY_DENSE_ROWS 1      /* query chunks with fewer rows go row by row (1..33) */
+#define NWCCH_TUNE_QUERY_SMEM_LABELS_MAX 2 /* per-warp query label bytes kept in shared memory */
+#define NWCCH_TUNE_UPDATE_BUDGET_NS 3      /* update level-sweep budget before the dense finish (0: estimate) */
+#define NWCCH_TUNE_QUERY_OCCUPANCY 4       /* 1: query kernel unconstrained, 2: capped at 64 registers */
+#define NWCCH_TUNE_QUERY_CTA_MAX 5         /* batches of at most this many queries run a CTA per query */
+int nwcch_tune_set(nwcch_topology* t, int key, int64_t value);
+int nwcch_tune_get(const nwcch_topology* t, int key, int64_t* value);
 
 /* ------------------------------------------------------------------------
  * Customization. Replaces cch_nb.customize (python/cch_nb.py:529-563) and
@@ -241,6 +255,23 @@ int nwcch_query_batch_plain(nwcch_topology* t, const int32_t* up_dev, const int3
 int nwcch_query_batch_noalloc(nwcch_topology* t, const int32_t* up_dev, const int32_t* dn_dev,
                               const int32_t* s_rank_dev, const int32_t* t_rank_dev, int64_t nq,
                               int64_t* dist_dev, void* stream);
+
+/* ------------------------------------------------------------------------
+ * Shortest paths. Replaces CCH.query_path (python/cch.py:406-507): the
+ * distance and the vertices of a shortest s-t path (ranks, s first, t last),
+ * each shortcut unpacked through its lowest lower-triangle vertex whose two
+ * sides add up to it, with the reference's choices among equal-length paths.
+ * off_dev int64[nq+1] receives the offsets of every query's vertices in
+ * path_dev (capacity cap; an unreachable pair gets none); *needed = the total.
+ * If cap < *needed, NWCCH_ERR_CAPACITY with off_dev and *needed filled and
+ * nothing written to path_dev. Synchronous.
+ * ---------------------------------------------------------------------- */
+int nwcch_query_paths(nwcch_topology* t, const int32_t* up_dev, const int32_t* dn_dev,
+                      const int32_t* s_rank_dev, const int32_t* t_rank_dev, int64_t nq, int64_t* dist_dev,
+                      int64_t* off_dev, int32_t* path_dev, int64_t cap, int64_t* needed, void* stream);
+int nwcch_query_paths_i64(nwcch_topology* t, const int64_t* up_dev, const int64_t* dn_dev,
+                          const int32_t* s_rank_dev, const int32_t* t_rank_dev, int64_t nq, int64_t* dist_dev,
+                          int64_t* off_dev, int32_t* path_dev, int64_t cap, int64_t* needed, void* stream);
 
 /* ------------------------------------------------------------------------
  * CCH potential

@@ -390,4 +390,79 @@ __global__ void __launch_bounds__((TILE / MT) * (TILE / MT))
     if (e) atomicOr(err, e);
 }
 
+// ------------------------------------------------------------------ small supernodes
+
+// One warp customizes a whole small supernode (k <= 32 rows, trapezoid of at
+// most SN_WARP_CAP arcs): the trapezoid's rows are consecutive in the CSR, so
+// it is staged into shared memory with coalesced loads; the pivots run in
+// order (pivot i relaxes every later row j against row i: the triangles
+// (s0+i; s0+j, column l)); then every boundary pair (B[p], B[q]) takes the
+// minimum over the k rows and is scattered into the ancestors' arcs by
+// atomicMin through `rel`; the trapezoid is written back. Small supernodes
+// are most of a road-like graph, where a CTA per panel or 16x16 tile would
+// leave nearly all of its threads idle.
+template <class T, int WARPS>
+__global__ void __launch_bounds__(32 * WARPS) k_sn_warp(DevTopo D, SnDev S, const int32_t* __restrict__ items,
+                                                        int64_t count, T* __restrict__ up, T* __restrict__ dn,
+                                                        int* __restrict__ err) {
+    __shared__ T su[WARPS][SN_WARP_CAP];
+    __shared__ T sd[WARPS][SN_WARP_CAP];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    up += blockIdx.y * D.m_plus;
+    dn += blockIdx.y * D.m_plus;
+    T* U = su[wib];
+    T* Dn = sd[wib];
+    int e = 0;
+    for (int64_t it = (int64_t)blockIdx.x * WARPS + wib; it < count; it += (int64_t)gridDim.x * WARPS) {
+        const int32_t sn = items[3 * it];
+        const int32_t s0 = S.s0[sn], k = S.k[sn], b = S.b[sn];
+        const int32_t width = k + b;
+        const int64_t base = D.first[s0];
+        const int32_t total = (int32_t)(D.first[s0 + k] - base);
+        for (int x = lane; x < total; x += 32) {
+            U[x] = up[base + x];
+            Dn[x] = dn[base + x];
+        }
+        __syncwarp();
+        auto ro = [&](int i) { return i * (width - 1) - i * (i - 1) / 2; };  // row i's first arc
+        for (int i = 0; i + 1 < k; i++) {
+            const int ri = ro(i);
+            for (int j = i + 1; j < k; j++) {
+                const T dij = Dn[ri + (j - i - 1)], uij = U[ri + (j - i - 1)];
+                const int rj = ro(j);
+                for (int l = j + 1 + lane; l < width; l += 32) {
+                    const T uil = U[ri + (l - i - 1)], dil = Dn[ri + (l - i - 1)];
+                    const int ejl = rj + (l - j - 1);
+                    T v;
+                    if (splus(dij, uil, v, e) && v < U[ejl]) U[ejl] = v;
+                    if (splus(dil, uij, v, e) && v < Dn[ejl]) Dn[ejl] = v;
+                }
+            }
+            __syncwarp();
+        }
+        const int32_t* rel = S.rel + S.rel_off[sn];
+        for (int p = 0; p + 1 < b; p++) {
+            const int prow = p * (2 * b - p - 1) / 2 - p - 1;  // + q: pair (p, q)
+            for (int q = p + 1 + lane; q < b; q += 32) {
+                T cu = Lim<T>::INF, cd = Lim<T>::INF;
+                for (int i = 0; i < k; i++) {
+                    const int ri = ro(i) - i - 1 + k;
+                    T v;
+                    if (splus(Dn[ri + p], U[ri + q], v, e) && v < cu) cu = v;
+                    if (splus(Dn[ri + q], U[ri + p], v, e) && v < cd) cd = v;
+                }
+                const int32_t a = rel[prow + q];
+                if (cu != Lim<T>::INF) atomic_min_t(&up[a], cu);
+                if (cd != Lim<T>::INF) atomic_min_t(&dn[a], cd);
+            }
+        }
+        for (int x = lane; x < total; x += 32) {
+            up[base + x] = U[x];
+            dn[base + x] = Dn[x];
+        }
+        __syncwarp();
+    }
+    if (e) atomicOr(err, e);
+}
+
 }  // namespace nwcch

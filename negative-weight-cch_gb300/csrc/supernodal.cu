@@ -144,9 +144,14 @@ SnPlan* build_supernodal_plan(int64_t n, const int64_t* first, const int32_t* he
     }
     P->rel_entries = rel_off[ns];
     // work items per level
-    std::vector<std::vector<int32_t>> small(L), big(L), out_small(L), out_big(L);
+    std::vector<std::vector<int32_t>> small(L), big(L), out_small(L), out_big(L), warp(L);
     for (int64_t s = 0; s < ns; s++) {
         const int32_t l = lvl[s];
+        if (kv[s] == 1 && bv[s] < 2) continue;  // no triangle has its lowest vertex here
+        if (sn_warp_sized(kv[s], bv[s])) {
+            warp[l].insert(warp[l].end(), {(int32_t)s, 0, 0});
+            continue;
+        }
         if (kv[s] >= 2 && kv[s] <= SN_SMALL_K) small[l].push_back((int32_t)s);
         if (kv[s] > SN_SMALL_K) big[l].push_back((int32_t)s);
         const int32_t b = bv[s];
@@ -178,6 +183,7 @@ SnPlan* build_supernodal_plan(int64_t n, const int64_t* first, const int32_t* he
         P->launches.push_back(la);
     };
     for (int32_t l = 0; l < L; l++) {
+        add(SN_WARP, l, 0, warp[l]);
         std::vector<int32_t> v;
         for (int32_t s : small[l]) v.insert(v.end(), {s, 0, 0});
         add(SN_INT_SMALL, l, 0, v);
@@ -267,6 +273,13 @@ int run_supernodal(nwcch_topology* t, SnPlan* P, const int32_t* w, T* up, T* dn,
             case SN_OUT_SMALL:
                 k_sn_tile<T, 16, 2, true><<<dim3((unsigned)la.count, metrics), 64, 0, s>>>(D, P->dev, it, 0, up, dn, err);
                 break;
+            case SN_WARP: {
+                constexpr int WARPS = sizeof(T) == 4 ? 8 : 4;
+                const int64_t blocks = std::min<int64_t>((la.count + WARPS - 1) / WARPS, 152 * 64);
+                k_sn_warp<T, WARPS><<<dim3((unsigned)blocks, metrics), 32 * WARPS, 0, s>>>(D, P->dev, it, la.count, up,
+                                                                                           dn, err);
+                break;
+            }
             default:
                 return NWCCH_ERR_TOPOLOGY;
         }

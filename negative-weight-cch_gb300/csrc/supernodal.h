@@ -31,7 +31,14 @@ enum SnKind : int {
     SN_TRAIL = 2,      // CTA per (supernode, row tile, column tile): trailing update
     SN_OUT_BIG = 3,    // CTA per 64x64 tile of the outgoing boundary x boundary block
     SN_OUT_SMALL = 4,  // CTA per 16x16 tile of the same
+    SN_WARP = 5,       // warp per small supernode: the whole supernode in shared memory
 };
+
+// A supernode whose trapezoid holds at most this many arcs (and k <= 32,
+// b <= 64) is customized by one warp from shared memory in one launch.
+constexpr int SN_WARP_CAP = 512;
+inline int64_t sn_trapezoid(int64_t k, int64_t b) { return k * (k + b - 1) - k * (k - 1) / 2; }
+inline bool sn_warp_sized(int64_t k, int64_t b) { return k <= 32 && b <= 64 && sn_trapezoid(k, b) <= SN_WARP_CAP; }
 
 struct SnLaunch {
     int kind;

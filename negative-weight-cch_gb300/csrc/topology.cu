@@ -238,6 +238,46 @@ extern "C" int nwcch_topology_destroy(nwcch_topology* t) {
     return NWCCH_OK;
 }
 
+extern "C" int nwcch_tune_set(nwcch_topology* t, int key, int64_t value) {
+    if (!t) return NWCCH_ERR_ARG;
+    switch (key) {
+        case NWCCH_TUNE_QUERY_DENSE_ROWS:
+            if (value < 1 || value > 33) return NWCCH_ERR_ARG;
+            t->tune.query_dense_rows = (int32_t)value;
+            return NWCCH_OK;
+        case NWCCH_TUNE_QUERY_SMEM_LABELS_MAX:
+            if (value < 0) return NWCCH_ERR_ARG;
+            t->tune.query_smem_labels_max = value;
+            return NWCCH_OK;
+        case NWCCH_TUNE_UPDATE_BUDGET_NS:
+            if (value < 0) return NWCCH_ERR_ARG;
+            t->tune.update_budget_ns = value;
+            return NWCCH_OK;
+        case NWCCH_TUNE_QUERY_OCCUPANCY:
+            if (value < 1 || value > 2) return NWCCH_ERR_ARG;
+            t->tune.query_occupancy = (int32_t)value;
+            return NWCCH_OK;
+        case NWCCH_TUNE_QUERY_CTA_MAX:
+            if (value < 0) return NWCCH_ERR_ARG;
+            t->tune.query_cta_max = value;
+            return NWCCH_OK;
+        default:
+            return NWCCH_ERR_ARG;
+    }
+}
+
+extern "C" int nwcch_tune_get(const nwcch_topology* t, int key, int64_t* value) {
+    if (!t || !value) return NWCCH_ERR_ARG;
+    switch (key) {
+        case NWCCH_TUNE_QUERY_DENSE_ROWS: *value = t->tune.query_dense_rows; return NWCCH_OK;
+        case NWCCH_TUNE_QUERY_SMEM_LABELS_MAX: *value = t->tune.query_smem_labels_max; return NWCCH_OK;
+        case NWCCH_TUNE_UPDATE_BUDGET_NS: *value = t->tune.update_budget_ns; return NWCCH_OK;
+        case NWCCH_TUNE_QUERY_OCCUPANCY: *value = t->tune.query_occupancy; return NWCCH_OK;
+        case NWCCH_TUNE_QUERY_CTA_MAX: *value = t->tune.query_cta_max; return NWCCH_OK;
+        default: return NWCCH_ERR_ARG;
+    }
+}
+
 extern "C" int nwcch_topology_info(const nwcch_topology* t, int64_t* info, int64_t len) {
     if (!t || !info || len < 8) return NWCCH_ERR_ARG;
     info[0] = t->d.n;

@@ -30,6 +30,16 @@ struct DevTopo {
     const int32_t* aeidx;   // [...]     ... as original arc ids
 };
 
+// Schedules that depend on the graph and are picked by measurement
+// (nwcch_tune_set; python nwcch.tune).
+struct Tuning {
+    int32_t query_dense_rows = 16;          // query chunks with fewer rows go row by row
+    int64_t query_smem_labels_max = 8192;   // per-warp query labels above this go to global scratch
+    int32_t query_occupancy = 1;            // 2: 32-bit query kernel capped at 64 registers
+    int64_t query_cta_max = 152 * 8;        // batches up to this many queries: a CTA per query
+    int64_t update_budget_ns = 0;           // level-sweep budget of an update (0: from the triangle count)
+};
+
 // Device words private to the calls enqueued on one stream: the error word
 // and 16 scratch counters (scan results, query range flags). Calls on
 // different streams of one handle never share them, so they may overlap.
@@ -53,6 +63,7 @@ struct nwcch_topology {
     int32_t* level_verts = nullptr;           // device: vertices sorted by (level, rank)
     std::vector<int64_t> level_arc_off;       // [levels+1]: arcs bucketed by tail level
     int64_t* d_level_arc_off = nullptr;       // device copy
+    nwcch::Tuning tune;                       // measured schedules (defaults until tuned)
     std::mutex slot_mu;                       // guards the stream slot table
     std::vector<cudaStream_t> slot_stream;    // stream bound to each slot in use
     std::vector<nwcch::StreamSlot> slots;     // device words, preallocated at create

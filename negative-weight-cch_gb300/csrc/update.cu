@@ -518,6 +518,7 @@ long long sweep_budget_ns(const nwcch_topology* t) {
     const char* mode = getenv("NWCCH_UPDATE_MODE");
     if (mode && !strcmp(mode, "dense")) return 0;
     if (mode && !strcmp(mode, "incremental")) return LLONG_MAX;
+    if (t->tune.update_budget_ns > 0) return t->tune.update_budget_ns;
     return std::max<long long>(200000, (long long)(t->triangles / 200));
 }
 

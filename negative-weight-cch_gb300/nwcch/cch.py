@@ -92,6 +92,16 @@ class CCH:
         """Checks only the arcs the last update changed (python/cch.py:666-671)."""
         return self.dev.negative_loops(self.metric) > 0 or self.metric.stats.get("changed_negative", 0) > 0
 
+    def query_path(self, s, t):
+        """python/cch.py:406-507: (distance, [original vertices of a shortest
+        path]) with the reference's choice among equal-length paths; (inf, [])
+        if t is unreachable."""
+        dist, off, path = self.dev.query_paths(self.metric, self.rank[[s]], self.rank[[t]])
+        inv = np.empty_like(self.rank)
+        inv[self.rank] = np.arange(self.n)
+        p = path.cpu().numpy()
+        return float(distances_to_float(dist)[0]), [int(v) for v in inv[p]]
+
     def potential(self) -> np.ndarray:
         """python/cch.py:734-755: the feasible potential p(v) = min(0,
         min_u dist(u, v)) read off the customized metric, per ORIGINAL vertex

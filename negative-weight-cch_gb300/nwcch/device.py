@@ -44,6 +44,8 @@ for _name, _args in {
     "nwcch_query_batch": [P, P, P, P, P, I64, P, P],
     "nwcch_query_batch_i64": [P, P, P, P, P, I64, P, P],
     "nwcch_potential": [P, P, P, P, P],
+    "nwcch_query_paths": [P, P, P, P, P, I64, P, P, P, I64, PI64, P],
+    "nwcch_query_paths_i64": [P, P, P, P, P, I64, P, P, P, I64, PI64, P],
     "nwcch_potential_i64": [P, P, P, P, P],
 }.items():
     _lib.register(_name, _args)
@@ -351,6 +353,32 @@ class DeviceTopology:
         _status(fn(self.handle, m.up.data_ptr(), m.dn.data_ptr(), s.data_ptr(), t.data_ptr(), s.numel(),
                    out.data_ptr(), _stream(torch)), "query_batch")
         return out
+
+    def query_paths(self, m: Metric, s_rank, t_rank, cap: int = 0):
+        """Distances (int64 tensor) and shortest paths (python/cch.py:406-507)
+        as (dist, off, path): path[off[i]:off[i+1]] are the ranks of pair i's
+        path, s first (empty when unreachable). Synchronous."""
+        torch = self._torch
+        lib = _lib.lib()
+        s = torch.as_tensor(np.asarray(s_rank) if not isinstance(s_rank, torch.Tensor) else s_rank)
+        t = torch.as_tensor(np.asarray(t_rank) if not isinstance(t_rank, torch.Tensor) else t_rank)
+        s = s.to(device="cuda", dtype=torch.int32).contiguous()
+        t = t.to(device="cuda", dtype=torch.int32).contiguous()
+        nq = s.numel()
+        dist = torch.empty(nq, dtype=torch.int64, device="cuda")
+        off = torch.empty(nq + 1, dtype=torch.int64, device="cuda")
+        fn = lib.nwcch_query_paths if m.storage == "int32" else lib.nwcch_query_paths_i64
+        need = C.c_int64()
+        cap = max(int(cap), 64 * max(nq, 1))
+        while True:
+            path = torch.empty(cap, dtype=torch.int32, device="cuda")
+            rc = fn(self.handle, m.up.data_ptr(), m.dn.data_ptr(), s.data_ptr(), t.data_ptr(), nq, dist.data_ptr(),
+                    off.data_ptr(), path.data_ptr(), cap, C.byref(need), _stream(torch))
+            if rc == -7 and need.value > cap:  # NWCCH_ERR_CAPACITY: retry with the exact size
+                cap = int(need.value)
+                continue
+            _status(rc, "query_paths")
+            return dist, off, path[:int(need.value)]
 
     # ------------------------------------------------------------ potential
     def potential(self, m: Metric, out=None):

@@ -1,0 +1,139 @@
+"""Autotuner for the schedules of one topology.
+
+The kernels' results never depend on these choices, only their time does,
+and the best choice depends on the graph (depth, supernode sizes) and the
+batch size. Each tuner times its candidates on the device with CUDA events on
+a sample of the caller's own workload, checks that every candidate returns
+the same answers, and leaves the fastest one set on the topology
+(`nwcch_tune_set`):
+
+* queries: chunks below `dense_rows` rows go row by row instead of the
+  32-row (min,+) form; labels in shared memory or in global scratch; the
+  32-bit kernel with or without a 64-register cap;
+* updates: the time the level sweep may spend before the dense finish.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import itertools
+import statistics
+
+import numpy as np
+
+from . import _lib
+from .device import DeviceTopology, Metric
+
+KEYS = {"query_dense_rows": 1, "query_smem_labels_max": 2, "update_budget_ns": 3, "query_occupancy": 4,
+        "query_cta_max": 5}
+
+_lib.register("nwcch_tune_set", [C.c_void_p, C.c_int, C.c_int64])
+_lib.register("nwcch_tune_get", [C.c_void_p, C.c_int, C.POINTER(C.c_int64)])
+
+
+def get(topo: DeviceTopology, key: str) -> int:
+    v = C.c_int64()
+    _lib.check(_lib.lib().nwcch_tune_get(topo.handle, KEYS[key], C.byref(v)), "tune_get")
+    return int(v.value)
+
+
+def set(topo: DeviceTopology, key: str, value: int) -> None:  # noqa: A001 - mirrors nwcch_tune_set
+    _lib.check(_lib.lib().nwcch_tune_set(topo.handle, KEYS[key], int(value)), "tune_set")
+
+
+def _time(torch, fn, reps: int) -> float:
+    stream = torch.cuda.current_stream()
+    fn()  # warm-up (allocations, first-launch costs)
+    out = []
+    for _ in range(reps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        out.append(e0.elapsed_time(e1))
+    return statistics.median(out)
+
+
+def tune_queries(topo: DeviceTopology, metric: Metric, s_rank, t_rank, reps: int = 3,
+                 dense_rows=(1, 8, 16, 24, 33), occupancy=(1, 2), labels=("auto", "global", "shared")) -> dict:
+    """Times every candidate schedule on the batch (s_rank, t_rank) and keeps
+    the fastest. Returns {"best": {...}, "ms": best time, "trials": [...]}."""
+    import torch
+    s = torch.as_tensor(np.asarray(s_rank, np.int32)).cuda()
+    t = torch.as_tensor(np.asarray(t_rank, np.int32)).cuda()
+    out = torch.empty(s.numel(), dtype=torch.int64, device="cuda")
+    smem_max = {"auto": 8192, "global": 0, "shared": 1 << 40}
+    before = {k: get(topo, k) for k in ("query_dense_rows", "query_smem_labels_max", "query_occupancy")}
+    ref = None
+    trials = []
+    try:
+        for dr, occ, lab in itertools.product(dense_rows, occupancy, labels):
+            set(topo, "query_dense_rows", dr)
+            set(topo, "query_occupancy", occ)
+            set(topo, "query_smem_labels_max", smem_max[lab])
+            ms = _time(torch, lambda: topo.query_batch(metric, s, t, out=out), reps)
+            res = out.clone()
+            if ref is None:
+                ref = res
+            elif not torch.equal(ref, res):
+                raise AssertionError(f"query schedule {dr, occ, lab} changed the answers")
+            trials.append({"query_dense_rows": dr, "query_occupancy": occ, "labels": lab, "ms": round(ms, 4)})
+    except BaseException:
+        for k, v in before.items():
+            set(topo, k, v)
+        raise
+    best = min(trials, key=lambda r: r["ms"])
+    set(topo, "query_dense_rows", best["query_dense_rows"])
+    set(topo, "query_occupancy", best["query_occupancy"])
+    set(topo, "query_smem_labels_max", smem_max[best["labels"]])
+    # then the form for this batch size: a warp or a CTA per query
+    nq = s.numel()
+    cta_before = get(topo, "query_cta_max")
+    forms = {}
+    for form, cta_max in (("warp", 0), ("cta", nq)):
+        set(topo, "query_cta_max", cta_max)
+        forms[form] = _time(torch, lambda: topo.query_batch(metric, s, t, out=out), reps)
+        if not torch.equal(ref, out):
+            set(topo, "query_cta_max", cta_before)
+            raise AssertionError(f"query form {form} changed the answers")
+        trials.append({**{k: best[k] for k in ("query_dense_rows", "query_occupancy", "labels")}, "form": form,
+                       "ms": round(forms[form], 4)})
+    form = min(forms, key=forms.get)
+    set(topo, "query_cta_max", max(cta_before, nq) if form == "cta" else min(cta_before, nq - 1))
+    return {"best": {**{k: best[k] for k in ("query_dense_rows", "query_occupancy", "labels")}, "form": form},
+            "ms": round(min(forms.values()), 4), "trials": trials}
+
+
+def tune_update(topo: DeviceTopology, metric: Metric, sizes=(1, 10, 100), factors=(0.25, 0.5, 1.0, 2.0),
+                seed: int = 0) -> dict:
+    """Times raise-and-restore update pairs of each size under sweep budgets
+    of `factors` x the default estimate (about half a full customization) and
+    keeps the budget with the least total time. The metric ends as it began."""
+    import torch
+    rng = np.random.default_rng(seed)
+    w0 = metric.w.cpu().numpy().copy()
+    default = max(200_000, topo.triangles // 200)
+    before = get(topo, "update_budget_ns")
+    trials = []
+    try:
+        for f in factors:
+            set(topo, "update_budget_ns", max(1, int(default * f)))
+            total = 0.0
+            for k in sizes:
+                idx = rng.choice(topo.m, size=k, replace=False)
+                raised = w0[idx].astype(np.int64) + 1 + rng.integers(0, 50, k)
+                for val in (raised, w0[idx]):
+                    torch.cuda.synchronize()
+                    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                    e0.record()
+                    topo.update(metric, idx, val)
+                    e1.record()
+                    torch.cuda.synchronize()
+                    total += e0.elapsed_time(e1)
+            trials.append({"factor": f, "budget_ns": int(default * f), "ms": round(total, 3)})
+    except BaseException:
+        set(topo, "update_budget_ns", before)
+        raise
+    best = min(trials, key=lambda r: r["ms"])
+    set(topo, "update_budget_ns", best["budget_ns"])
+    return {"best": best, "trials": trials}

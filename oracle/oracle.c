@@ -430,6 +430,129 @@ int orc_virtual_source_potential(int64_t n, const int64_t* off, const int32_t* t
     return r;
 }
 
+static int64_t arc_of(const int64_t* first, const int32_t* head, int64_t lo, int64_t hi) {
+    int64_t a = first[lo], b = first[lo + 1];
+    while (a < b) {
+        const int64_t mid = (a + b) / 2;
+        if (head[mid] < hi) a = mid + 1;
+        else b = mid;
+    }
+    return (a < first[lo + 1] && head[a] == hi) ? a : -1;
+}
+
+int64_t orc_query_path(int64_t n, const int64_t* first, const int32_t* head, const int64_t* parent,
+                       const int32_t* tail, const int64_t* doff, const int32_t* darc, const int64_t* up,
+                       const int64_t* dn, int64_t s, int64_t t, int64_t* dist, int64_t* path, int64_t cap) {
+    int64_t* df = (int64_t*)malloc((size_t)n * sizeof(int64_t));
+    int64_t* dr = (int64_t*)malloc((size_t)n * sizeof(int64_t));
+    int64_t* pf = (int64_t*)malloc((size_t)n * sizeof(int64_t));
+    int64_t* pr = (int64_t*)malloc((size_t)n * sizeof(int64_t));
+    unsigned char* anc = (unsigned char*)calloc((size_t)n, 1);
+    int64_t* legs = (int64_t*)malloc((size_t)(4 * n + 4) * sizeof(int64_t));
+    int64_t* stack = (int64_t*)malloc((size_t)(4 * n + 4) * sizeof(int64_t));
+    int64_t len = 0, nlegs = 0;
+    for (int64_t v = 0; v < n; v++) {
+        df[v] = dr[v] = ORC_INF;
+        pf[v] = pr[v] = -1;
+    }
+    /* python/cch.py:413-440: sweeps recording the first arc reaching each label */
+    df[s] = 0;
+    dr[t] = 0;
+    for (int64_t x = s; x >= 0; x = parent[x])
+        if (df[x] != ORC_INF)
+            for (int64_t a = first[x]; a < first[x + 1]; a++) {
+                int64_t v;
+                if (add_ok(df[x], up[a], &v) && v < df[head[a]]) {
+                    df[head[a]] = v;
+                    pf[head[a]] = a;
+                }
+            }
+    for (int64_t x = t; x >= 0; x = parent[x])
+        if (dr[x] != ORC_INF)
+            for (int64_t a = first[x]; a < first[x + 1]; a++) {
+                int64_t v;
+                if (add_ok(dr[x], dn[a], &v) && v < dr[head[a]]) {
+                    dr[head[a]] = v;
+                    pr[head[a]] = a;
+                }
+            }
+    /* :441-452: the lowest common ancestor reaching the minimum */
+    for (int64_t x = t; x >= 0; x = parent[x]) anc[x] = 1;
+    int64_t best = ORC_INF, peak = -1;
+    for (int64_t x = s; x >= 0; x = parent[x]) {
+        int64_t v;
+        if (anc[x] && add_ok(df[x], dr[x], &v) && v < best) {
+            best = v;
+            peak = x;
+        }
+    }
+    *dist = best;
+    if (peak >= 0) {
+        /* :455-467: the shortcut legs, s -> peak, then peak -> t */
+        for (int64_t x = peak; x != s;) {
+            const int64_t v = tail[pf[x]];
+            legs[2 * nlegs] = v;
+            legs[2 * nlegs + 1] = x;
+            nlegs++;
+            x = v;
+        }
+        for (int64_t i = 0, j = nlegs - 1; i < j; i++, j--) {
+            const int64_t a0 = legs[2 * i], a1 = legs[2 * i + 1];
+            legs[2 * i] = legs[2 * j];
+            legs[2 * i + 1] = legs[2 * j + 1];
+            legs[2 * j] = a0;
+            legs[2 * j + 1] = a1;
+        }
+        for (int64_t x = peak; x != t;) {
+            const int64_t v = tail[pr[x]];
+            legs[2 * nlegs] = x;
+            legs[2 * nlegs + 1] = v;
+            nlegs++;
+            x = v;
+        }
+        /* :468-470, 482-501: unpack every leg */
+#define PUSH_VERTEX(v) do { if (len < cap) path[len] = (v); len++; } while (0)
+        PUSH_VERTEX(nlegs ? legs[0] : s);
+        for (int64_t l = 0; l < nlegs; l++) {
+            int64_t sp = 0;
+            stack[sp++] = legs[2 * l];
+            stack[sp++] = legs[2 * l + 1];
+            while (sp > 0) {
+                const int64_t w = stack[--sp], v = stack[--sp];
+                const int64_t lo = v < w ? v : w, hi = v < w ? w : v;
+                const int64_t a = arc_of(first, head, lo, hi);
+                const int64_t cost = v < w ? up[a] : dn[a];
+                int64_t mid = -1;
+                for (int64_t j = doff[lo]; j < doff[lo + 1] && mid < 0; j++) {
+                    const int64_t xl = darc[j], x = tail[xl];
+                    const int64_t xh = arc_of(first, head, x, hi);
+                    if (xh < 0) continue;
+                    const int64_t av = v == lo ? xl : xh, aw = w == lo ? xl : xh;
+                    int64_t c;
+                    if (add_ok(dn[av], up[aw], &c) && c == cost) mid = x;
+                }
+                if (mid < 0) {
+                    PUSH_VERTEX(w);
+                } else {
+                    stack[sp++] = mid;
+                    stack[sp++] = w;
+                    stack[sp++] = v;
+                    stack[sp++] = mid;
+                }
+            }
+        }
+#undef PUSH_VERTEX
+    }
+    free(df);
+    free(dr);
+    free(pf);
+    free(pr);
+    free(anc);
+    free(legs);
+    free(stack);
+    return len > cap ? -len : len;
+}
+
 int orc_has_negative_cycle(int64_t n, const int64_t* off, const int32_t* tgt, const int32_t* w) {
     int64_t* dist = (int64_t*)calloc((size_t)n, sizeof(int64_t));
     unsigned char* inq = (unsigned char*)calloc((size_t)n, 1);

@@ -80,4 +80,16 @@ void orc_potential(int64_t n, const int64_t* first, const int32_t* head, const i
 int orc_virtual_source_potential(int64_t n, const int64_t* off, const int32_t* tgt, const int32_t* w,
                                  int64_t* p);
 
+/* python/cch.py:406-507: distance and shortest path (ranks, s first) with the
+ * reference's choices among equal paths: the first arc (in sweep order) that
+ * reaches a label's value, the lowest common ancestor reaching the minimum,
+ * and each shortcut unpacked through its lowest lower-triangle vertex whose
+ * two sides add up to it. tail int32[m+]: lower endpoint of every arc;
+ * doff int64[n+1] / darc int32[m+]: arcs (x, y) grouped by y, ascending x.
+ * Writes *dist (ORC_INF if unreachable); returns the path length (0 if
+ * unreachable), or -(length) if cap is too small (nothing written then). */
+int64_t orc_query_path(int64_t n, const int64_t* first, const int32_t* head, const int64_t* parent,
+                       const int32_t* tail, const int64_t* doff, const int32_t* darc, const int64_t* up,
+                       const int64_t* dn, int64_t s, int64_t t, int64_t* dist, int64_t* path, int64_t cap);
+
 #endif

@@ -56,6 +56,8 @@ def lib():
             L.orc_virtual_source_potential.argtypes = [I64, P, P, P, P]
             L.orc_virtual_source_potential.restype = C.c_int
             L.orc_has_negative_cycle.restype = C.c_int
+            L.orc_query_path.argtypes = [I64, P, P, P, P, P, P, P, P, I64, I64, P, P, I64]
+            L.orc_query_path.restype = I64
             _lib = L
     return _lib
 
@@ -84,6 +86,17 @@ class Topo:
     @classmethod
     def from_dict(cls, t):
         return cls(t["n"], t["first"], t["head"], t["parent"], t["e_arc"], t["e_up"])
+
+    def lower_lists(self):
+        """tail int32[m+], and the arcs grouped by head (ascending tail):
+        doff int64[n+1], darc int32[m+] (built once)."""
+        if not hasattr(self, "_lower"):
+            tail = np.repeat(np.arange(self.n, dtype=np.int32), np.diff(self.first))
+            darc = np.argsort(self.head, kind="stable").astype(np.int32)
+            doff = np.zeros(self.n + 1, np.int64)
+            np.cumsum(np.bincount(self.head, minlength=self.n), out=doff[1:])
+            self._lower = (tail, doff, darc)
+        return self._lower
 
 
 def customize(T: Topo, w):
@@ -155,6 +168,21 @@ def virtual_source_potential(n, off, tgt, w):
     off, tgt, w = _c(off, np.int64), _c(tgt, np.int32), _c(w, np.int32)
     p = np.empty(n, np.int64)
     return None if lib().orc_virtual_source_potential(n, _p(off), _p(tgt), _p(w), _p(p)) else p
+
+
+def query_path(T: Topo, up, dn, s_rank: int, t_rank: int):
+    """python/cch.py:406-507 in rank space: (distance, int64 array of ranks)."""
+    up, dn = _c(up, np.int64), _c(dn, np.int64)
+    tail, doff, darc = T.lower_lists()
+    cap = 1024
+    while True:
+        path = np.empty(cap, np.int64)
+        d = C.c_int64()
+        n = lib().orc_query_path(T.n, _p(T.first), _p(T.head), _p(T.parent), _p(tail), _p(doff), _p(darc),
+                                 _p(up), _p(dn), int(s_rank), int(t_rank), C.byref(d), _p(path), cap)
+        if n >= 0:
+            return int(d.value), path[:n].copy()
+        cap = -n
 
 
 def to_float(a):

@@ -32,10 +32,15 @@ Fixtures (np.savez_compressed):
 * potential.npz   - the reference's CCH potential: CCH.potential
   (python/cch.py:734-755) on every family.npz graph rebuilt in the
   reference with the fixture's order, and cch_potential (cpp/cch.cpp:631-655)
-  on grid64.npz; original vertex ids.
+  on grid64.npz; original vertex ids;
+* paths.npz       - the reference's shortest paths, CCH.query_path
+  (python/cch.py:406-507), for the 50 query pairs of every family.npz graph:
+  distance and vertex list (original ids), the reference's choice among
+  equal-length paths.
 
 `--only NAME[,NAME]` regenerates some fixtures (techniques, family, grid64,
-delaunay_negcycle, potential); potential reads family.npz and grid64.npz.
+delaunay_negcycle, potential, paths); potential and paths read family.npz
+(potential also grid64.npz).
 """
 from __future__ import annotations
 
@@ -386,6 +391,44 @@ def make_potential(R):
     print(f"potential.npz: {int(fam['cases'])} family graphs + grid64, min p {out['grid64_p'].min()}")
 
 
+def _family_cch(R, fam, ci):
+    """A family.npz graph rebuilt in the reference with the fixture's order."""
+    gm, CCH = R["graphs"], R["cch"].CCH
+    pre = f"c{ci}_"
+    n = int(fam[pre + "n"])
+    off, tgt, w = fam[pre + "off"], fam[pre + "tgt"], fam[pre + "w"]
+    g = gm.Graph(n)
+    for u in range(n):
+        for k in range(off[u], off[u + 1]):
+            g.add_edge(u, int(tgt[k]), float(w[k]))
+    c = CCH(g, order=[int(r) for r in fam[pre + "rank"]], log=lambda *_: None)
+    assert list(c.first) == fam[pre + "first"].tolist() and list(c.head) == fam[pre + "head"].tolist()
+    assert not c.customize(g)
+    return g, c
+
+
+def make_paths(R):
+    fam = np.load(HERE / "family.npz")
+    out = {}
+    for ci in range(int(fam["cases"])):
+        pre = f"c{ci}_"
+        g, c = _family_cch(R, fam, ci)
+        dists, offs, verts = [], [0], []
+        for s, t in zip(fam[pre + "qs"], fam[pre + "qt"]):
+            d, path = c.query_path(int(s), int(t))
+            dists.append(d)
+            verts.extend(path)
+            offs.append(len(verts))
+            if path:  # the path realises the distance on the original graph
+                assert path[0] == s and path[-1] == t
+        out[pre + "dist"] = to_i64(dists)
+        out[pre + "off"] = np.array(offs, np.int64)
+        out[pre + "path"] = np.array(verts, np.int64)
+    out["cases"] = fam["cases"]
+    np.savez_compressed(HERE / "paths.npz", **out)
+    print(f"paths.npz: {int(fam['cases'])} family graphs x 50 pairs")
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default="/root/reference")
@@ -393,7 +436,7 @@ def main():
     args = ap.parse_args()
     R = import_reference(Path(args.reference))
     makers = dict(techniques=make_techniques, family=make_family, grid64=make_grid64,
-                  delaunay_negcycle=make_delaunay_negcycle, potential=make_potential)
+                  delaunay_negcycle=make_delaunay_negcycle, potential=make_potential, paths=make_paths)
     only = [s for s in args.only.split(",") if s] or list(makers)
     for name in only:
         makers[name](R)

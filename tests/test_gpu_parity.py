@@ -158,6 +158,17 @@ def test_query_forms_agree(gpu, oracle, kind, n):
         assert np.array_equal(T.query_batch(m, s, t).cpu().numpy(), want)
     finally:
         del os.environ["NWCCH_QUERY_GLOBAL_LABELS"]
+    # every schedule: a warp or a CTA per query, row-by-row or 32-row chunks,
+    # with or without the register cap
+    from nwcch import tune
+    for cta_max in (0, 1 << 30):
+        for rows in (1, 16, 33):
+            for occ in (1, 2):
+                tune.set(T, "query_cta_max", cta_max)
+                tune.set(T, "query_dense_rows", rows)
+                tune.set(T, "query_occupancy", occ)
+                assert np.array_equal(T.query_batch(m, s, t).cpu().numpy(), want), (cta_max, rows, occ)
+                assert np.array_equal(T.query_batch(m, s[:7], t[:7]).cpu().numpy(), want[:7])
 
 
 def test_large_weights_take_the_exact_path(gpu, oracle):
@@ -356,3 +367,64 @@ def test_potential_against_oracle(gpu, oracle, kind, n):
     assert np.array_equal(pv, oracle.virtual_source_potential(g["n"], g["off"], g["tgt"], g["w"]))
     src = np.repeat(np.arange(g["n"]), np.diff(g["off"]))
     assert np.all(g["w"].astype(np.int64) + pv[src] - pv[g["tgt"]] >= 0)
+
+
+@pytest.mark.parametrize("kind,n", [("delaunay", 30_000), ("road", 60_000)])
+def test_autotuner_keeps_answers(gpu, oracle, kind, n):
+    """Every query schedule the autotuner tries gives the same answers (it
+    asserts so), the chosen one equals the oracle, and an update budget is
+    picked with the metric left as it was."""
+    from nwcch import graphs as G
+    from nwcch import tune
+    from nwcch.device import DeviceTopology
+    g, top = _seeded(kind, n, seed=21)
+    T = DeviceTopology.from_dict(top)
+    OT = oracle.Topo.from_dict(top)
+    oup, odn = oracle.customize(OT, g["w"])
+    m = T.customize(g["w"], "int32")
+    s, t = G.random_pairs(g["n"], 2000, seed=12)
+    s, t = top["rank"][s], top["rank"][t]
+    r = tune.tune_queries(T, m, s, t, reps=1)
+    assert len(r["trials"]) == 5 * 2 * 3 + 2  # schedules, then the two forms
+    assert tune.get(T, "query_dense_rows") == r["best"]["query_dense_rows"]
+    assert np.array_equal(T.query_batch(m, s, t).cpu().numpy(), oracle.query_batch(OT, oup, odn, s, t))
+    before = m.to_numpy()
+    u = tune.tune_update(T, m, sizes=(1, 20), factors=(0.5, 1.0))
+    assert tune.get(T, "update_budget_ns") == u["best"]["budget_ns"]
+    after = m.to_numpy()
+    assert np.array_equal(before[0], after[0]) and np.array_equal(before[1], after[1])
+
+
+@pytest.mark.parametrize("storage", ["int32", "int64"])
+def test_query_paths_golden(gpu, storage):
+    """Device paths equal the reference's CCH.query_path (golden) on every
+    family graph: distances and vertex lists, ties broken the same way."""
+    Pz = load_golden("paths.npz")
+    F = load_golden("family.npz")
+    for i in range(int(Pz["cases"])):
+        c = family_case(F, i)
+        T = dev_topo(c)
+        m = T.customize(c["w"], storage)
+        dist, off, path = T.query_paths(m, gpu_ranks(c, "qs"), gpu_ranks(c, "qt"))
+        inv = np.empty_like(c["rank"])
+        inv[c["rank"]] = np.arange(c["rank"].size)
+        assert np.array_equal(dist.cpu().numpy(), Pz[f"c{i}_dist"])
+        assert np.array_equal(off.cpu().numpy(), Pz[f"c{i}_off"])
+        assert np.array_equal(inv[path.cpu().numpy()], Pz[f"c{i}_path"])
+
+
+def test_query_paths_against_oracle(gpu, oracle):
+    from nwcch import graphs as G
+    from nwcch.device import DeviceTopology
+    g, top = _seeded("road", 80_000, seed=21)
+    T = DeviceTopology.from_dict(top)
+    OT = oracle.Topo.from_dict(top)
+    oup, odn = oracle.customize(OT, g["w"])
+    m = T.customize(g["w"], "int32")
+    s, t = G.random_pairs(g["n"], 300, seed=3)
+    s, t = top["rank"][s], top["rank"][t]
+    dist, off, path = T.query_paths(m, s, t, cap=16)  # too small at first: the binding retries
+    dist, off, path = dist.cpu().numpy(), off.cpu().numpy(), path.cpu().numpy()
+    for i in range(s.size):
+        d, p = oracle.query_path(OT, oup, odn, s[i], t[i])
+        assert dist[i] == d and np.array_equal(path[off[i]:off[i + 1]], p)

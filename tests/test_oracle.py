@@ -137,3 +137,28 @@ def test_potential_against_reference(oracle):
     p = oracle.potential(topo(oracle, z), i32_to_i64(z["up"]), i32_to_i64(z["dn"]))[z["rank"]]
     assert np.array_equal(p, P["grid64_p"])
     assert np.array_equal(p, oracle.virtual_source_potential(int(z["n"]), z["off"], z["tgt"], z["w"]))
+
+
+def test_query_path_against_reference(oracle):
+    """python/cch.py:406-507: the oracle's paths are the reference's paths
+    (same choice among equal-length ones), and each realises its distance."""
+    Pz = load_golden("paths.npz")
+    F = load_golden("family.npz")
+    for i in range(int(Pz["cases"])):
+        c = family_case(F, i)
+        T = topo(oracle, c)
+        up, dn = i32_to_i64(c["up"]), i32_to_i64(c["dn"])
+        inv = np.empty_like(c["rank"])
+        inv[c["rank"]] = np.arange(c["rank"].size)
+        off, path, dist = Pz[f"c{i}_off"], Pz[f"c{i}_path"], Pz[f"c{i}_dist"]
+        wmap = {}
+        for u in range(int(c["n"])):
+            for k in range(c["off"][u], c["off"][u + 1]):
+                key = (u, int(c["tgt"][k]))
+                wmap[key] = min(wmap.get(key, INF), int(c["w"][k]))
+        for j, (s, t) in enumerate(zip(c["qs"], c["qt"])):
+            d, pr = oracle.query_path(T, up, dn, c["rank"][s], c["rank"][t])
+            assert d == dist[j]
+            assert np.array_equal(inv[pr], path[off[j]:off[j + 1]])
+            if pr.size:
+                assert sum(wmap[(int(a), int(b))] for a, b in zip(inv[pr][:-1], inv[pr][1:])) == d
