@@ -203,10 +203,14 @@ def run_ours(args, W, world):
     if W["w_bad"] is not None:
         assert neg > 0, "injected negative cycle not detected"
     assert T.negative_cycle_arcs(good) == 0
-    # the autotuner picks the query schedule on a sample of this workload
-    tuned = None
+    # the autotuner picks the customization and query schedules on this workload
+    tuned = cust_tuned = None
     if not args.no_tune:
         from nwcch import tune
+        rc = tune.tune_customize(T, w_dev, caps=(0, 256, 512), min_counts=(0, 1024), reps=2)
+        cust_tuned = {**rc["best"], "default_ms": next(x["ms"] for x in rc["trials"]
+                                                        if x["sn_warp_cap"] == 512 and x["sn_warp_min_count"] == 1024)}
+        log(f"customization schedule: {cust_tuned}")
         k = min(W["qs"].size, 8192)
         r = tune.tune_queries(T, good, W["qs"][:k], W["qt"][:k], reps=2)
         tuned = {"sample_queries": k, **r["best"], "sample_ms": r["ms"],
@@ -301,7 +305,7 @@ def run_ours(args, W, world):
         torch.cuda.synchronize()
         pot_ms.append(e0.elapsed_time(e1))
     good_host = good.to_numpy()
-    return dict(T=T, tuned=tuned, cust_ms=cust_ms, q_ms=q_ms, wall=wall, plain_ms=plain_ms, plain_equal=same,
+    return dict(T=T, tuned=tuned, cust_tuned=cust_tuned, cust_ms=cust_ms, q_ms=q_ms, wall=wall, plain_ms=plain_ms, plain_equal=same,
                 e2e_ms=e2e_ms,
                 plain_q_ms=plain_q_ms, pot_ms=pot_ms, pot=pot.cpu().numpy(), good_host=good_host,
                 lat_us=lat, clocks=clocks.summary(), neg=neg_k, saturated=bool(sat))
@@ -441,6 +445,18 @@ def run_serving(args, Ws, loads):
     W8 = G.scaled_metrics(g, 8, seed=21)
     keys = list(range(8))
     runs = []
+    # one customization of this topology, for scale (events, warm)
+    import torch
+    m0 = T.customize(W8[0], "int32")
+    cms = []
+    for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        T.customize(m0.w, "int32", out=m0, sync=False)
+        e1.record()
+        torch.cuda.synchronize()
+        cms.append(e0.elapsed_time(e1))
+    del m0
     for method in ("supernodal", "plain"):
         for rate in loads:
             if method == "plain" and rate > 1e5:
@@ -462,7 +478,8 @@ def run_serving(args, Ws, loads):
                           mean_batch=round((loop.batched_queries - q0) / max(1, nb), 1))
             log(f"serving: {st}")
             runs.append(st)
-    return {"workload": Ws["name"], "n": top["n"], "metrics": 8, "update_sizes": [1, 10, 100, 1000],
+    return {"workload": Ws["name"], "n": top["n"], "m_plus": T.m_plus, "triangles": T.triangles,
+            "customize_ms": round(statistics.median(cms), 3), "metrics": 8, "update_sizes": [1, 10, 100, 1000],
             "updates_per_s": 10, "latency": "scheduled arrival to answer on the host", "runs": runs}
 
 
@@ -570,6 +587,7 @@ def main():
         "plain_equals_supernodal": R["plain_equal"],
         "queries_per_s": round(nq / (qms / 1000) * world, 1), "query_batch_ms": round(qms, 4),
         "query_schedule": R["tuned"],
+        "customize_schedule": R["cust_tuned"],
         "plain_queries_per_s": round(nq / (R["plain_q_ms"] / 1000) * world, 1),
         "query_latency_us": {"p50": round(lat[len(lat) // 2], 2), "p99": round(lat[max(0, int(len(lat) * 0.99) - 1)], 2),
                              "mode": "one query per call, host-timed"},

@@ -129,6 +129,12 @@ int nwcch_check(nwcch_topology* t, void* stream);
 #define NWCCH_TUNE_UPDATE_BUDGET_NS 3      /* update level-sweep budget before the dense finish (0: estimate) */
 #define NWCCH_TUNE_QUERY_OCCUPANCY 4       /* 1: query kernel unconstrained, 2: capped at 64 registers */
 #define NWCCH_TUNE_QUERY_CTA_MAX 5         /* batches of at most this many queries run a CTA per query */
+/* Customization schedule: supernodes with k <= 32, b <= 64 and a trapezoid of
+ * at most SN_WARP_CAP (<= 512) arcs are customized by one warp each, in
+ * levels holding at least SN_WARP_MIN_COUNT of them. Setting either rebuilds
+ * the plan (synchronizes the device; no other call on the handle meanwhile). */
+#define NWCCH_TUNE_SN_WARP_CAP 6
+#define NWCCH_TUNE_SN_WARP_MIN_COUNT 7
 int nwcch_tune_set(nwcch_topology* t, int key, int64_t value);
 int nwcch_tune_get(const nwcch_topology* t, int key, int64_t* value);
 

@@ -46,17 +46,29 @@ __device__ __forceinline__ int64_t arc_at(const DevTopo& D, int32_t s0, int32_t 
 // ---------------------------------------------------------------- upward
 
 // Rows [i0, i0+rows) of a supernode: the diagonal block, by one warp.
+// Lane j's column of the diagonal block [i0, i0+rows): w(i0+r, i0+j) for
+// r < j, loaded up front so that the solve below is shuffles only.
+template <class T>
+__device__ __forceinline__ void diag_weights(const DevTopo& D, int32_t s0, int32_t i0, int rows, const T* W,
+                                             T (&u)[31]) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int r = 0; r < 31; r++)
+        u[r] = (r < lane && lane < rows) ? W[arc_at(D, s0, i0 + r, i0 + lane)] : Lim<T>::INF;
+}
+
 template <class T>
 __device__ void up_diagonal(const DevTopo& D, int32_t s0, int32_t i0, int rows, const T* __restrict__ up,
                             int64_t* p, int& e) {
     const int lane = threadIdx.x & 31;
     int64_t pj = lane < rows ? p[s0 + i0 + lane] : 0;
-    for (int r = 0; r + 1 < rows; r++) {
+    T u[31];
+    diag_weights<T>(D, s0, i0, rows, up, u);
+#pragma unroll
+    for (int r = 0; r < 31; r++) {
         const int64_t pr = __shfl_sync(FULL, (long long)pj, r);
-        if (lane > r && lane < rows) {
-            const int64_t c = label_plus(pr, up[arc_at(D, s0, i0 + r, i0 + lane)], e);
-            if (c < pj) pj = c;
-        }
+        const int64_t c = label_plus(pr, u[r], e);  // INF unless r < lane < rows
+        if (c < pj) pj = c;
     }
     if (lane < rows) p[s0 + i0 + lane] = pj;
 }
@@ -66,6 +78,7 @@ template <class T>
 __device__ __forceinline__ int64_t up_column(const DevTopo& D, int32_t s0, int32_t i0, int32_t i1, int32_t j,
                                              const T* __restrict__ up, const int64_t* p, int& e) {
     int64_t acc = INF64;
+#pragma unroll 8
     for (int32_t i = i0; i < i1; i++) acc = min(acc, label_plus(p[s0 + i], up[arc_at(D, s0, i, j)], e));
     return acc;
 }
@@ -140,11 +153,16 @@ __device__ void down_diagonal(const DevTopo& D, int32_t s0, int32_t i0, int rows
                               int64_t* p, int& e) {
     const int lane = threadIdx.x & 31;
     int64_t mine = lane < rows ? p[s0 + i0 + lane] : INF64;
-    for (int r = rows - 2; r >= 0; r--) {
-        int64_t c = INF64;
-        if (lane > r && lane < rows) c = label_plus(mine, dn[arc_at(D, s0, i0 + r, i0 + lane)], e);
-        c = warp_min64(c);
-        if (lane == r && c < mine) mine = c;
+    T u[31];
+    diag_weights<T>(D, s0, i0, rows, dn, u);
+#pragma unroll
+    for (int rr = 0; rr < 31; rr++) {
+        const int r = 30 - rr;  // bottom-up; constant indices keep u in registers
+        if (r <= rows - 2) {
+            int64_t c = label_plus(mine, u[r], e);  // INF unless r < lane < rows
+            c = warp_min64(c);
+            if (lane == r && c < mine) mine = c;
+        }
     }
     if (lane < rows) p[s0 + i0 + lane] = mine;
 }
@@ -204,6 +222,44 @@ __global__ void __launch_bounds__(256) k_pot_down_cta(DevTopo D, SnDev S, const 
     if (e) atomicOr(err, e);
 }
 
+// Single-vertex supernodes (k = 1, most of a road-like graph): a thread per
+// vertex. Upward: its value is final (its lower neighbours are in earlier
+// levels), push it along its row. Downward: its heads are final, pull.
+template <class T>
+__global__ void __launch_bounds__(256) k_pot_up_single(DevTopo D, SnDev S, const int32_t* __restrict__ sns,
+                                                       int64_t count, const T* __restrict__ up, int64_t* p, int* err) {
+    int e = 0;
+    for (int64_t it = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; it < count;
+         it += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t x = S.s0[sns[it]];
+        const int64_t px = p[x];
+        for (int64_t a = D.first[x]; a < D.first[x + 1]; a++) {
+            const int64_t c = label_plus(px, up[a], e);
+            if (c < 0) atomicMin(reinterpret_cast<long long*>(p + D.head[a]), (long long)c);
+        }
+    }
+    if (e) atomicOr(err, e);
+}
+
+template <class T>
+__global__ void __launch_bounds__(256) k_pot_down_single(DevTopo D, SnDev S, const int32_t* __restrict__ sns,
+                                                         int64_t count, const T* __restrict__ dn, int64_t* p,
+                                                         int* err) {
+    int e = 0;
+    for (int64_t it = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; it < count;
+         it += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t x = S.s0[sns[it]];
+        int64_t best = p[x];
+        for (int64_t a = D.first[x]; a < D.first[x + 1]; a++) best = min(best, label_plus(p[D.head[a]], dn[a], e));
+        p[x] = best;
+    }
+    if (e) atomicOr(err, e);
+}
+
+int thread_grid(int64_t count) {
+    return (int)std::max<int64_t>(1, std::min<int64_t>((count + 255) / 256, 152 * 16));
+}
+
 int warp_grid(int64_t count) {
     return (int)std::max<int64_t>(1, std::min<int64_t>((count + 3) / 4, 152 * 64));
 }
@@ -211,33 +267,46 @@ int warp_grid(int64_t count) {
 }  // namespace
 
 template <class T>
-int potential(nwcch_topology* t, const T* up, const T* dn, int64_t* p, cudaStream_t s) {
-    auto* P = static_cast<SnPlan*>(t->sn_plan);
-    if (!P) return NWCCH_ERR_TOPOLOGY;
-    int* err = stream_slot(t, s).err;
+int potential_launches(nwcch_topology* t, SnPlan* P, const T* up, const T* dn, int64_t* p, int* err, cudaStream_t s) {
     const DevTopo& D = t->d;
     NWCCH_CUDA_TRY(cudaMemsetAsync(p, 0, sizeof(int64_t) * std::max<int64_t>(1, D.n), s));
     const int32_t L = P->levels;
     for (int32_t l = 0; l < L; l++) {
-        const int64_t off = P->sn_level_off[l], big = P->sn_level_big[l], cnt = P->sn_level_off[l + 1] - off;
-        if (big)
-            k_pot_up_cta<T><<<(unsigned)std::min<int64_t>(big, 152 * 8), 256, 0, s>>>(D, P->dev, P->d_sn_order + off,
-                                                                                   big, up, p, err);
-        if (cnt > big)
-            k_pot_up_warp<T><<<warp_grid(cnt - big), 128, 0, s>>>(D, P->dev, P->d_sn_order + off + big, cnt - big, up,
-                                                                  p, err);
+        const int64_t off = P->sn_level_off[l], big = P->sn_level_big[l], single = P->sn_level_single[l];
+        const int64_t cnt = P->sn_level_off[l + 1] - off;
+        const int32_t* o = P->d_sn_order + off;
+        if (big) k_pot_up_cta<T><<<(unsigned)std::min<int64_t>(big, 152 * 8), 256, 0, s>>>(D, P->dev, o, big, up, p, err);
+        if (single > big)
+            k_pot_up_warp<T><<<warp_grid(single - big), 128, 0, s>>>(D, P->dev, o + big, single - big, up, p, err);
+        if (cnt > single)
+            k_pot_up_single<T><<<thread_grid(cnt - single), 256, 0, s>>>(D, P->dev, o + single, cnt - single, up, p,
+                                                                         err);
     }
     for (int32_t l = L - 1; l >= 0; l--) {
-        const int64_t off = P->sn_level_off[l], big = P->sn_level_big[l], cnt = P->sn_level_off[l + 1] - off;
+        const int64_t off = P->sn_level_off[l], big = P->sn_level_big[l], single = P->sn_level_single[l];
+        const int64_t cnt = P->sn_level_off[l + 1] - off;
+        const int32_t* o = P->d_sn_order + off;
         if (big)
-            k_pot_down_cta<T><<<(unsigned)std::min<int64_t>(big, 152 * 8), 256, 0, s>>>(
-                D, P->dev, P->d_sn_order + off, big, dn, p, err);
-        if (cnt > big)
-            k_pot_down_warp<T><<<warp_grid(cnt - big), 128, 0, s>>>(D, P->dev, P->d_sn_order + off + big, cnt - big,
-                                                                    dn, p, err);
+            k_pot_down_cta<T><<<(unsigned)std::min<int64_t>(big, 152 * 8), 256, 0, s>>>(D, P->dev, o, big, dn, p, err);
+        if (single > big)
+            k_pot_down_warp<T><<<warp_grid(single - big), 128, 0, s>>>(D, P->dev, o + big, single - big, dn, p, err);
+        if (cnt > single)
+            k_pot_down_single<T><<<thread_grid(cnt - single), 256, 0, s>>>(D, P->dev, o + single, cnt - single, dn, p,
+                                                                           err);
     }
     NWCCH_CUDA_TRY(cudaGetLastError());
     return NWCCH_OK;
+}
+
+// The sweeps' launches (4 per supernode level) replay as one CUDA graph per
+// (up, dn, p) binding.
+template <class T>
+int potential(nwcch_topology* t, const T* up, const T* dn, int64_t* p, cudaStream_t s) {
+    auto* P = static_cast<SnPlan*>(t->sn_plan);
+    if (!P) return NWCCH_ERR_TOPOLOGY;
+    int* err = stream_slot(t, s).err;
+    SnGraph key{SN_GRAPH_POTENTIAL, (int)sizeof(T), 1, err, p, up, dn, nullptr, 0};
+    return launch_cached(P, key, s, [&](cudaStream_t cs) { return potential_launches<T>(t, P, up, dn, p, err, cs); });
 }
 
 }  // namespace nwcch

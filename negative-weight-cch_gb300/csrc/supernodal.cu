@@ -15,8 +15,11 @@
 // reference's serial loop bit for bit.
 //
 // Kernels per level:
-//   k_sn_int_small  warp per supernode with k <= 32: row i pushes its pairs;
-//   k_sn_panel      big supernodes, one 32-row panel: every CTA factors the
+//   k_sn_warp       small supernodes (k <= 32, b <= 64, trapezoid within a
+//                   tuned cap, in levels with many of them): one warp does
+//                   the whole supernode, internal and outgoing, from shared
+//                   memory;
+//   k_sn_panel      other supernodes, one 32-row panel: every CTA factors the
 //                   panel's 32x32 diagonal triangle in shared memory, then
 //                   each thread runs the panel recurrence down one column in
 //                   registers (columns are independent given that triangle);
@@ -70,7 +73,8 @@ void free_supernodal_plan(SnPlan* p) {
     delete p;
 }
 
-SnPlan* build_supernodal_plan(int64_t n, const int64_t* first, const int32_t* head, const int32_t* parent, int* rc) {
+SnPlan* build_supernodal_plan(int64_t n, const int64_t* first, const int32_t* head, const int32_t* parent,
+                              const SnPlanParams& prm, int* rc) {
     *rc = NWCCH_OK;
     auto* P = new (std::nothrow) SnPlan();
     if (!P) {
@@ -144,11 +148,17 @@ SnPlan* build_supernodal_plan(int64_t n, const int64_t* first, const int32_t* he
     }
     P->rel_entries = rel_off[ns];
     // work items per level
+    P->params = prm;
+    const int64_t cap = std::min<int64_t>(prm.warp_cap, SN_WARP_CAP);
+    auto warp_ok = [&](int64_t s) { return kv[s] <= 32 && bv[s] <= 64 && sn_trapezoid(kv[s], bv[s]) <= cap; };
+    std::vector<int64_t> warp_count(L, 0);
+    for (int64_t s = 0; s < ns; s++)
+        if (warp_ok(s)) warp_count[lvl[s]]++;
     std::vector<std::vector<int32_t>> small(L), big(L), out_small(L), out_big(L), warp(L);
     for (int64_t s = 0; s < ns; s++) {
         const int32_t l = lvl[s];
         if (kv[s] == 1 && bv[s] < 2) continue;  // no triangle has its lowest vertex here
-        if (sn_warp_sized(kv[s], bv[s])) {
+        if (warp_ok(s) && warp_count[l] >= prm.warp_min_count) {
             warp[l].insert(warp[l].end(), {(int32_t)s, 0, 0});
             continue;
         }
@@ -213,11 +223,13 @@ SnPlan* build_supernodal_plan(int64_t n, const int64_t* first, const int32_t* he
         add(SN_OUT_BIG, l, 0, out_big[l]);
     }
     P->items = (int64_t)items.size() / 3;
-    // supernodes by level, whole-CTA ones first within a level
+    // supernodes by level: whole-CTA ones, then warp ones, then single
+    // vertices (k = 1), which a thread each sweeps
     std::vector<int32_t> order;
     order.reserve(ns);
     P->sn_level_off.assign(L + 1, 0);
     P->sn_level_big.assign(L, 0);
+    P->sn_level_single.assign(L, 0);
     {
         std::vector<std::vector<int32_t>> by_level(L);
         for (int64_t s = 0; s < ns; s++) by_level[lvl[s]].push_back((int32_t)s);
@@ -227,7 +239,10 @@ SnPlan* build_supernodal_plan(int64_t n, const int64_t* first, const int32_t* he
                 if (sn_sweep_big(kv[s], bv[s])) order.push_back(s);
             P->sn_level_big[l] = (int64_t)order.size() - P->sn_level_off[l];
             for (int32_t s : by_level[l])
-                if (!sn_sweep_big(kv[s], bv[s])) order.push_back(s);
+                if (!sn_sweep_big(kv[s], bv[s]) && kv[s] > 1) order.push_back(s);
+            P->sn_level_single[l] = (int64_t)order.size() - P->sn_level_off[l];
+            for (int32_t s : by_level[l])
+                if (!sn_sweep_big(kv[s], bv[s]) && kv[s] == 1) order.push_back(s);
         }
         P->sn_level_off[L] = (int64_t)order.size();
     }
@@ -287,18 +302,16 @@ int run_supernodal(nwcch_topology* t, SnPlan* P, const int32_t* w, T* up, T* dn,
     return cudaGetLastError() == cudaSuccess ? NWCCH_OK : NWCCH_ERR_CUDA;
 }
 
-template <class T>
-int launch_supernodal(nwcch_topology* t, SnPlan* P, const int32_t* w, T* up, T* dn, cudaStream_t s, int metrics) {
+int launch_cached(SnPlan* P, const SnGraph& key, cudaStream_t s, const std::function<int(cudaStream_t)>& enqueue) {
     static const bool no_graph = getenv("NWCCH_NO_GRAPH") != nullptr;
     cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
     NWCCH_CUDA_TRY(cudaStreamIsCapturing(s, &cap));
-    int* err = stream_slot(t, s).err;
-    if (no_graph || cap != cudaStreamCaptureStatusNone) return run_supernodal<T>(t, P, w, up, dn, s, err, metrics);
+    if (no_graph || cap != cudaStreamCaptureStatusNone) return enqueue(s);
     std::lock_guard<std::mutex> lock(P->graph_mu);
-    const int storage = (int)sizeof(T);
     SnGraph* hit = nullptr;
     for (auto& g : P->graphs)
-        if (g.storage == storage && g.metrics == metrics && g.err == err && g.w == w && g.up == up && g.dn == dn)
+        if (g.kind == key.kind && g.storage == key.storage && g.metrics == key.metrics && g.err == key.err &&
+            g.w == key.w && g.up == key.up && g.dn == key.dn)
             hit = &g;
     if (!hit) {
         cudaStream_t cs;
@@ -306,7 +319,7 @@ int launch_supernodal(nwcch_topology* t, SnPlan* P, const int32_t* w, T* up, T* 
         cudaGraph_t graph = nullptr;
         int rc = NWCCH_OK;
         if (cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal) != cudaSuccess) rc = NWCCH_ERR_CUDA;
-        if (!rc) rc = run_supernodal<T>(t, P, w, up, dn, cs, err, metrics);
+        if (!rc) rc = enqueue(cs);
         if (cudaStreamEndCapture(cs, &graph) != cudaSuccess && !rc) rc = NWCCH_ERR_CUDA;
         cudaGraphExec_t exec = nullptr;
         if (!rc && cudaGraphInstantiate(&exec, graph, 0) != cudaSuccess) rc = NWCCH_ERR_CUDA;
@@ -319,12 +332,21 @@ int launch_supernodal(nwcch_topology* t, SnPlan* P, const int32_t* w, T* up, T* 
             cudaGraphExecDestroy(old->exec);
             P->graphs.erase(old);
         }
-        P->graphs.push_back(SnGraph{storage, metrics, err, w, up, dn, exec, 0});
+        SnGraph g = key;
+        g.exec = exec;
+        P->graphs.push_back(g);
         hit = &P->graphs.back();
     }
     hit->last_use = ++P->graph_clock;
     NWCCH_CUDA_TRY(cudaGraphLaunch(hit->exec, s));
     return NWCCH_OK;
+}
+
+template <class T>
+int launch_supernodal(nwcch_topology* t, SnPlan* P, const int32_t* w, T* up, T* dn, cudaStream_t s, int metrics) {
+    int* err = stream_slot(t, s).err;
+    SnGraph key{SN_GRAPH_CUSTOMIZE, (int)sizeof(T), metrics, err, w, up, dn, nullptr, 0};
+    return launch_cached(P, key, s, [&](cudaStream_t cs) { return run_supernodal<T>(t, P, w, up, dn, cs, err, metrics); });
 }
 
 template int launch_supernodal<int32_t>(nwcch_topology*, SnPlan*, const int32_t*, int32_t*, int32_t*, cudaStream_t, int);

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <functional>
 #include <mutex>
 #include <vector>
 
@@ -38,7 +39,6 @@ enum SnKind : int {
 // b <= 64) is customized by one warp from shared memory in one launch.
 constexpr int SN_WARP_CAP = 512;
 inline int64_t sn_trapezoid(int64_t k, int64_t b) { return k * (k + b - 1) - k * (k - 1) / 2; }
-inline bool sn_warp_sized(int64_t k, int64_t b) { return k <= 32 && b <= 64 && sn_trapezoid(k, b) <= SN_WARP_CAP; }
 
 struct SnLaunch {
     int kind;
@@ -48,19 +48,34 @@ struct SnLaunch {
     int64_t count;  // items
 };
 
-// A captured customization for one (storage, metrics, w, up, dn, err) binding.
+enum SnGraphKind : int { SN_GRAPH_CUSTOMIZE = 0, SN_GRAPH_POTENTIAL = 1 };
+
+// A captured launch sequence for one binding: (kind, storage, metrics, error
+// word, w or the output, up, dn).
 struct SnGraph {
+    int kind;
     int storage;
     int metrics;
     int* err;
     const void* w;
-    void* up;
-    void* dn;
+    const void* up;
+    const void* dn;
     cudaGraphExec_t exec;
     uint64_t last_use;
 };
 
+// Schedule choices of a plan (measured per topology; results never depend
+// on them): a supernode with k <= 32, b <= 64 and a trapezoid of at most
+// warp_cap arcs takes the warp kernel when its level holds at least
+// warp_min_count such supernodes (a throughput form: near the top of the
+// tree a lone supernode finishes sooner on the panel and tile kernels).
+struct SnPlanParams {
+    int32_t warp_cap = SN_WARP_CAP;
+    int64_t warp_min_count = 1024;
+};
+
 struct SnPlan {
+    SnPlanParams params;
     std::vector<SnGraph> graphs;  // up to 16, least recently used dropped first
     uint64_t graph_clock = 0;
     std::mutex graph_mu;
@@ -70,10 +85,12 @@ struct SnPlan {
     int64_t rel_entries = 0;
     int32_t max_b = 0;            // longest boundary of any supernode
     // supernodes grouped by level (the vertex sweeps of the potential):
-    // level l is sn_order[sn_level_off[l] .. sn_level_off[l+1]), its first
-    // sn_level_big[l] entries taking a whole CTA each, the rest a warp each
+    // level l is sn_order[sn_level_off[l] .. sn_level_off[l+1]): entries
+    // [0, sn_level_big[l]) take a whole CTA each, [sn_level_big[l],
+    // sn_level_single[l]) a warp each, the rest (single vertices) a thread
     std::vector<int64_t> sn_level_off;
     std::vector<int64_t> sn_level_big;
+    std::vector<int64_t> sn_level_single;
     int32_t* d_sn_order = nullptr;
     std::vector<SnLaunch> launches;
     SnDev dev{};
@@ -83,7 +100,8 @@ struct SnPlan {
 };
 
 // Builds the plan from the host copy of a topology; nullptr on failure.
-SnPlan* build_supernodal_plan(int64_t n, const int64_t* first, const int32_t* head, const int32_t* parent, int* rc);
+SnPlan* build_supernodal_plan(int64_t n, const int64_t* first, const int32_t* head, const int32_t* parent,
+                              const SnPlanParams& prm, int* rc);
 void free_supernodal_plan(SnPlan* p);
 
 // Enqueues a full customization on stream s (base values + every launch) of
@@ -109,5 +127,10 @@ int query_sn_async(nwcch_topology* t, const T* up, const T* dn, const int32_t* s
 template <class T>
 int launch_supernodal(nwcch_topology* t, SnPlan* P, const int32_t* w, T* up, T* dn, cudaStream_t s,
                       int metrics = 1);
+
+// Enqueues `enqueue`'s launches on s as a CUDA graph captured once per key
+// (16 kept per plan, least recently used dropped first); enqueues them
+// directly when s is being captured or NWCCH_NO_GRAPH is set.
+int launch_cached(SnPlan* P, const SnGraph& key, cudaStream_t s, const std::function<int(cudaStream_t)>& enqueue);
 
 }  // namespace nwcch

@@ -164,7 +164,7 @@ extern "C" int nwcch_topology_create(int64_t n, const int64_t* first, const int3
             for (int64_t k = 0; k < m; k++)
                 if (e_arc[k] >= 0) aeidx[fill[e_arc[k]]++] = (int32_t)k;
         }
-        t->sn_plan = build_supernodal_plan(n, first, head, parent, &rc);
+        t->sn_plan = build_supernodal_plan(n, first, head, parent, SnPlanParams{}, &rc);
         if (rc) break;
         t->device_bytes += static_cast<SnPlan*>(t->sn_plan)->bytes;
         t->triangles = tri;
@@ -238,9 +238,43 @@ extern "C" int nwcch_topology_destroy(nwcch_topology* t) {
     return NWCCH_OK;
 }
 
+namespace {
+
+// Rebuilds the supernodal plan with new schedule parameters from the device
+// copy of the topology. Every call on the handle must have completed (the
+// old plan's arrays and captured graphs may be in use until then).
+int replan(nwcch_topology* t, const SnPlanParams& prm) {
+    NWCCH_CUDA_TRY(cudaDeviceSynchronize());
+    const int64_t n = t->d.n, mp = t->d.m_plus;
+    std::vector<int64_t> first(n + 1);
+    std::vector<int32_t> head(std::max<int64_t>(1, mp)), parent(std::max<int64_t>(1, n));
+    NWCCH_CUDA_TRY(cudaMemcpy(first.data(), t->d.first, (n + 1) * 8, cudaMemcpyDeviceToHost));
+    if (mp) NWCCH_CUDA_TRY(cudaMemcpy(head.data(), t->d.head, mp * 4, cudaMemcpyDeviceToHost));
+    if (n) NWCCH_CUDA_TRY(cudaMemcpy(parent.data(), t->d.parent, n * 4, cudaMemcpyDeviceToHost));
+    int rc = NWCCH_OK;
+    SnPlan* P = build_supernodal_plan(n, first.data(), head.data(), parent.data(), prm, &rc);
+    if (!P) return rc ? rc : NWCCH_ERR_NOMEM;
+    auto* old = static_cast<SnPlan*>(t->sn_plan);
+    if (old) t->device_bytes -= old->bytes;
+    free_supernodal_plan(old);
+    t->sn_plan = P;
+    t->device_bytes += P->bytes;
+    return NWCCH_OK;
+}
+
+}  // namespace
+
 extern "C" int nwcch_tune_set(nwcch_topology* t, int key, int64_t value) {
     if (!t) return NWCCH_ERR_ARG;
     switch (key) {
+        case NWCCH_TUNE_SN_WARP_CAP:
+        case NWCCH_TUNE_SN_WARP_MIN_COUNT: {
+            if (value < 0 || !t->sn_plan) return NWCCH_ERR_ARG;
+            SnPlanParams prm = static_cast<SnPlan*>(t->sn_plan)->params;
+            if (key == NWCCH_TUNE_SN_WARP_CAP) prm.warp_cap = (int32_t)std::min<int64_t>(value, SN_WARP_CAP);
+            else prm.warp_min_count = value;
+            return replan(t, prm);
+        }
         case NWCCH_TUNE_QUERY_DENSE_ROWS:
             if (value < 1 || value > 33) return NWCCH_ERR_ARG;
             t->tune.query_dense_rows = (int32_t)value;
@@ -274,6 +308,13 @@ extern "C" int nwcch_tune_get(const nwcch_topology* t, int key, int64_t* value) 
         case NWCCH_TUNE_UPDATE_BUDGET_NS: *value = t->tune.update_budget_ns; return NWCCH_OK;
         case NWCCH_TUNE_QUERY_OCCUPANCY: *value = t->tune.query_occupancy; return NWCCH_OK;
         case NWCCH_TUNE_QUERY_CTA_MAX: *value = t->tune.query_cta_max; return NWCCH_OK;
+        case NWCCH_TUNE_SN_WARP_CAP:
+        case NWCCH_TUNE_SN_WARP_MIN_COUNT: {
+            if (!t->sn_plan) return NWCCH_ERR_ARG;
+            const SnPlanParams& prm = static_cast<const SnPlan*>(t->sn_plan)->params;
+            *value = key == NWCCH_TUNE_SN_WARP_CAP ? prm.warp_cap : prm.warp_min_count;
+            return NWCCH_OK;
+        }
         default: return NWCCH_ERR_ARG;
     }
 }

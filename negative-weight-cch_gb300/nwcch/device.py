@@ -156,8 +156,12 @@ class DeviceTopology:
         _lib.check(lib.nwcch_topology_create(self.n, _lib.ptr(first), _lib.ptr(head), _lib.ptr(parent), e_arc.size,
                                              _lib.ptr(e_arc), _lib.ptr(e_up), C.byref(h)), "topology_create")
         self._h = h
+        self.refresh_info()
+
+    def refresh_info(self):
+        """Re-reads the handle's figures (the plan's change when re-planned)."""
         info = np.zeros(12, np.int64)
-        _lib.check(lib.nwcch_topology_info(h, _lib.ptr(info), 12), "topology_info")
+        _lib.check(_lib.lib().nwcch_topology_info(self.handle, _lib.ptr(info), 12), "topology_info")
         (self.n, self.m_plus, self.m, self.triangles, self.levels, self.depth, self.max_row,
          self.device_bytes, self.supernodes, self.sn_levels, self.sn_launches,
          self.rel_entries) = (int(v) for v in info)

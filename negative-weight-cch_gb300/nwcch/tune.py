@@ -7,9 +7,12 @@ a sample of the caller's own workload, checks that every candidate returns
 the same answers, and leaves the fastest one set on the topology
 (`nwcch_tune_set`):
 
+* customization: which small supernodes one warp customizes whole (the
+  rest go through the panel and tile kernels); the plan is rebuilt for
+  each candidate;
 * queries: chunks below `dense_rows` rows go row by row instead of the
   32-row (min,+) form; labels in shared memory or in global scratch; the
-  32-bit kernel with or without a 64-register cap;
+  32-bit kernel with or without a 64-register cap; a warp or a CTA per query;
 * updates: the time the level sweep may spend before the dense finish.
 """
 from __future__ import annotations
@@ -24,7 +27,8 @@ from . import _lib
 from .device import DeviceTopology, Metric
 
 KEYS = {"query_dense_rows": 1, "query_smem_labels_max": 2, "update_budget_ns": 3, "query_occupancy": 4,
-        "query_cta_max": 5}
+        "query_cta_max": 5, "sn_warp_cap": 6, "sn_warp_min_count": 7}
+PLAN_KEYS = {"sn_warp_cap", "sn_warp_min_count"}
 
 _lib.register("nwcch_tune_set", [C.c_void_p, C.c_int, C.c_int64])
 _lib.register("nwcch_tune_get", [C.c_void_p, C.c_int, C.POINTER(C.c_int64)])
@@ -38,6 +42,41 @@ def get(topo: DeviceTopology, key: str) -> int:
 
 def set(topo: DeviceTopology, key: str, value: int) -> None:  # noqa: A001 - mirrors nwcch_tune_set
     _lib.check(_lib.lib().nwcch_tune_set(topo.handle, KEYS[key], int(value)), "tune_set")
+    if key in PLAN_KEYS:
+        topo.refresh_info()
+
+
+def tune_customize(topo: DeviceTopology, w, caps=(0, 128, 256, 512), min_counts=(0, 1024, 16384),
+                   reps: int = 3) -> dict:
+    """Re-plans the customization with each small-supernode schedule (which
+    supernodes one warp customizes: trapezoid of at most `cap` arcs, in
+    levels with at least `min_count` of them; cap 0 = none), times the
+    customization of w on each (CUDA events, captured graph replayed), checks
+    that the customized values never change, and keeps the fastest plan."""
+    import torch
+    wt = topo.weights(w)
+    m = topo.customize(wt, "int32")
+    ref = (m.up.clone(), m.dn.clone())
+    before = (get(topo, "sn_warp_cap"), get(topo, "sn_warp_min_count"))
+    cands = [(0, 0)] + [(c, k) for c in caps if c > 0 for k in min_counts]
+    trials = []
+    try:
+        for cap, cnt in cands:
+            set(topo, "sn_warp_cap", cap)
+            set(topo, "sn_warp_min_count", cnt)
+            ms = _time(torch, lambda: topo.customize(wt, "int32", out=m, sync=False), reps)
+            if not (torch.equal(ref[0], m.up) and torch.equal(ref[1], m.dn)):
+                raise AssertionError(f"customization schedule {(cap, cnt)} changed the values")
+            trials.append({"sn_warp_cap": cap, "sn_warp_min_count": cnt, "ms": round(ms, 4),
+                           "launches": topo.sn_launches})
+    except BaseException:
+        set(topo, "sn_warp_cap", before[0])
+        set(topo, "sn_warp_min_count", before[1])
+        raise
+    best = min(trials, key=lambda r: r["ms"])
+    set(topo, "sn_warp_cap", best["sn_warp_cap"])
+    set(topo, "sn_warp_min_count", best["sn_warp_min_count"])
+    return {"best": best, "trials": trials}
 
 
 def _time(torch, fn, reps: int) -> float:

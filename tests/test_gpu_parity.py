@@ -428,3 +428,23 @@ def test_query_paths_against_oracle(gpu, oracle):
     for i in range(s.size):
         d, p = oracle.query_path(OT, oup, odn, s[i], t[i])
         assert dist[i] == d and np.array_equal(path[off[i]:off[i + 1]], p)
+
+
+def test_customize_schedules_keep_values(gpu, oracle):
+    """Every customization schedule the autotuner tries (which small
+    supernodes one warp customizes; the plan is rebuilt each time) gives the
+    oracle's values, and the chosen one stays set."""
+    from nwcch import tune
+    from nwcch.device import DeviceTopology
+    g, top = _seeded("road", 80_000, seed=21)
+    T = DeviceTopology.from_dict(top)
+    oup, odn = oracle.customize(oracle.Topo.from_dict(top), g["w"])
+    r = tune.tune_customize(T, g["w"], caps=(0, 512), min_counts=(0, 4096), reps=1)
+    assert len(r["trials"]) == 3
+    assert tune.get(T, "sn_warp_cap") == r["best"]["sn_warp_cap"]
+    for cap, cnt in ((512, 0), (0, 0), (128, 64)):
+        tune.set(T, "sn_warp_cap", cap)
+        tune.set(T, "sn_warp_min_count", cnt)
+        for storage in ("int32", "int64"):
+            up, dn = T.customize(g["w"], storage).to_numpy()
+            assert np.array_equal(up, oup) and np.array_equal(dn, odn), (cap, cnt, storage)
