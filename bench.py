@@ -445,8 +445,22 @@ def run_serving(args, Ws, loads):
     W8 = G.scaled_metrics(g, 8, seed=21)
     keys = list(range(8))
     runs = []
-    # one customization of this topology, for scale (events, warm)
     import torch
+    tuned = None
+    if not args.no_tune:
+        # the autotuner on this topology: customization plan, the query
+        # schedule of a serving-sized batch, the update sweep budget
+        from nwcch import tune
+        rc = tune.tune_customize(T, W8[0], caps=(0, 256, 512), min_counts=(0, 1024), reps=2)
+        m0 = T.customize(W8[0], "int32")
+        sq, tq = G.random_pairs(top["n"], 512, seed=3)
+        rq = tune.tune_queries(T, m0, top["rank"][sq], top["rank"][tq], reps=2, dense_rows=(1, 8, 16),
+                               labels=("auto", "shared"))
+        ru = tune.tune_update(T, m0, sizes=(1, 10, 100, 1000), factors=(0.1, 0.25, 0.5, 1.0))
+        tuned = {"customize": rc["best"], "queries": rq["best"], "update_budget_ns": ru["best"]["budget_ns"]}
+        log(f"serving schedules: {tuned}")
+        del m0
+    # one customization of this topology, for scale (events, warm)
     m0 = T.customize(W8[0], "int32")
     cms = []
     for _ in range(3):
@@ -479,8 +493,52 @@ def run_serving(args, Ws, loads):
             log(f"serving: {st}")
             runs.append(st)
     return {"workload": Ws["name"], "n": top["n"], "m_plus": T.m_plus, "triangles": T.triangles,
-            "customize_ms": round(statistics.median(cms), 3), "metrics": 8, "update_sizes": [1, 10, 100, 1000],
+            "customize_ms": round(statistics.median(cms), 3), "schedules": tuned,
+            "metrics": 8, "update_sizes": [1, 10, 100, 1000],
             "updates_per_s": 10, "latency": "scheduled arrival to answer on the host", "runs": runs}
+
+
+def profile_part(args):
+    """One part of the hot path on the workload, --warmup then --steps times,
+    with a fixed schedule (plan parameters from the command line, default
+    query schedule): a small, repeatable command for ncu captures."""
+    import torch
+
+    from nwcch import tune
+    from nwcch.device import DeviceTopology
+    W = make_workload(args.workload, seed=0)
+    T = DeviceTopology.from_dict(W["top"])
+    if args.sn_warp_cap is not None:
+        tune.set(T, "sn_warp_cap", args.sn_warp_cap)
+    if args.sn_warp_min_count is not None:
+        tune.set(T, "sn_warp_min_count", args.sn_warp_min_count)
+    w = torch.from_numpy(W["w"]).cuda()
+    m = T.customize(w, "int32")
+    qs, qt = torch.from_numpy(W["qs"]).cuda(), torch.from_numpy(W["qt"]).cuda()
+    rng = np.random.default_rng(1)
+    idx = rng.choice(T.m, size=100, replace=False)
+    w0 = W["w"][idx].astype(np.int64)
+    parts = {
+        "customize": lambda i: T.customize(w, "int32", out=m, sync=False),
+        "potential": lambda i: T.potential(m),
+        "queries": lambda i: T.query_batch(m, qs, qt),
+        "update": lambda i: T.update(m, idx, w0 + (1 + i % 2)),
+    }
+    fn = parts[args.profile]
+    for i in range(args.warmup):
+        fn(i)
+    torch.cuda.synchronize()
+    times = []
+    for i in range(args.steps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        fn(i)
+        e1.record()
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1))
+    print(json.dumps({"profile": args.profile, "workload": args.workload, "ms": [round(x, 4) for x in times],
+                      "sn_launches": T.sn_launches, "sn_warp_cap": tune.get(T, "sn_warp_cap"),
+                      "sn_warp_min_count": tune.get(T, "sn_warp_min_count")}), flush=True)
 
 
 def cpu_baseline(W, budget_s: float):
@@ -517,9 +575,16 @@ def main():
     ap.add_argument("--no-tune", action="store_true", help="keep the default query schedule")
     ap.add_argument("--plain-steps", type=int, default=-1,
                     help="plain per-level customizations to time (-1: one, none above 5M vertices)")
+    ap.add_argument("--profile", choices=["customize", "potential", "queries", "update"],
+                    help="run only this part, --steps times after --warmup (for ncu captures); no bench line")
+    ap.add_argument("--sn-warp-cap", type=int, default=None, help="customization plan: warp-kernel trapezoid cap")
+    ap.add_argument("--sn-warp-min-count", type=int, default=None, help="customization plan: level threshold")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
+    if args.profile:
+        profile_part(args)
+        return
     if args.impl == "reference":
         if rank != 0:
             return

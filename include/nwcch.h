@@ -81,6 +81,15 @@ int nwcch_symbolic(int64_t n, const int64_t* noff, const int32_t* nbr, const int
 int nwcch_edge_arcs(int64_t n, const int64_t* off, const int32_t* tgt, const int32_t* rank,
                     const int64_t* first, const int32_t* head, int64_t* e_arc, int8_t* e_up);
 
+/* The same mapping computed on the device from device arrays (off_dev
+ * int64[n+1], tgt_dev int32[m], rank_dev int32[n], first_dev int64[n+1],
+ * head_dev int32[m+]) into e_arc_dev int64[m], e_up_dev int8[m].
+ * NWCCH_ERR_TOPOLOGY if an arc has no shortcut (the order's chordal graph
+ * does not hold it). Synchronous. */
+int nwcch_edge_arcs_device(int64_t n, const int64_t* off_dev, const int32_t* tgt_dev, const int32_t* rank_dev,
+                           const int64_t* first_dev, const int32_t* head_dev, int64_t* e_arc_dev, int8_t* e_up_dev,
+                           void* stream);
+
 /* Unique undirected edges (u < v, sorted) of a triangle list int64[ntri*3];
  * a helper of the synthetic graph generators (no reference counterpart). */
 int nwcch_triangle_edges(int64_t n, int64_t ntri, const int64_t* tri, int64_t** eu, int64_t** ev,
@@ -127,7 +136,8 @@ int nwcch_check(nwcch_topology* t, void* stream);
 #define NWCCH_TUNE_QUERY_DENSE_ROWS 1      /* query chunks with fewer rows go row by row (1..33) */
 #define NWCCH_TUNE_QUERY_SMEM_LABELS_MAX 2 /* per-warp query label bytes kept in shared memory */
 #define NWCCH_TUNE_UPDATE_BUDGET_NS 3      /* update level-sweep budget before the dense finish (0: estimate) */
-#define NWCCH_TUNE_QUERY_OCCUPANCY 4       /* 1: query kernel unconstrained, 2: capped at 64 registers */
+#define NWCCH_TUNE_QUERY_OCCUPANCY 4       /* 32-bit query kernel: 1 light, 2 light capped at 64 registers,
+                                              3 chunk labels and row offsets held in registers */
 #define NWCCH_TUNE_QUERY_CTA_MAX 5         /* batches of at most this many queries run a CTA per query */
 /* Customization schedule: supernodes with k <= 32, b <= 64 and a trapezoid of
  * at most SN_WARP_CAP (<= 512) arcs are customized by one warp each, in

@@ -287,7 +287,7 @@ __device__ __forceinline__ void rows32(const DevTopo& D, const int32_t* __restri
 // a CTA per query, the warps solving each chunk's 32x32 triangle redundantly
 // (no extra barrier; warp 0 alone writes labels and meets) and splitting the
 // chunk's column groups and the rows' entries between them.
-template <bool RECORD, bool MEET, int WARPS>
+template <bool RECORD, bool MEET, int WARPS, bool REGS = false>
 __device__ void sn_sweep32(const DevTopo& D, const SnDev& S, const int32_t* __restrict__ W, int32_t start,
                            int32_t dstart, int32_t* L, int32_t* chain, const int32_t* F, const int32_t* chain_s,
                            int32_t ds, int32_t& best, int dense_rows) {
@@ -336,20 +336,45 @@ __device__ void sn_sweep32(const DevTopo& D, const SnDev& S, const int32_t* __re
             // incrementally, so few registers stay live across the 32 loads
             const int32_t* Wb = W + base - c0 - 1;
             const int32_t st = (int32_t)step - 1;
-            for (int jb = c0 + n + 32 * wq; jb < cols; jb += 32 * WARPS) {
-                const int j = jb + lane;
-                const bool ok = j < cols;
-                int32_t acc = Q32::CINF;
-                int32_t ro = 0;
+            if (REGS) {
+                // the chunk's labels and row offsets held in registers across
+                // the column groups: fewer instructions per arc, more registers
+                int32_t fr[32], ro[32];
+                int32_t o = 0;
 #pragma unroll
                 for (int r = 0; r < 32; r++) {
-                    const int32_t fr = __shfl_sync(FULL, lab, r);
-                    if (ok && r < n) acc = __viaddmin_s32(fr, Q32::w(Wb[ro + j]), acc);
-                    ro += st - r;
+                    fr[r] = __shfl_sync(FULL, lab, r);
+                    ro[r] = o;
+                    o += st - r;
                 }
-                if (ok && !Q32::none(acc)) {
-                    const int32_t pj = j < k ? pos0 + (j - i0) : dstart - D.hdep[base + (j - c0 - 1)];
-                    if (acc < L[pj]) L[pj] = acc;
+                for (int jb = c0 + n + 32 * wq; jb < cols; jb += 32 * WARPS) {
+                    const int j = jb + lane;
+                    const bool ok = j < cols;
+                    int32_t acc = Q32::CINF;
+#pragma unroll
+                    for (int r = 0; r < 32; r++)
+                        if (ok && r < n) acc = __viaddmin_s32(fr[r], Q32::w(Wb[ro[r] + j]), acc);
+                    if (ok && !Q32::none(acc)) {
+                        const int32_t pj = j < k ? pos0 + (j - i0) : dstart - D.hdep[base + (j - c0 - 1)];
+                        if (acc < L[pj]) L[pj] = acc;
+                    }
+                }
+            } else {
+                for (int jb = c0 + n + 32 * wq; jb < cols; jb += 32 * WARPS) {
+                    const int j = jb + lane;
+                    const bool ok = j < cols;
+                    int32_t acc = Q32::CINF;
+                    int32_t ro = 0;
+#pragma unroll
+                    for (int r = 0; r < 32; r++) {
+                        const int32_t fr = __shfl_sync(FULL, lab, r);
+                        if (ok && r < n) acc = __viaddmin_s32(fr, Q32::w(Wb[ro + j]), acc);
+                        ro += st - r;
+                    }
+                    if (ok && !Q32::none(acc)) {
+                        const int32_t pj = j < k ? pos0 + (j - i0) : dstart - D.hdep[base + (j - c0 - 1)];
+                        if (acc < L[pj]) L[pj] = acc;
+                    }
                 }
             }
             qsync<WARPS>();
@@ -362,7 +387,7 @@ __device__ void sn_sweep32(const DevTopo& D, const SnDev& S, const int32_t* __re
 // Labels live in shared memory, or - for trees so deep that shared memory
 // would leave only a few warps per SM - in a global scratch (`gscratch`,
 // 12 * (depth + 1) + 16 bytes per warp, L1/L2-resident while in use).
-template <int MINB>
+template <int MINB, bool REGS>
 __global__ void __launch_bounds__(512, MINB) k_query_sn32(DevTopo D, SnDev S, const int32_t* __restrict__ up, const int32_t* __restrict__ dn,
                              const int32_t* __restrict__ s_rank, const int32_t* __restrict__ t_rank, int64_t nq,
                              int64_t* __restrict__ dist, const unsigned int* __restrict__ maxabs,
@@ -396,9 +421,9 @@ __global__ void __launch_bounds__(512, MINB) k_query_sn32(DevTopo D, SnDev S, co
         }
         __syncwarp();
         int32_t best = Q32::CINF;
-        sn_sweep32<true, false, 1>(D, S, up, s, ds, F, chain, nullptr, nullptr, 0, best, dense_rows);
+        sn_sweep32<true, false, 1, REGS>(D, S, up, s, ds, F, chain, nullptr, nullptr, 0, best, dense_rows);
         __syncwarp();
-        sn_sweep32<false, true, 1>(D, S, dn, t, dt, R, nullptr, F, chain, ds, best, dense_rows);
+        sn_sweep32<false, true, 1, REGS>(D, S, dn, t, dt, R, nullptr, F, chain, ds, best, dense_rows);
         for (int o = 16; o > 0; o >>= 1) best = min(best, __shfl_xor_sync(FULL, best, o));
         if (lane == 0) dist[q] = Q32::none(best) ? INF64 : (int64_t)best;
         __syncwarp();
@@ -552,7 +577,10 @@ int query_sn_async(nwcch_topology* t, const T* up, const T* dn, const int32_t* s
         const bool force_global = getenv("NWCCH_QUERY_GLOBAL_LABELS") != nullptr;  // for tests
         // register cap: MINB = 2 holds 64 registers (two 512-thread blocks
         // per SM) at the price of a few spills; MINB = 1 leaves the compiler free
-        auto kern = t->tune.query_occupancy >= 2 ? k_query_sn32<2> : k_query_sn32<1>;
+        // 3: chunk labels and row offsets in registers (the most registers)
+        auto kern = t->tune.query_occupancy == 3   ? k_query_sn32<1, true>
+                    : t->tune.query_occupancy == 2 ? k_query_sn32<2, false>
+                                                   : k_query_sn32<1, false>;
         const size_t cta_smem = (size_t)(((12 * Dp + 16) + 15) & ~15LL);
         if (nq <= t->tune.query_cta_max && cta_smem <= 200 * 1024) {
             // few queries: a CTA of 8 warps per query

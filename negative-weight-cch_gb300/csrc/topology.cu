@@ -288,7 +288,7 @@ extern "C" int nwcch_tune_set(nwcch_topology* t, int key, int64_t value) {
             t->tune.update_budget_ns = value;
             return NWCCH_OK;
         case NWCCH_TUNE_QUERY_OCCUPANCY:
-            if (value < 1 || value > 2) return NWCCH_ERR_ARG;
+            if (value < 1 || value > 3) return NWCCH_ERR_ARG;
             t->tune.query_occupancy = (int32_t)value;
             return NWCCH_OK;
         case NWCCH_TUNE_QUERY_CTA_MAX:

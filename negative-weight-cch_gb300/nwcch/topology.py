@@ -79,6 +79,31 @@ def edge_arcs(n, off, tgt, rank, first, head):
     return e_arc, e_up
 
 
+_lib.register("nwcch_edge_arcs_device", [C.c_int64] + [C.c_void_p] * 8)
+
+
+def edge_arcs_device(n, off, tgt, rank, first, head):
+    """The same mapping on the device (python/cch_nb.py:496-514): inputs are
+    host arrays or CUDA tensors; returns CUDA tensors (e_arc int64, e_up int8)."""
+    import torch
+    if not torch.cuda.is_available():
+        raise RuntimeError("edge_arcs_device needs a CUDA device")
+
+    def dev(a, dt):
+        t = a if isinstance(a, torch.Tensor) else torch.from_numpy(np.ascontiguousarray(a))
+        return t.to(device="cuda", dtype=dt).contiguous()
+    off_d, tgt_d, rank_d = dev(off, torch.int64), dev(tgt, torch.int32), dev(rank, torch.int32)
+    first_d, head_d = dev(first, torch.int64), dev(head, torch.int32)
+    m = int(off_d[-1].item()) if n > 0 else 0
+    e_arc = torch.empty(max(m, 1), dtype=torch.int64, device="cuda")
+    e_up = torch.empty(max(m, 1), dtype=torch.int8, device="cuda")
+    _lib.check(_lib.lib().nwcch_edge_arcs_device(int(n), off_d.data_ptr(), tgt_d.data_ptr(), rank_d.data_ptr(),
+                                                  first_d.data_ptr(), head_d.data_ptr(), e_arc.data_ptr(),
+                                                  e_up.data_ptr(), torch.cuda.current_stream().cuda_stream),
+               "edge_arcs_device")
+    return e_arc[:m], e_up[:m]
+
+
 def count_triangles(n, first, head):
     d = np.diff(np.asarray(first, dtype=np.int64))
     return int((d * (d - 1) // 2).sum())

@@ -94,7 +94,7 @@ def _time(torch, fn, reps: int) -> float:
 
 
 def tune_queries(topo: DeviceTopology, metric: Metric, s_rank, t_rank, reps: int = 3,
-                 dense_rows=(1, 8, 16, 24, 33), occupancy=(1, 2), labels=("auto", "global", "shared")) -> dict:
+                 dense_rows=(1, 8, 16, 24, 33), occupancy=(1, 2, 3), labels=("auto", "global", "shared")) -> dict:
     """Times every candidate schedule on the batch (s_rank, t_rank) and keeps
     the fastest. Returns {"best": {...}, "ms": best time, "trials": [...]}."""
     import torch

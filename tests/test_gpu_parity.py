@@ -163,7 +163,7 @@ def test_query_forms_agree(gpu, oracle, kind, n):
     from nwcch import tune
     for cta_max in (0, 1 << 30):
         for rows in (1, 16, 33):
-            for occ in (1, 2):
+            for occ in (1, 2, 3):
                 tune.set(T, "query_cta_max", cta_max)
                 tune.set(T, "query_dense_rows", rows)
                 tune.set(T, "query_occupancy", occ)
@@ -385,7 +385,7 @@ def test_autotuner_keeps_answers(gpu, oracle, kind, n):
     s, t = G.random_pairs(g["n"], 2000, seed=12)
     s, t = top["rank"][s], top["rank"][t]
     r = tune.tune_queries(T, m, s, t, reps=1)
-    assert len(r["trials"]) == 5 * 2 * 3 + 2  # schedules, then the two forms
+    assert len(r["trials"]) == 5 * 3 * 3 + 2  # schedules, then the two forms
     assert tune.get(T, "query_dense_rows") == r["best"]["query_dense_rows"]
     assert np.array_equal(T.query_batch(m, s, t).cpu().numpy(), oracle.query_batch(OT, oup, odn, s, t))
     before = m.to_numpy()
@@ -448,3 +448,16 @@ def test_customize_schedules_keep_values(gpu, oracle):
         for storage in ("int32", "int64"):
             up, dn = T.customize(g["w"], storage).to_numpy()
             assert np.array_equal(up, oup) and np.array_equal(dn, odn), (cap, cnt, storage)
+
+
+def test_edge_arcs_device(gpu):
+    """Device arc mapping equals the host one and the reference's (golden)."""
+    from nwcch import topology as TT
+    F = load_golden("family.npz")
+    for i in (0, 5, 11):
+        c = family_case(F, i)
+        ea, eu = TT.edge_arcs_device(int(c["n"]), c["off"], c["tgt"], c["rank"], c["first"], c["head"])
+        assert np.array_equal(ea.cpu().numpy(), c["e_arc"]) and np.array_equal(eu.cpu().numpy(), c["e_up"])
+    g, top = _seeded("road", 80_000, seed=21)
+    ea, eu = TT.edge_arcs_device(g["n"], g["off"], g["tgt"], top["rank"], top["first"], top["head"])
+    assert np.array_equal(ea.cpu().numpy(), top["e_arc"]) and np.array_equal(eu.cpu().numpy(), top["e_up"])
