@@ -145,6 +145,9 @@ int nwcch_check(nwcch_topology* t, void* stream);
  * the plan (synchronizes the device; no other call on the handle meanwhile). */
 #define NWCCH_TUNE_SN_WARP_CAP 6
 #define NWCCH_TUNE_SN_WARP_MIN_COUNT 7
+/* 1: the customization's kernels are programmatic dependent launches (each
+ * may start while the previous drains, then waits for it on the device). */
+#define NWCCH_TUNE_PDL 8
 int nwcch_tune_set(nwcch_topology* t, int key, int64_t value);
 int nwcch_tune_get(const nwcch_topology* t, int key, int64_t* value);
 

@@ -88,6 +88,34 @@ __device__ __forceinline__ bool negative_pair(T u, T v) {
     return s < 0;
 }
 
+// Programmatic dependent launch. A kernel of the customization sequence may
+// be launched before the previous one has finished (its CTAs then occupy
+// free SM slots instead of waiting for the launch); pdl_wait() blocks until
+// the previous grid has completed and its memory is visible, so it comes
+// before any global access. pdl_launch_dependents() lets the next grid's CTAs
+// be scheduled once every CTA of this grid has started. Without the launch
+// attribute both are no-ops.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_launch_dependents() { asm volatile("griddepcontrol.launch_dependents;" :::); }
+
+// Launches `kernel` on s, allowed to start before the previous kernel on s
+// has finished when `pdl` (the kernel must begin with pdl_wait()).
+template <class... KArgs, class... Args>
+cudaError_t launch_pdl(bool pdl, void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+                       Args&&... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = pdl ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+}
+
 #define NWCCH_CUDA_TRY(expr)                            \
     do {                                                \
         cudaError_t _e = (expr);                        \

@@ -25,6 +25,8 @@ namespace nwcch {
 
 template <class T>
 __global__ void k_fill2(T* __restrict__ a, T* __restrict__ b, int64_t count, T v) {
+    pdl_wait();
+    pdl_launch_dependents();
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < count;
          i += (int64_t)gridDim.x * blockDim.x) {
         a[i] = v;
@@ -37,6 +39,8 @@ __global__ void k_fill2(T* __restrict__ a, T* __restrict__ b, int64_t count, T v
 template <class T>
 __global__ void k_base(DevTopo D, const int32_t* __restrict__ w, T* __restrict__ up, T* __restrict__ dn,
                        int* __restrict__ err) {
+    pdl_wait();
+    pdl_launch_dependents();
     // metric blockIdx.y of a metric-major batch (weights m apart, arcs m+ apart)
     w += blockIdx.y * D.m;
     up += blockIdx.y * D.m_plus;
@@ -151,7 +155,9 @@ template <class T>
 int base_init(nwcch_topology* t, const int32_t* w, T* up, T* dn, cudaStream_t s, int* err, int metrics) {
     const DevTopo& D = t->d;
     k_fill2<T><<<grid_for(D.m_plus * metrics, 256), 256, 0, s>>>(up, dn, D.m_plus * metrics, Lim<T>::INF);
-    if (D.m > 0) k_base<T><<<dim3(grid_for(D.m, 256), metrics), 256, 0, s>>>(D, w, up, dn, err);
+    if (D.m > 0)
+        NWCCH_CUDA_TRY(launch_pdl(t->tune.pdl != 0, k_base<T>, dim3(grid_for(D.m, 256), metrics), dim3(256), 0, s, D,
+                                  w, up, dn, err));
     return cudaGetLastError() == cudaSuccess ? NWCCH_OK : NWCCH_ERR_CUDA;
 }
 

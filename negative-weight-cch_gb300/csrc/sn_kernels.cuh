@@ -182,6 +182,8 @@ __global__ void __launch_bounds__(CT) k_sn_panel(DevTopo D, SnDev S, const int32
                                                  T* __restrict__ up, T* __restrict__ dn, int* __restrict__ err) {
     using E = Exact<T>;
     __shared__ PanelSmem<T, CT> sm;
+    pdl_wait();
+    pdl_launch_dependents();
     up += blockIdx.y * D.m_plus;  // metric blockIdx.y of a metric-major batch
     dn += blockIdx.y * D.m_plus;
     const int32_t s = items[3 * blockIdx.x], ct = items[3 * blockIdx.x + 1];
@@ -369,6 +371,8 @@ __global__ void __launch_bounds__((TILE / MT) * (TILE / MT))
     constexpr int CH = sizeof(T) == 4 ? 32 : 16;
     using E = Exact<T>;
     __shared__ TileSmem<T, TILE, CH> sm;
+    pdl_wait();
+    pdl_launch_dependents();
     up += blockIdx.y * D.m_plus;  // metric blockIdx.y of a metric-major batch
     dn += blockIdx.y * D.m_plus;
     const auto c = tile_ctx<T, TILE, MT, OUT>(S, items, panel);
@@ -407,6 +411,8 @@ __global__ void __launch_bounds__(32 * WARPS) k_sn_warp(DevTopo D, SnDev S, cons
                                                         int* __restrict__ err) {
     __shared__ T su[WARPS][SN_WARP_CAP];
     __shared__ T sd[WARPS][SN_WARP_CAP];
+    pdl_wait();
+    pdl_launch_dependents();
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     up += blockIdx.y * D.m_plus;
     dn += blockIdx.y * D.m_plus;

@@ -273,31 +273,36 @@ int run_supernodal(nwcch_topology* t, SnPlan* P, const int32_t* w, T* up, T* dn,
     if (rc) return rc;
     const DevTopo& D = t->d;
     constexpr int CT = sizeof(T) == 4 ? 128 : 32;
+    const bool pdl = t->tune.pdl != 0;
     for (const SnLaunch& la : P->launches) {
         const int32_t* it = P->d_items + 3 * la.off;
+        const dim3 grid((unsigned)la.count, metrics);
+        cudaError_t e = cudaSuccess;
         switch (la.kind) {
             case SN_PANEL:
-                k_sn_panel<T, CT><<<dim3((unsigned)la.count, metrics), CT, 0, s>>>(D, P->dev, it, la.panel, up, dn, err);
+                e = launch_pdl(pdl, k_sn_panel<T, CT>, grid, dim3(CT), 0, s, D, P->dev, it, la.panel, up, dn, err);
                 break;
             case SN_TRAIL:
-                k_sn_tile<T, 64, 4, false><<<dim3((unsigned)la.count, metrics), 256, 0, s>>>(D, P->dev, it, la.panel, up, dn, err);
+                e = launch_pdl(pdl, k_sn_tile<T, 64, 4, false>, grid, dim3(256), 0, s, D, P->dev, it, la.panel, up, dn,
+                               err);
                 break;
             case SN_OUT_BIG:
-                k_sn_tile<T, 64, 4, true><<<dim3((unsigned)la.count, metrics), 256, 0, s>>>(D, P->dev, it, 0, up, dn, err);
+                e = launch_pdl(pdl, k_sn_tile<T, 64, 4, true>, grid, dim3(256), 0, s, D, P->dev, it, 0, up, dn, err);
                 break;
             case SN_OUT_SMALL:
-                k_sn_tile<T, 16, 2, true><<<dim3((unsigned)la.count, metrics), 64, 0, s>>>(D, P->dev, it, 0, up, dn, err);
+                e = launch_pdl(pdl, k_sn_tile<T, 16, 2, true>, grid, dim3(64), 0, s, D, P->dev, it, 0, up, dn, err);
                 break;
             case SN_WARP: {
                 constexpr int WARPS = sizeof(T) == 4 ? 8 : 4;
                 const int64_t blocks = std::min<int64_t>((la.count + WARPS - 1) / WARPS, 152 * 64);
-                k_sn_warp<T, WARPS><<<dim3((unsigned)blocks, metrics), 32 * WARPS, 0, s>>>(D, P->dev, it, la.count, up,
-                                                                                           dn, err);
+                e = launch_pdl(pdl, k_sn_warp<T, WARPS>, dim3((unsigned)blocks, metrics), dim3(32 * WARPS), 0, s, D,
+                               P->dev, it, la.count, up, dn, err);
                 break;
             }
             default:
                 return NWCCH_ERR_TOPOLOGY;
         }
+        if (e != cudaSuccess) return NWCCH_ERR_CUDA;
     }
     return cudaGetLastError() == cudaSuccess ? NWCCH_OK : NWCCH_ERR_CUDA;
 }
@@ -345,7 +350,8 @@ int launch_cached(SnPlan* P, const SnGraph& key, cudaStream_t s, const std::func
 template <class T>
 int launch_supernodal(nwcch_topology* t, SnPlan* P, const int32_t* w, T* up, T* dn, cudaStream_t s, int metrics) {
     int* err = stream_slot(t, s).err;
-    SnGraph key{SN_GRAPH_CUSTOMIZE, (int)sizeof(T), metrics, err, w, up, dn, nullptr, 0};
+    // the launch form (programmatic dependent launches or not) is part of the key
+    SnGraph key{SN_GRAPH_CUSTOMIZE, (int)sizeof(T), metrics * 2 + (t->tune.pdl != 0), err, w, up, dn, nullptr, 0};
     return launch_cached(P, key, s, [&](cudaStream_t cs) { return run_supernodal<T>(t, P, w, up, dn, cs, err, metrics); });
 }
 

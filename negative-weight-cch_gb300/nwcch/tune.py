@@ -27,7 +27,7 @@ from . import _lib
 from .device import DeviceTopology, Metric
 
 KEYS = {"query_dense_rows": 1, "query_smem_labels_max": 2, "update_budget_ns": 3, "query_occupancy": 4,
-        "query_cta_max": 5, "sn_warp_cap": 6, "sn_warp_min_count": 7}
+        "query_cta_max": 5, "sn_warp_cap": 6, "sn_warp_min_count": 7, "pdl": 8}
 PLAN_KEYS = {"sn_warp_cap", "sn_warp_min_count"}
 
 _lib.register("nwcch_tune_set", [C.c_void_p, C.c_int, C.c_int64])
@@ -76,6 +76,20 @@ def tune_customize(topo: DeviceTopology, w, caps=(0, 128, 256, 512), min_counts=
     best = min(trials, key=lambda r: r["ms"])
     set(topo, "sn_warp_cap", best["sn_warp_cap"])
     set(topo, "sn_warp_min_count", best["sn_warp_min_count"])
+    # then the launch form on the chosen plan: programmatic dependent launches
+    pdl_before = get(topo, "pdl")
+    forms = {}
+    for pdl in (0, 1):
+        set(topo, "pdl", pdl)
+        forms[pdl] = _time(torch, lambda: topo.customize(wt, "int32", out=m, sync=False), reps)
+        if not (torch.equal(ref[0], m.up) and torch.equal(ref[1], m.dn)):
+            set(topo, "pdl", pdl_before)
+            raise AssertionError(f"launch form pdl={pdl} changed the values")
+        trials.append({"sn_warp_cap": best["sn_warp_cap"], "sn_warp_min_count": best["sn_warp_min_count"],
+                       "pdl": pdl, "ms": round(forms[pdl], 4), "launches": topo.sn_launches})
+    pdl = min(forms, key=forms.get)
+    set(topo, "pdl", pdl)
+    best = {**best, "pdl": pdl, "ms": round(forms[pdl], 4)}
     return {"best": best, "trials": trials}
 
 

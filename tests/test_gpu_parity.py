@@ -440,14 +440,17 @@ def test_customize_schedules_keep_values(gpu, oracle):
     T = DeviceTopology.from_dict(top)
     oup, odn = oracle.customize(oracle.Topo.from_dict(top), g["w"])
     r = tune.tune_customize(T, g["w"], caps=(0, 512), min_counts=(0, 4096), reps=1)
-    assert len(r["trials"]) == 3
+    assert len(r["trials"]) == 3 + 2  # plans, then the two launch forms
     assert tune.get(T, "sn_warp_cap") == r["best"]["sn_warp_cap"]
-    for cap, cnt in ((512, 0), (0, 0), (128, 64)):
+    for cap, cnt, pdl in ((512, 0, 0), (0, 0, 1), (128, 64, 1), (512, 0, 1)):
         tune.set(T, "sn_warp_cap", cap)
         tune.set(T, "sn_warp_min_count", cnt)
+        tune.set(T, "pdl", pdl)
         for storage in ("int32", "int64"):
             up, dn = T.customize(g["w"], storage).to_numpy()
-            assert np.array_equal(up, oup) and np.array_equal(dn, odn), (cap, cnt, storage)
+            assert np.array_equal(up, oup) and np.array_equal(dn, odn), (cap, cnt, pdl, storage)
+        b = T.customize_batch(np.stack([g["w"], g["w"]]))
+        assert np.array_equal(b.metric(1).to_numpy()[0], oup)
 
 
 def test_edge_arcs_device(gpu):
