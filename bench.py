@@ -98,6 +98,13 @@ def algorithmic_bytes(n, m, m_plus, triangles, s_w=4):
     return triangles * (4 * s_w + 4) + m_plus * (4 * s_w + 4) + 8 * (n + 1) + m * (4 + 8 + 1 + 4)
 
 
+# DRAM bytes (read + write) of one customization, from one ncu capture of
+# `bench.py --profile customize` on the workload (dram__bytes_read.sum +
+# dram__bytes_write.sum over the customization's launches; the capture's
+# summary is profiles/customize_usa24m_launches_dram.md).
+MEASURED_TRAFFIC = {"usa24m": (21.146e9, "ncu, plan: warp cap 256, level threshold 1024")}
+
+
 def peak_hbm():
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -289,12 +296,14 @@ def run_ours(args, W, world):
         e2e_ms.append((time.perf_counter() - t0) * 1000)
         assert c == neg_k
     # single-query latency (one query per call)
-    lat = []
+    lat, lat_dist = [], []
     for i in range(min(200, W["qs"].size)):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        T.query_batch(good, qs[i:i + 1], qt[i:i + 1])
+        d1 = T.query_batch(good, qs[i:i + 1], qt[i:i + 1])
         lat.append((time.perf_counter() - t0) * 1e6)
+        lat_dist.append(int(d1[0]))
+    lat_dist = np.array(lat_dist, np.int64)
     # the CCH potential of the conservative metric (two sweeps)
     pot_ms = []
     for _ in range(3):
@@ -307,7 +316,7 @@ def run_ours(args, W, world):
     good_host = good.to_numpy()
     return dict(T=T, tuned=tuned, cust_tuned=cust_tuned, cust_ms=cust_ms, q_ms=q_ms, wall=wall, plain_ms=plain_ms, plain_equal=same,
                 e2e_ms=e2e_ms,
-                plain_q_ms=plain_q_ms, pot_ms=pot_ms, pot=pot.cpu().numpy(), good_host=good_host,
+                plain_q_ms=plain_q_ms, lat_dist=lat_dist, pot_ms=pot_ms, pot=pot.cpu().numpy(), good_host=good_host,
                 lat_us=lat, clocks=clocks.summary(), neg=neg_k, saturated=bool(sat))
 
 
@@ -320,6 +329,19 @@ def cpu_potential(W, good_host, pot_dev):
     p = orc.potential(OT, *good_host)
     ms = (time.perf_counter() - t0) * 1000
     return dict(ms=ms, equal=bool(np.array_equal(p, pot_dev)))
+
+
+def cpu_queries(W, good_host, count: int = 200):
+    """The oracle's ET query (python/cch_nb.py:577-615 as plain C), one
+    thread, one query after another, on the same metric and pairs: the CPU
+    per-query latency beside the device's."""
+    import oracle as orc
+    OT = orc.Topo.from_dict(W["top"])
+    s, t = W["qs"][:count].astype(np.int64), W["qt"][:count].astype(np.int64)
+    t0 = time.perf_counter()
+    d = orc.query_batch(OT, *good_host, s, t, threads=1)
+    ms = (time.perf_counter() - t0) * 1000 / max(1, s.size)
+    return dict(ms_per_query=ms, queries=int(s.size), dist=d)
 
 
 def batched_bytes(n, m, m_plus, triangles, k, s_w=4):
@@ -635,6 +657,8 @@ def main():
     achieved = B / (cust / 1000) / 1e9
     cb = cpu_baseline(W, args.cpu_budget)
     cp = cpu_potential(W, R["good_host"], R["pot"])
+    cq = cpu_queries(W, R["good_host"])
+    assert np.array_equal(cq["dist"], R["lat_dist"][:cq["queries"]]), "device and oracle distances differ"
     line = {
         "metric": METRIC, "value": round(cust_total * 1000 / replica_units(args.steps, world), 4), "unit": UNIT,
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -655,16 +679,24 @@ def main():
         "customize_schedule": R["cust_tuned"],
         "plain_queries_per_s": round(nq / (R["plain_q_ms"] / 1000) * world, 1),
         "query_latency_us": {"p50": round(lat[len(lat) // 2], 2), "p99": round(lat[max(0, int(len(lat) * 0.99) - 1)], 2),
-                             "mode": "one query per call, host-timed"},
+                             "mode": "one query per call, host-timed",
+                             "cpu_oracle_us_per_query": round(cq["ms_per_query"] * 1000, 2),
+                             "cpu_note": "the oracle's ET query, 1 thread, same graph, metric and pairs"},
         "e2e": {"value": round(statistics.median(R["e2e_ms"]), 4), "unit": "ms",
                 "h2d_bytes_per_step": int(W["w"].size * 4), "d2h_bytes_per_step": 8},
         # per timed step: k_fill2 + k_base + the supernodal launches, the
         # scan, and the query batch's k_maxabs + k_query_sn32 + k_query_sn
         "gpu_launches": (2 + T.sn_launches + 1 + 3) * args.steps,
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "peak_source": peak_src,
-                     "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": None,
+                     "unit": "GB/s", "frac": round(achieved / peak, 4),
+                     "traffic": (int(MEASURED_TRAFFIC[args.workload][0]) if args.workload in MEASURED_TRAFFIC
+                                 else None),
+                     "traffic_source": (MEASURED_TRAFFIC[args.workload][1] if args.workload in MEASURED_TRAFFIC
+                                        else None),
+                     "dram_gbs_at_traffic": (round(MEASURED_TRAFFIC[args.workload][0] / (cust / 1000) / 1e9, 1)
+                                             if args.workload in MEASURED_TRAFFIC else None),
                      "algorithmic_bytes_per_launch": int(B),
-                     "kernel": "supernodal customization (CUDA graph of k_base, k_sn_panel, k_sn_tile)"},
+                     "launch": "one customization: CUDA graph of k_fill2, k_base, k_sn_warp, k_sn_panel, k_sn_tile"},
         "cpu_baseline": {"value": round(cb["value"], 3), "unit": "ms", "cores": cb["cores"], "kind": "port",
                          "sample": f"{cb['runs']} level-parallel customizations + scans of the same metric"},
         "clocks": R["clocks"],

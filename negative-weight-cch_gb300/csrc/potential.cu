@@ -151,18 +151,21 @@ __device__ __forceinline__ int64_t down_row(const DevTopo& D, int32_t s0, int32_
 template <class T>
 __device__ void down_diagonal(const DevTopo& D, int32_t s0, int32_t i0, int rows, const T* __restrict__ dn,
                               int64_t* p, int& e) {
+    // push form: when row j is final (every row below it has pushed), rows
+    // r < j take p(j) + dn(r, j); lane r holds dn(r, j) for j > r in
+    // registers, so each step is one shuffle and one min
     const int lane = threadIdx.x & 31;
     int64_t mine = lane < rows ? p[s0 + i0 + lane] : INF64;
-    T u[31];
-    diag_weights<T>(D, s0, i0, rows, dn, u);
+    T u[32];
 #pragma unroll
-    for (int rr = 0; rr < 31; rr++) {
-        const int r = 30 - rr;  // bottom-up; constant indices keep u in registers
-        if (r <= rows - 2) {
-            int64_t c = label_plus(mine, u[r], e);  // INF unless r < lane < rows
-            c = warp_min64(c);
-            if (lane == r && c < mine) mine = c;
-        }
+    for (int j = 0; j < 32; j++)
+        u[j] = (lane < j && j < rows) ? dn[arc_at(D, s0, i0 + lane, i0 + j)] : Lim<T>::INF;
+#pragma unroll
+    for (int jj = 0; jj < 31; jj++) {
+        const int j = 31 - jj;  // bottom-up; constant indices keep u in registers
+        const int64_t pj = __shfl_sync(FULL, (long long)mine, j);
+        const int64_t c = label_plus(pj, u[j], e);  // INF unless lane < j < rows
+        if (c < mine) mine = c;
     }
     if (lane < rows) p[s0 + i0 + lane] = mine;
 }
