@@ -200,21 +200,21 @@ using namespace nwcch;
 
 extern "C" int nwcch_customize_async(nwcch_topology* t, const int32_t* w_dev, int32_t* up_dev,
                                      int32_t* dn_dev, void* stream) {
-    if (!t || !up_dev || !dn_dev || (t->d.m > 0 && !w_dev)) return NWCCH_ERR_ARG;
+    if (!t || (t->d.m_plus > 0 && (!up_dev || !dn_dev)) || (t->d.m > 0 && !w_dev)) return NWCCH_ERR_ARG;
     return launch_supernodal<int32_t>(t, static_cast<SnPlan*>(t->sn_plan), w_dev, up_dev, dn_dev,
                                       (cudaStream_t)stream);
 }
 
 extern "C" int nwcch_customize_i64_async(nwcch_topology* t, const int32_t* w_dev, int64_t* up_dev,
                                          int64_t* dn_dev, void* stream) {
-    if (!t || !up_dev || !dn_dev || (t->d.m > 0 && !w_dev)) return NWCCH_ERR_ARG;
+    if (!t || (t->d.m_plus > 0 && (!up_dev || !dn_dev)) || (t->d.m > 0 && !w_dev)) return NWCCH_ERR_ARG;
     return launch_supernodal<int64_t>(t, static_cast<SnPlan*>(t->sn_plan), w_dev, up_dev, dn_dev,
                                       (cudaStream_t)stream);
 }
 
 extern "C" int nwcch_customize_plain_async(nwcch_topology* t, const int32_t* w_dev, int32_t* up_dev,
                                            int32_t* dn_dev, void* stream) {
-    if (!t || !up_dev || !dn_dev || (t->d.m > 0 && !w_dev)) return NWCCH_ERR_ARG;
+    if (!t || (t->d.m_plus > 0 && (!up_dev || !dn_dev)) || (t->d.m > 0 && !w_dev)) return NWCCH_ERR_ARG;
     return customize_plain<int32_t>(t, w_dev, up_dev, dn_dev, (cudaStream_t)stream);
 }
 
@@ -246,19 +246,19 @@ extern "C" int nwcch_customize_i64(nwcch_topology* t, const int32_t* w_dev, int6
 
 extern "C" int nwcch_negative_cycle_arcs(nwcch_topology* t, const int32_t* up_dev, const int32_t* dn_dev,
                                          int64_t* count, void* stream) {
-    if (!t || !up_dev || !dn_dev || !count) return NWCCH_ERR_ARG;
+    if (!t || (t->d.m_plus > 0 && (!up_dev || !dn_dev)) || !count) return NWCCH_ERR_ARG;
     return negative_cycle_arcs<int32_t>(t, up_dev, dn_dev, count, (cudaStream_t)stream);
 }
 
 extern "C" int nwcch_negative_cycle_arcs_i64(nwcch_topology* t, const int64_t* up_dev, const int64_t* dn_dev,
                                              int64_t* count, void* stream) {
-    if (!t || !up_dev || !dn_dev || !count) return NWCCH_ERR_ARG;
+    if (!t || (t->d.m_plus > 0 && (!up_dev || !dn_dev)) || !count) return NWCCH_ERR_ARG;
     return negative_cycle_arcs<int64_t>(t, up_dev, dn_dev, count, (cudaStream_t)stream);
 }
 
 extern "C" int nwcch_customize_batch_async(nwcch_topology* t, int64_t metrics, const int32_t* w_dev,
                                            int32_t* up_dev, int32_t* dn_dev, void* stream) {
-    if (!t || metrics < 1 || metrics > 65535 || !up_dev || !dn_dev || (t->d.m > 0 && !w_dev)) return NWCCH_ERR_ARG;
+    if (!t || metrics < 1 || metrics > 65535 || (t->d.m_plus > 0 && (!up_dev || !dn_dev)) || (t->d.m > 0 && !w_dev)) return NWCCH_ERR_ARG;
     return launch_supernodal<int32_t>(t, static_cast<SnPlan*>(t->sn_plan), w_dev, up_dev, dn_dev,
                                       (cudaStream_t)stream, (int)metrics);
 }
@@ -272,7 +272,7 @@ extern "C" int nwcch_customize_batch(nwcch_topology* t, int64_t metrics, const i
 
 extern "C" int nwcch_negative_cycle_arcs_batch_async(nwcch_topology* t, int64_t metrics, const int32_t* up_dev,
                                                      const int32_t* dn_dev, int64_t* counts_dev, void* stream) {
-    if (!t || metrics < 1 || metrics > 65535 || !up_dev || !dn_dev || !counts_dev) return NWCCH_ERR_ARG;
+    if (!t || metrics < 1 || metrics > 65535 || (t->d.m_plus > 0 && (!up_dev || !dn_dev)) || !counts_dev) return NWCCH_ERR_ARG;
     cudaStream_t s = (cudaStream_t)stream;
     NWCCH_CUDA_TRY(cudaMemsetAsync(counts_dev, 0, sizeof(int64_t) * metrics, s));
     k_negcycle<int32_t><<<dim3(grid_for(t->d.m_plus, 256), (unsigned)metrics), 256, 0, s>>>(
@@ -283,7 +283,7 @@ extern "C" int nwcch_negative_cycle_arcs_batch_async(nwcch_topology* t, int64_t 
 
 extern "C" int nwcch_negative_cycle_arcs_async(nwcch_topology* t, const int32_t* up_dev, const int32_t* dn_dev,
                                                int64_t* count_dev, void* stream) {
-    if (!t || !up_dev || !dn_dev || !count_dev) return NWCCH_ERR_ARG;
+    if (!t || (t->d.m_plus > 0 && (!up_dev || !dn_dev)) || !count_dev) return NWCCH_ERR_ARG;
     cudaStream_t s = (cudaStream_t)stream;
     NWCCH_CUDA_TRY(cudaMemsetAsync(count_dev, 0, sizeof(int64_t), s));
     k_negcycle<int32_t><<<grid_for(t->d.m_plus, 256), 256, 0, s>>>(

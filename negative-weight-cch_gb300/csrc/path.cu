@@ -324,7 +324,7 @@ extern "C" int nwcch_query_paths(nwcch_topology* t, const int32_t* up_dev, const
                                  const int32_t* s_rank_dev, const int32_t* t_rank_dev, int64_t nq, int64_t* dist_dev,
                                  int64_t* off_dev, int32_t* path_dev, int64_t cap, int64_t* needed, void* stream) {
     if (!t || nq < 0 || !off_dev || !needed || cap < 0 || (cap > 0 && !path_dev) ||
-        (nq > 0 && (!up_dev || !dn_dev || !s_rank_dev || !t_rank_dev || !dist_dev)))
+        (nq > 0 && ((t->d.m_plus > 0 && (!up_dev || !dn_dev)) || !s_rank_dev || !t_rank_dev || !dist_dev)))
         return NWCCH_ERR_ARG;
     *needed = 0;
     if (nq == 0) return cudaMemsetAsync(off_dev, 0, sizeof(int64_t), (cudaStream_t)stream) == cudaSuccess
@@ -338,7 +338,7 @@ extern "C" int nwcch_query_paths_i64(nwcch_topology* t, const int64_t* up_dev, c
                                      int64_t* dist_dev, int64_t* off_dev, int32_t* path_dev, int64_t cap,
                                      int64_t* needed, void* stream) {
     if (!t || nq < 0 || !off_dev || !needed || cap < 0 || (cap > 0 && !path_dev) ||
-        (nq > 0 && (!up_dev || !dn_dev || !s_rank_dev || !t_rank_dev || !dist_dev)))
+        (nq > 0 && ((t->d.m_plus > 0 && (!up_dev || !dn_dev)) || !s_rank_dev || !t_rank_dev || !dist_dev)))
         return NWCCH_ERR_ARG;
     *needed = 0;
     if (nq == 0) return cudaMemsetAsync(off_dev, 0, sizeof(int64_t), (cudaStream_t)stream) == cudaSuccess

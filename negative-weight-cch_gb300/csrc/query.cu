@@ -114,7 +114,7 @@ using namespace nwcch;
 extern "C" int nwcch_query_batch(nwcch_topology* t, const int32_t* up_dev, const int32_t* dn_dev,
                                  const int32_t* s_rank_dev, const int32_t* t_rank_dev, int64_t nq,
                                  int64_t* dist_dev, void* stream) {
-    if (!t || nq < 0 || (nq > 0 && (!up_dev || !dn_dev || !s_rank_dev || !t_rank_dev || !dist_dev)))
+    if (!t || nq < 0 || (nq > 0 && ((t->d.m_plus > 0 && (!up_dev || !dn_dev)) || !s_rank_dev || !t_rank_dev || !dist_dev)))
         return NWCCH_ERR_ARG;
     if (nq == 0) return NWCCH_OK;
     bool used = false;
@@ -128,7 +128,7 @@ extern "C" int nwcch_query_batch(nwcch_topology* t, const int32_t* up_dev, const
 extern "C" int nwcch_query_batch_async(nwcch_topology* t, const int32_t* up_dev, const int32_t* dn_dev,
                                        const int32_t* s_rank_dev, const int32_t* t_rank_dev, int64_t nq,
                                        int64_t* dist_dev, void* stream) {
-    if (!t || nq < 0 || (nq > 0 && (!up_dev || !dn_dev || !s_rank_dev || !t_rank_dev || !dist_dev)))
+    if (!t || nq < 0 || (nq > 0 && ((t->d.m_plus > 0 && (!up_dev || !dn_dev)) || !s_rank_dev || !t_rank_dev || !dist_dev)))
         return NWCCH_ERR_ARG;
     if (nq == 0) return NWCCH_OK;
     bool used = false;
@@ -141,7 +141,7 @@ extern "C" int nwcch_query_batch_async(nwcch_topology* t, const int32_t* up_dev,
 extern "C" int nwcch_query_batch_plain(nwcch_topology* t, const int32_t* up_dev, const int32_t* dn_dev,
                                        const int32_t* s_rank_dev, const int32_t* t_rank_dev, int64_t nq,
                                        int64_t* dist_dev, void* stream) {
-    if (!t || nq < 0 || (nq > 0 && (!up_dev || !dn_dev || !s_rank_dev || !t_rank_dev || !dist_dev)))
+    if (!t || nq < 0 || (nq > 0 && ((t->d.m_plus > 0 && (!up_dev || !dn_dev)) || !s_rank_dev || !t_rank_dev || !dist_dev)))
         return NWCCH_ERR_ARG;
     if (nq == 0) return NWCCH_OK;
     return query_plain<int32_t>(t, up_dev, dn_dev, s_rank_dev, t_rank_dev, nq, dist_dev, (cudaStream_t)stream);
@@ -150,7 +150,7 @@ extern "C" int nwcch_query_batch_plain(nwcch_topology* t, const int32_t* up_dev,
 extern "C" int nwcch_query_batch_i64(nwcch_topology* t, const int64_t* up_dev, const int64_t* dn_dev,
                                      const int32_t* s_rank_dev, const int32_t* t_rank_dev, int64_t nq,
                                      int64_t* dist_dev, void* stream) {
-    if (!t || nq < 0 || (nq > 0 && (!up_dev || !dn_dev || !s_rank_dev || !t_rank_dev || !dist_dev)))
+    if (!t || nq < 0 || (nq > 0 && ((t->d.m_plus > 0 && (!up_dev || !dn_dev)) || !s_rank_dev || !t_rank_dev || !dist_dev)))
         return NWCCH_ERR_ARG;
     if (nq == 0) return NWCCH_OK;
     bool used = false;
@@ -206,7 +206,7 @@ static int static_query_scratch(int64_t** out) {
 extern "C" int nwcch_query_batch_noalloc(nwcch_topology* t, const int32_t* up_dev, const int32_t* dn_dev,
                                          const int32_t* s_rank_dev, const int32_t* t_rank_dev, int64_t nq,
                                          int64_t* dist_dev, void* stream) {
-    if (!t || nq < 0 || (nq > 0 && (!up_dev || !dn_dev || !s_rank_dev || !t_rank_dev || !dist_dev)))
+    if (!t || nq < 0 || (nq > 0 && ((t->d.m_plus > 0 && (!up_dev || !dn_dev)) || !s_rank_dev || !t_rank_dev || !dist_dev)))
         return NWCCH_ERR_ARG;
     if (nq == 0) return NWCCH_OK;
     const int64_t Dp = t->d.max_depth + 1;

@@ -102,7 +102,38 @@ __device__ void panel_compute(PanelSmem<V, CT>& sm, int pn, bool hasj, int& e) {
         }
     }
     __syncthreads();
-    if (hasj) {
+    if (!hasj) return;
+    if constexpr (sizeof(V) == 4) {
+        // 32-bit values: the thread's column lives in registers (fully
+        // unrolled, constant indices), the diagonal is read by broadcast;
+        // rows at or past pn are neither read nor relaxed
+        V cu[SN_P], cd[SN_P];
+#pragma unroll
+        for (int r = 0; r < SN_P; r++) {
+            cu[r] = r < pn ? sm.cU[r][tid] : P::inf();
+            cd[r] = r < pn ? sm.cD[r][tid] : P::inf();
+        }
+#pragma unroll
+        for (int a = 0; a + 1 < SN_P; a++) {
+            if (a + 1 < pn) {
+                const V ua = P::clean(cu[a]), da = P::clean(cd[a]);
+#pragma unroll
+                for (int r = a + 1; r < SN_P; r++) {
+                    if (r < pn) {
+                        P::relax(cu[r], sm.Dd[a][r], ua, e);
+                        P::relax(cd[r], da, sm.Ud[a][r], e);
+                    }
+                }
+            }
+        }
+#pragma unroll
+        for (int r = 0; r < SN_P; r++) {
+            if (r < pn) {
+                sm.cU[r][tid] = cu[r];
+                sm.cD[r][tid] = cd[r];
+            }
+        }
+    } else {
         for (int a = 0; a + 1 < pn; a++) {
             const V cu = P::clean(sm.cU[a][tid]), cd = P::clean(sm.cD[a][tid]);
 #pragma unroll 4

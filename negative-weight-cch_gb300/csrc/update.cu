@@ -625,7 +625,7 @@ using namespace nwcch;
 extern "C" int nwcch_update(nwcch_topology* t, int32_t* w_dev, int32_t* up_dev, int32_t* dn_dev,
                             const int64_t* edge_idx, const int32_t* new_w, int64_t k, int64_t* stats,
                             int32_t* changed_dev, void* stream) {
-    if (!t || !w_dev || !up_dev || !dn_dev || k < 0 || (k > 0 && (!edge_idx || !new_w)) || !stats)
+    if (!t || (t->d.m > 0 && !w_dev) || (t->d.m_plus > 0 && (!up_dev || !dn_dev)) || k < 0 || (k > 0 && (!edge_idx || !new_w)) || !stats)
         return NWCCH_ERR_ARG;
     return update<int32_t>(t, w_dev, up_dev, dn_dev, edge_idx, new_w, k, stats, changed_dev, (cudaStream_t)stream);
 }
@@ -633,7 +633,7 @@ extern "C" int nwcch_update(nwcch_topology* t, int32_t* w_dev, int32_t* up_dev, 
 extern "C" int nwcch_update_i64(nwcch_topology* t, int32_t* w_dev, int64_t* up_dev, int64_t* dn_dev,
                                 const int64_t* edge_idx, const int32_t* new_w, int64_t k, int64_t* stats,
                                 int32_t* changed_dev, void* stream) {
-    if (!t || !w_dev || !up_dev || !dn_dev || k < 0 || (k > 0 && (!edge_idx || !new_w)) || !stats)
+    if (!t || (t->d.m > 0 && !w_dev) || (t->d.m_plus > 0 && (!up_dev || !dn_dev)) || k < 0 || (k > 0 && (!edge_idx || !new_w)) || !stats)
         return NWCCH_ERR_ARG;
     return update<int64_t>(t, w_dev, up_dev, dn_dev, edge_idx, new_w, k, stats, changed_dev, (cudaStream_t)stream);
 }
