@@ -124,12 +124,26 @@ __global__ void __launch_bounds__(256) k_pot_up_cta(DevTopo D, SnDev S, const in
             }
             __syncthreads();
         }
-        const int64_t brow = D.first[s0 + k - 1];
-        for (int32_t q = threadIdx.x; q < b; q += blockDim.x) {
+        (void)b;  // the boundary push is k_pot_up_bnd's, spread over many CTAs
+    }
+    if (e) atomicOr(err, e);
+}
+
+// Upward boundary push of the CTA-swept supernodes: a CTA per (supernode,
+// 256 boundary columns), a thread per column, the minimum over every row of
+// the (final) supernode pushed into the ancestor.
+template <class T>
+__global__ void __launch_bounds__(256) k_pot_up_bnd(DevTopo D, SnDev S, const int32_t* __restrict__ items,
+                                                    int64_t count, const T* __restrict__ up, int64_t* p, int* err) {
+    int e = 0;
+    for (int64_t it = blockIdx.x; it < count; it += gridDim.x) {
+        const int32_t sn = items[2 * it], tile = items[2 * it + 1];
+        const int32_t s0 = S.s0[sn], k = S.k[sn], b = S.b[sn];
+        const int32_t q = tile * 256 + threadIdx.x;
+        if (q < b) {
             const int64_t acc = up_column<T>(D, s0, 0, k, k + q, up, p, e);
-            if (acc < 0) atomicMin(reinterpret_cast<long long*>(p + D.head[brow + q]), (long long)acc);
+            if (acc < 0) atomicMin(reinterpret_cast<long long*>(p + D.head[D.first[s0 + k - 1] + q]), (long long)acc);
         }
-        __syncthreads();
     }
     if (e) atomicOr(err, e);
 }
@@ -201,14 +215,9 @@ __global__ void __launch_bounds__(256) k_pot_down_cta(DevTopo D, SnDev S, const 
     int e = 0;
     for (int64_t it = blockIdx.x; it < count; it += gridDim.x) {
         const int32_t sn = sns[it];
-        const int32_t s0 = S.s0[sn], k = S.k[sn], b = S.b[sn];
-        const int32_t* B = D.head + D.first[s0 + k - 1];
-        auto bval = [&](int32_t j) { return p[B[j - k]]; };
-        for (int32_t i = warp; i < k; i += nwarps) {
-            const int64_t c = down_row<T>(D, s0, i, k, k + b, dn, bval, e);
-            if (lane == 0 && c < p[s0 + i]) p[s0 + i] = c;
-        }
-        __syncthreads();
+        const int32_t s0 = S.s0[sn], k = S.k[sn];
+        // the boundary product came first (k_pot_down_bnd); here the rows
+        // are solved against each other, bottom-up
         auto ival = [&](int32_t j) { return p[s0 + j]; };
         for (int32_t i1 = k; i1 > 0; i1 -= 32) {
             const int32_t i0 = max(0, i1 - 32);
@@ -220,6 +229,38 @@ __global__ void __launch_bounds__(256) k_pot_down_cta(DevTopo D, SnDev S, const 
             __syncthreads();
             if (warp == 0) down_diagonal<T>(D, s0, i0, i1 - i0, dn, p, e);
             __syncthreads();
+        }
+    }
+    if (e) atomicOr(err, e);
+}
+
+// Downward boundary product of the CTA-swept supernodes: a CTA per
+// (supernode, 32 rows), each warp 4 rows at once (the boundary values, final,
+// loaded once per 4 rows), p(row) = min(p(row), min_q p(B[q]) + dn(row, q)).
+template <class T>
+__global__ void __launch_bounds__(256) k_pot_down_bnd(DevTopo D, SnDev S, const int32_t* __restrict__ items,
+                                                      int64_t count, const T* __restrict__ dn, int64_t* p, int* err) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int e = 0;
+    for (int64_t it = blockIdx.x; it < count; it += gridDim.x) {
+        const int32_t sn = items[2 * it], tile = items[2 * it + 1];
+        const int32_t s0 = S.s0[sn], k = S.k[sn], b = S.b[sn];
+        const int32_t* B = D.head + D.first[s0 + k - 1];
+        const int32_t r0 = tile * 32 + warp * 4;
+        int64_t acc[4] = {INF64, INF64, INF64, INF64};
+        int64_t base[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) base[u] = r0 + u < k ? D.first[s0 + r0 + u] + (k - (r0 + u) - 1) : 0;
+        for (int32_t q = lane; q < b; q += 32) {
+            const int64_t pb = p[B[q]];
+#pragma unroll
+            for (int u = 0; u < 4; u++)
+                if (r0 + u < k) acc[u] = min(acc[u], label_plus(pb, dn[base[u] + q], e));
+        }
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            const int64_t c = warp_min64(acc[u]);
+            if (lane == 0 && r0 + u < k && c < p[s0 + r0 + u]) p[s0 + r0 + u] = c;
         }
     }
     if (e) atomicOr(err, e);
@@ -278,7 +319,13 @@ int potential_launches(nwcch_topology* t, SnPlan* P, const T* up, const T* dn, i
         const int64_t off = P->sn_level_off[l], big = P->sn_level_big[l], single = P->sn_level_single[l];
         const int64_t cnt = P->sn_level_off[l + 1] - off;
         const int32_t* o = P->d_sn_order + off;
-        if (big) k_pot_up_cta<T><<<(unsigned)std::min<int64_t>(big, 152 * 8), 256, 0, s>>>(D, P->dev, o, big, up, p, err);
+        if (big) {
+            k_pot_up_cta<T><<<(unsigned)std::min<int64_t>(big, 152 * 8), 256, 0, s>>>(D, P->dev, o, big, up, p, err);
+            const int64_t bo = P->pot_bu_off[l], bn = P->pot_bu_off[l + 1] - bo;
+            if (bn)
+                k_pot_up_bnd<T><<<(unsigned)std::min<int64_t>(bn, 152 * 16), 256, 0, s>>>(D, P->dev, P->d_pot_bu + 2 * bo,
+                                                                                        bn, up, p, err);
+        }
         if (single > big)
             k_pot_up_warp<T><<<warp_grid(single - big), 128, 0, s>>>(D, P->dev, o + big, single - big, up, p, err);
         if (cnt > single)
@@ -289,8 +336,13 @@ int potential_launches(nwcch_topology* t, SnPlan* P, const T* up, const T* dn, i
         const int64_t off = P->sn_level_off[l], big = P->sn_level_big[l], single = P->sn_level_single[l];
         const int64_t cnt = P->sn_level_off[l + 1] - off;
         const int32_t* o = P->d_sn_order + off;
-        if (big)
+        if (big) {
+            const int64_t bo = P->pot_bd_off[l], bn = P->pot_bd_off[l + 1] - bo;
+            if (bn)
+                k_pot_down_bnd<T><<<(unsigned)std::min<int64_t>(bn, 152 * 16), 256, 0, s>>>(
+                    D, P->dev, P->d_pot_bd + 2 * bo, bn, dn, p, err);
             k_pot_down_cta<T><<<(unsigned)std::min<int64_t>(big, 152 * 8), 256, 0, s>>>(D, P->dev, o, big, dn, p, err);
+        }
         if (single > big)
             k_pot_down_warp<T><<<warp_grid(single - big), 128, 0, s>>>(D, P->dev, o + big, single - big, dn, p, err);
         if (cnt > single)

@@ -246,12 +246,27 @@ SnPlan* build_supernodal_plan(int64_t n, const int64_t* first, const int32_t* he
         }
         P->sn_level_off[L] = (int64_t)order.size();
     }
+    std::vector<int32_t> pot_bu, pot_bd;
+    P->pot_bu_off.assign(L + 1, 0);
+    P->pot_bd_off.assign(L + 1, 0);
+    for (int32_t l = 0; l < L; l++) {
+        P->pot_bu_off[l] = (int64_t)pot_bu.size() / 2;
+        P->pot_bd_off[l] = (int64_t)pot_bd.size() / 2;
+        for (int64_t i = P->sn_level_off[l]; i < P->sn_level_off[l] + P->sn_level_big[l]; i++) {
+            const int32_t s = order[i];
+            for (int64_t tile = 0; tile < ceil_div(bv[s], 256); tile++) pot_bu.insert(pot_bu.end(), {s, (int32_t)tile});
+            for (int64_t tile = 0; tile < ceil_div(kv[s], 32); tile++) pot_bd.insert(pot_bd.end(), {s, (int32_t)tile});
+        }
+    }
+    P->pot_bu_off[L] = (int64_t)pot_bu.size() / 2;
+    P->pot_bd_off[L] = (int64_t)pot_bd.size() / 2;
     int32_t *d_s0, *d_k, *d_b, *d_rel, *d_sid;
     int64_t* d_rel_off;
     if ((*rc = upload_vec(P, s0v, &d_s0)) || (*rc = upload_vec(P, kv, &d_k)) || (*rc = upload_vec(P, bv, &d_b)) ||
         (*rc = upload_vec(P, rel_off, &d_rel_off)) || (*rc = upload_vec(P, rel, &d_rel)) ||
         (*rc = upload_vec(P, items, &P->d_items)) || (*rc = upload_vec(P, sid, &d_sid)) ||
-        (*rc = upload_vec(P, order, &P->d_sn_order))) {
+        (*rc = upload_vec(P, order, &P->d_sn_order)) || (*rc = upload_vec(P, pot_bu, &P->d_pot_bu)) ||
+        (*rc = upload_vec(P, pot_bd, &P->d_pot_bd))) {
         free_supernodal_plan(P);
         return nullptr;
     }

@@ -91,6 +91,12 @@ struct SnPlan {
     std::vector<int64_t> sn_level_off;
     std::vector<int64_t> sn_level_big;
     std::vector<int64_t> sn_level_single;
+    // the potential's boundary products of those CTA-swept supernodes, as
+    // (supernode, tile) pairs by level: upward 256 boundary columns a tile,
+    // downward 32 rows a tile
+    std::vector<int64_t> pot_bu_off, pot_bd_off;  // [levels+1], in pairs
+    int32_t* d_pot_bu = nullptr;
+    int32_t* d_pot_bd = nullptr;
     int32_t* d_sn_order = nullptr;
     std::vector<SnLaunch> launches;
     SnDev dev{};
