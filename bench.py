@@ -223,6 +223,8 @@ def run_ours(args, W, world):
         tuned = {"sample_queries": k, **r["best"], "sample_ms": r["ms"],
                  "default_ms": next(x["ms"] for x in r["trials"] if x["query_dense_rows"] == 16
                                     and x["query_occupancy"] == 1 and x["labels"] == "auto")}
+        rl = tune.tune_latency(T, good, W["qs"][-16:], W["qt"][-16:])
+        tuned["single_query"] = rl["best"]
         log(f"query schedule: {tuned}")
 
     def step(ev0=None, ev1=None):

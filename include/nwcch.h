@@ -148,6 +148,10 @@ int nwcch_check(nwcch_topology* t, void* stream);
 /* 1: the customization's kernels are programmatic dependent launches (each
  * may start while the previous drains, then waits for it on the device). */
 #define NWCCH_TUNE_PDL 8
+/* The CTA-per-query form: 16 warps a query for batches of at most
+ * QUERY_CTA_WIDE_MAX queries (else 8); its own row-by-row threshold. */
+#define NWCCH_TUNE_QUERY_CTA_WIDE_MAX 9
+#define NWCCH_TUNE_QUERY_CTA_DENSE_ROWS 10
 int nwcch_tune_set(nwcch_topology* t, int key, int64_t value);
 int nwcch_tune_get(const nwcch_topology* t, int key, int64_t* value);
 

@@ -583,12 +583,21 @@ int query_sn_async(nwcch_topology* t, const T* up, const T* dn, const int32_t* s
                                                    : k_query_sn32<1, false>;
         const size_t cta_smem = (size_t)(((12 * Dp + 16) + 15) & ~15LL);
         if (nq <= t->tune.query_cta_max && cta_smem <= 200 * 1024) {
-            // few queries: a CTA of 8 warps per query
+            // few queries: a CTA per query, 16 warps when there are at most
+            // as many queries as SMs, else 8
             int64_t blocks = 0;
-            int rc = launch_shape(k_query_sn32_cta<8>, 8, cta_smem, nq * 8, &blocks);  // one query per CTA
-            if (rc) return rc;
-            k_query_sn32_cta<8><<<(unsigned)blocks, 256, cta_smem, s>>>(t->d, S, u32, d32, s_rank, t_rank, nq, dist,
-                                                                       maxabs, err, t->tune.query_dense_rows);
+            const int rows = t->tune.query_cta_dense_rows;
+            if (nq <= t->tune.query_cta_wide_max) {
+                int rc = launch_shape(k_query_sn32_cta<16>, 16, cta_smem, nq * 16, &blocks);
+                if (rc) return rc;
+                k_query_sn32_cta<16><<<(unsigned)blocks, 512, cta_smem, s>>>(t->d, S, u32, d32, s_rank, t_rank, nq,
+                                                                            dist, maxabs, err, rows);
+            } else {
+                int rc = launch_shape(k_query_sn32_cta<8>, 8, cta_smem, nq * 8, &blocks);  // one query per CTA
+                if (rc) return rc;
+                k_query_sn32_cta<8><<<(unsigned)blocks, 256, cta_smem, s>>>(t->d, S, u32, d32, s_rank, t_rank, nq,
+                                                                           dist, maxabs, err, rows);
+            }
         } else if (allow_alloc && (force_global || per_warp > t->tune.query_smem_labels_max)) {
             // deep tree: labels in global scratch, occupancy set by registers
             int64_t blocks = 0;

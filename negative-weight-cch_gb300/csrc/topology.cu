@@ -299,6 +299,14 @@ extern "C" int nwcch_tune_set(nwcch_topology* t, int key, int64_t value) {
             if (value < 0 || value > 1) return NWCCH_ERR_ARG;
             t->tune.pdl = (int32_t)value;
             return NWCCH_OK;
+        case NWCCH_TUNE_QUERY_CTA_WIDE_MAX:
+            if (value < 0) return NWCCH_ERR_ARG;
+            t->tune.query_cta_wide_max = value;
+            return NWCCH_OK;
+        case NWCCH_TUNE_QUERY_CTA_DENSE_ROWS:
+            if (value < 1 || value > 33) return NWCCH_ERR_ARG;
+            t->tune.query_cta_dense_rows = (int32_t)value;
+            return NWCCH_OK;
         default:
             return NWCCH_ERR_ARG;
     }
@@ -313,6 +321,8 @@ extern "C" int nwcch_tune_get(const nwcch_topology* t, int key, int64_t* value) 
         case NWCCH_TUNE_QUERY_OCCUPANCY: *value = t->tune.query_occupancy; return NWCCH_OK;
         case NWCCH_TUNE_QUERY_CTA_MAX: *value = t->tune.query_cta_max; return NWCCH_OK;
         case NWCCH_TUNE_PDL: *value = t->tune.pdl; return NWCCH_OK;
+        case NWCCH_TUNE_QUERY_CTA_WIDE_MAX: *value = t->tune.query_cta_wide_max; return NWCCH_OK;
+        case NWCCH_TUNE_QUERY_CTA_DENSE_ROWS: *value = t->tune.query_cta_dense_rows; return NWCCH_OK;
         case NWCCH_TUNE_SN_WARP_CAP:
         case NWCCH_TUNE_SN_WARP_MIN_COUNT: {
             if (!t->sn_plan) return NWCCH_ERR_ARG;

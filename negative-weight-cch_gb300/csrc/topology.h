@@ -37,6 +37,8 @@ struct Tuning {
     int64_t query_smem_labels_max = 8192;   // per-warp query labels above this go to global scratch
     int32_t query_occupancy = 1;            // 2: 32-bit query kernel capped at 64 registers
     int64_t query_cta_max = 152 * 8;        // batches up to this many queries: a CTA per query
+    int64_t query_cta_wide_max = 152;       // ... of 16 warps up to this many, else of 8
+    int32_t query_cta_dense_rows = 1;       // the CTA form's row-by-row threshold
     int32_t pdl = 0;                        // customization kernels as programmatic dependent launches
     int64_t update_budget_ns = 0;           // level-sweep budget of an update (0: from the triangle count)
 };

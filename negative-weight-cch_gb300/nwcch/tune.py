@@ -27,7 +27,8 @@ from . import _lib
 from .device import DeviceTopology, Metric
 
 KEYS = {"query_dense_rows": 1, "query_smem_labels_max": 2, "update_budget_ns": 3, "query_occupancy": 4,
-        "query_cta_max": 5, "sn_warp_cap": 6, "sn_warp_min_count": 7, "pdl": 8}
+        "query_cta_max": 5, "sn_warp_cap": 6, "sn_warp_min_count": 7, "pdl": 8, "query_cta_wide_max": 9,
+        "query_cta_dense_rows": 10}
 PLAN_KEYS = {"sn_warp_cap", "sn_warp_min_count"}
 
 _lib.register("nwcch_tune_set", [C.c_void_p, C.c_int, C.c_int64])
@@ -155,6 +156,40 @@ def tune_queries(topo: DeviceTopology, metric: Metric, s_rank, t_rank, reps: int
     set(topo, "query_cta_max", max(cta_before, nq) if form == "cta" else min(cta_before, nq - 1))
     return {"best": {**{k: best[k] for k in ("query_dense_rows", "query_occupancy", "labels")}, "form": form},
             "ms": round(min(forms.values()), 4), "trials": trials}
+
+
+def tune_latency(topo: DeviceTopology, metric: Metric, s_rank, t_rank, dense_rows=(1, 8, 33), wide=(0, 1)) -> dict:
+    """The single-query form (a CTA per query): 8 or 16 warps, and its
+    row-by-row threshold, timed over one-query calls of the given pairs; the
+    fastest is kept (median call)."""
+    import torch
+    s = torch.as_tensor(np.asarray(s_rank, np.int32)).cuda()
+    t = torch.as_tensor(np.asarray(t_rank, np.int32)).cuda()
+    out = torch.empty(1, dtype=torch.int64, device="cuda")
+    before = {k: get(topo, k) for k in ("query_cta_wide_max", "query_cta_dense_rows")}
+    ref, trials = None, []
+    try:
+        for dr, wd in itertools.product(dense_rows, wide):
+            set(topo, "query_cta_dense_rows", dr)
+            set(topo, "query_cta_wide_max", 152 if wd else 0)
+            res, times = [], []
+            for i in range(s.numel()):
+                ms = _time(torch, lambda: topo.query_batch(metric, s[i:i + 1], t[i:i + 1], out=out), 1)
+                times.append(ms)
+                res.append(int(out[0]))
+            if ref is None:
+                ref = res
+            elif res != ref:
+                raise AssertionError(f"single-query schedule {(dr, wd)} changed the answers")
+            trials.append({"query_cta_dense_rows": dr, "wide": wd, "ms": round(statistics.median(times), 4)})
+    except BaseException:
+        for k, v in before.items():
+            set(topo, k, v)
+        raise
+    best = min(trials, key=lambda r: r["ms"])
+    set(topo, "query_cta_dense_rows", best["query_cta_dense_rows"])
+    set(topo, "query_cta_wide_max", 152 if best["wide"] else 0)
+    return {"best": best, "trials": trials}
 
 
 def tune_update(topo: DeviceTopology, metric: Metric, sizes=(1, 10, 100), factors=(0.25, 0.5, 1.0, 2.0),

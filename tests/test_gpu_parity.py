@@ -388,6 +388,12 @@ def test_autotuner_keeps_answers(gpu, oracle, kind, n):
     assert len(r["trials"]) == 5 * 3 * 3 + 2  # schedules, then the two forms
     assert tune.get(T, "query_dense_rows") == r["best"]["query_dense_rows"]
     assert np.array_equal(T.query_batch(m, s, t).cpu().numpy(), oracle.query_batch(OT, oup, odn, s, t))
+    rl = tune.tune_latency(T, m, s[:6], t[:6])
+    assert len(rl["trials"]) == 6
+    for wide in (0, 200):  # both CTA widths on a small batch
+        tune.set(T, "query_cta_wide_max", wide)
+        assert np.array_equal(T.query_batch(m, s[:100], t[:100]).cpu().numpy(),
+                              oracle.query_batch(OT, oup, odn, s[:100], t[:100]))
     before = m.to_numpy()
     u = tune.tune_update(T, m, sizes=(1, 20), factors=(0.5, 1.0))
     assert tune.get(T, "update_budget_ns") == u["best"]["budget_ns"]
