@@ -92,4 +92,33 @@ int64_t orc_query_path(int64_t n, const int64_t* first, const int32_t* head, con
                        const int32_t* tail, const int64_t* doff, const int32_t* darc, const int64_t* up,
                        const int64_t* dn, int64_t s, int64_t t, int64_t* dist, int64_t* path, int64_t cap);
 
+/* ---- battery-constrained profiles (oracle_battery.c), float64 ----------
+ * python/cch_nb_battery.py:48-183: the customization, x ascending, into
+ * per-direction profiles (d = 2*arc + (0 up, 1 down)). Returns an opaque
+ * handle (NULL on allocation failure). w float64[m], battery capacity M. */
+void* orc_battery_customize(int64_t n, const int64_t* first, const int32_t* head, int64_t m, const int64_t* e_arc,
+                            const int8_t* e_up, const double* w, double M);
+/* Total pieces of all profiles. */
+int64_t orc_battery_pieces(const void* handle);
+/* Canonical layout: cnt int32[2m+], off int64[2m+ + 1] (direction order),
+ * pieces float64[total][3] as (in, cost, out). */
+void orc_battery_export(const void* handle, int32_t* cnt, int64_t* off, double* pieces);
+void orc_battery_free(void* handle);
+
+/* python/cch_nb_battery.py:296-343: best charge at t leaving s with b0
+ * (-inf if infeasible); scratch soc/dsoc float64[n], mark int64[n], q a fresh
+ * query id. */
+double orc_battery_query(int64_t s_rank, int64_t t_rank, double b0, const int64_t* first, const int32_t* head,
+                         const int64_t* parent, const int32_t* cnt, const int64_t* off, const double* pieces,
+                         double* soc, double* dsoc, int64_t* mark, int64_t q);
+void orc_battery_query_batch(int64_t n, const int64_t* first, const int32_t* head, const int64_t* parent,
+                             const int32_t* cnt, const int64_t* off, const double* pieces, int64_t nq,
+                             const int64_t* s_rank, const int64_t* t_rank, const double* b0, double* out,
+                             int threads);
+
+/* python/cch_nb_battery.py:316-351: max charge at every vertex from s by
+ * label correcting on the original graph (original ids); soc float64[n]. */
+void orc_battery_label_correcting(int64_t n, const int64_t* off, const int32_t* tgt, const double* w, double M,
+                                  int64_t s, double b0, double* soc);
+
 #endif

@@ -23,7 +23,7 @@ _lib = None
 
 def build(force: bool = False) -> Path:
     """Compiles liboracle.so with the Makefile in this directory."""
-    src = [HERE / "oracle.c", HERE / "oracle.h"]
+    src = [HERE / "oracle.c", HERE / "oracle_battery.c", HERE / "oracle.h"]
     if force or not LIB.exists() or any(p.stat().st_mtime > LIB.stat().st_mtime for p in src):
         subprocess.run(["make", "-s", "-C", str(HERE), "oracle"], check=True)
     return LIB
@@ -58,6 +58,18 @@ def lib():
             L.orc_has_negative_cycle.restype = C.c_int
             L.orc_query_path.argtypes = [I64, P, P, P, P, P, P, P, P, I64, I64, P, P, I64]
             L.orc_query_path.restype = I64
+            L.orc_battery_customize.argtypes = [I64, P, P, I64, P, P, P, C.c_double]
+            L.orc_battery_customize.restype = P
+            L.orc_battery_pieces.argtypes = [P]
+            L.orc_battery_pieces.restype = I64
+            L.orc_battery_export.argtypes = [P, P, P, P]
+            L.orc_battery_export.restype = None
+            L.orc_battery_free.argtypes = [P]
+            L.orc_battery_free.restype = None
+            L.orc_battery_query_batch.argtypes = [I64, P, P, P, P, P, P, I64, P, P, P, P, C.c_int]
+            L.orc_battery_query_batch.restype = None
+            L.orc_battery_label_correcting.argtypes = [I64, P, P, P, C.c_double, I64, C.c_double, P]
+            L.orc_battery_label_correcting.restype = None
             _lib = L
     return _lib
 
@@ -183,6 +195,49 @@ def query_path(T: Topo, up, dn, s_rank: int, t_rank: int):
         if n >= 0:
             return int(d.value), path[:n].copy()
         cap = -n
+
+
+def battery_customize(T: Topo, w, M: float):
+    """python/cch_nb_battery.py:48-183: battery profiles of the float64 arc
+    energies w for capacity M, canonical layout (cnt int32[2m+], off
+    int64[2m+ + 1], pieces float64[total, 3] as (in, cost, out)); direction
+    d = 2*arc + (0 up, 1 down)."""
+    w = _c(w, np.float64)
+    L = lib()
+    h = L.orc_battery_customize(T.n, _p(T.first), _p(T.head), T.m, _p(T.e_arc), _p(T.e_up), _p(w), float(M))
+    if not h:
+        raise MemoryError("battery oracle: allocation failed")
+    try:
+        total = int(L.orc_battery_pieces(h))
+        cnt = np.empty(2 * T.m_plus, np.int32)
+        off = np.empty(2 * T.m_plus + 1, np.int64)
+        pieces = np.empty((total, 3), np.float64)
+        L.orc_battery_export(h, _p(cnt), _p(off), _p(pieces))
+    finally:
+        L.orc_battery_free(h)
+    return cnt, off, pieces
+
+
+def battery_query_batch(T: Topo, profiles, s_rank, t_rank, b0, threads: int = 0):
+    """python/cch_nb_battery.py:296-343 per pair: best charge at t (-inf if
+    infeasible)."""
+    cnt, off, pieces = profiles
+    cnt, off, pieces = _c(cnt, np.int32), _c(off, np.int64), _c(pieces, np.float64)
+    s_rank, t_rank = _c(s_rank, np.int64), _c(t_rank, np.int64)
+    b0 = _c(np.broadcast_to(b0, s_rank.shape), np.float64)
+    out = np.empty(s_rank.size, np.float64)
+    lib().orc_battery_query_batch(T.n, _p(T.first), _p(T.head), _p(T.parent), _p(cnt), _p(off), _p(pieces),
+                                  s_rank.size, _p(s_rank), _p(t_rank), _p(b0), _p(out), int(threads))
+    return out
+
+
+def battery_label_correcting(n, off, tgt, w, M: float, s: int, b0: float):
+    """python/cch_nb_battery.py:316-351: max charge at every vertex from s
+    (original ids), float64[n] with -inf where infeasible."""
+    off, tgt, w = _c(off, np.int64), _c(tgt, np.int32), _c(w, np.float64)
+    soc = np.empty(n, np.float64)
+    lib().orc_battery_label_correcting(n, _p(off), _p(tgt), _p(w), float(M), int(s), float(b0), _p(soc))
+    return soc
 
 
 def to_float(a):

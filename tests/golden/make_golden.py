@@ -429,6 +429,72 @@ def make_paths(R):
     print(f"paths.npz: {int(fam['cases'])} family graphs x 50 pairs")
 
 
+def canonical_profiles(cnt, I1, C1, O1, pst, PI, PC, PO):
+    """The reference's profile storage (inline single pieces, pooled longer
+    ones; python/cch_nb_battery.py:1-8) -> cnt int32[d], off int64[d+1],
+    pieces float64[total, 3] in direction order."""
+    cnt = np.asarray(cnt, np.int32)
+    off = np.zeros(cnt.size + 1, np.int64)
+    np.cumsum(cnt, out=off[1:])
+    pieces = np.empty((int(off[-1]), 3), np.float64)
+    for d in range(cnt.size):
+        if cnt[d] == 1:
+            pieces[off[d]] = (I1[d], C1[d], O1[d])
+        elif cnt[d] > 1:
+            p0 = int(pst[d])
+            for t in range(int(cnt[d])):
+                pieces[off[d] + t] = (PI[p0 + t], PC[p0 + t], PO[p0 + t])
+    return cnt, off, pieces
+
+
+def make_battery(R):
+    """battery.npz: python/cch_nb_battery.py, run un-jitted, on the graphs of
+    python/test_cch_battery.py:54-56 (ev_grid 12 and ev_geometric 250, seeds
+    0-2; float64 energies) with the reference CCH's order (leaf 8), for the
+    capacities 3, 10 and 40 of test_cch_battery.py:58: the reference's
+    profiles, and 30 queries per capacity (uniform s, t; b0 uniform in [0, M])
+    answered by battery_query and by the label-correcting battery_reference."""
+    gm, CCH = R["graphs"], R["cch"].CCH
+    nbb = importlib.import_module("cch_nb_battery")
+    rng = random.Random(9)
+    cases = ([gm.ev_grid(12, seed=i) for i in range(3)] + [gm.ev_geometric(250, seed=i) for i in range(3)])
+    out = {}
+    for ci, g in enumerate(cases):
+        c = CCH(g, leaf=8, log=lambda *_: None)
+        off, tgt, w = adj_csr(g)
+        first, head = np.array(c.first, np.int64), np.array(c.head, np.int64)
+        parent, rank = np.array(c.parent, np.int64), np.array(c.rank, np.int64)
+        e_arc, e_up = np.array(c.edge_arc, np.int64), np.array(c.edge_dir, np.bool_)
+        pre = f"c{ci}_"
+        out[pre + "n"] = np.int64(g.n)
+        out[pre + "off"], out[pre + "tgt"], out[pre + "w"] = off, tgt, w
+        out[pre + "rank"], out[pre + "first"], out[pre + "head"] = rank, first, head.astype(np.int32)
+        out[pre + "parent"], out[pre + "e_arc"], out[pre + "e_up"] = parent, e_arc, e_up.astype(np.int8)
+        soc, dsoc, mark = np.full(g.n, -np.inf), np.full(g.n, -np.inf), np.zeros(g.n, np.int64)
+        q = 0
+        for mi, M in enumerate((3.0, 10.0, 40.0)):
+            prof = nbb.battery_customize(g.n, first, head, e_arc, e_up, w, M)
+            cnt, poff, pieces = canonical_profiles(*prof)
+            qs = np.array([rng.randrange(g.n) for _ in range(30)], np.int64)
+            qt = np.array([rng.randrange(g.n) for _ in range(30)], np.int64)
+            b0 = np.array([rng.uniform(0, M) for _ in range(30)], np.float64)
+            ans, truth = [], []
+            for s, t, b in zip(qs, qt, b0):
+                q += 1
+                ans.append(nbb.battery_query(rank[s], rank[t], b, first, head, parent, *prof, soc, dsoc, mark, q))
+                truth.append(nbb.battery_reference(g.n, off, tgt, w, M, s, b)[t])
+            p2 = f"{pre}m{mi}_"
+            out[p2 + "M"] = np.float64(M)
+            out[p2 + "cnt"], out[p2 + "poff"], out[p2 + "pieces"] = cnt, poff, pieces
+            out[p2 + "qs"], out[p2 + "qt"], out[p2 + "b0"] = qs, qt, b0
+            out[p2 + "ans"], out[p2 + "truth"] = np.array(ans, np.float64), np.array(truth, np.float64)
+            print(f"battery case {ci} M={M}: {int(poff[-1])} pieces, largest profile {int(cnt.max())}")
+    out["cases"] = np.int64(len(cases))
+    out["capacities"] = np.int64(3)
+    np.savez_compressed(HERE / "battery.npz", **out)
+    print(f"battery.npz: {len(cases)} graphs x 3 capacities")
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default="/root/reference")
@@ -436,7 +502,8 @@ def main():
     args = ap.parse_args()
     R = import_reference(Path(args.reference))
     makers = dict(techniques=make_techniques, family=make_family, grid64=make_grid64,
-                  delaunay_negcycle=make_delaunay_negcycle, potential=make_potential, paths=make_paths)
+                  delaunay_negcycle=make_delaunay_negcycle, potential=make_potential, paths=make_paths,
+                  battery=make_battery)
     only = [s for s in args.only.split(",") if s] or list(makers)
     for name in only:
         makers[name](R)

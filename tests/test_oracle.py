@@ -162,3 +162,40 @@ def test_query_path_against_reference(oracle):
             assert np.array_equal(inv[pr], path[off[j]:off[j + 1]])
             if pr.size:
                 assert sum(wmap[(int(a), int(b))] for a, b in zip(inv[pr][:-1], inv[pr][1:])) == d
+
+
+def battery_cases():
+    """battery.npz as a list of (graph dict, [per-capacity dicts])."""
+    B = load_golden("battery.npz")
+    out = []
+    for i in range(int(B["cases"])):
+        pre = f"c{i}_"
+        g = {k[len(pre):]: v for k, v in B.items() if k.startswith(pre) and not k[len(pre):].startswith("m")}
+        caps = []
+        for mi in range(int(B["capacities"])):
+            p2 = f"{pre}m{mi}_"
+            caps.append({k[len(p2):]: v for k, v in B.items() if k.startswith(p2)})
+        out.append((g, caps))
+    return out
+
+
+def test_battery_against_reference(oracle):
+    """python/cch_nb_battery.py: the oracle's profiles are the reference's
+    piece for piece (same float64 operations, same merge order), its queries
+    return the reference's answers exactly, and the label-correcting search
+    (python/cch_nb_battery.py:316-351) the reference's too; both agree within
+    the reference's own tolerance (python/run_nb_battery.py:99-104)."""
+    for g, caps in battery_cases():
+        T = topo(oracle, g)
+        for c in caps:
+            cnt, off, pieces = oracle.battery_customize(T, g["w"], float(c["M"]))
+            assert np.array_equal(cnt, c["cnt"]) and np.array_equal(off, c["poff"])
+            assert np.array_equal(pieces, c["pieces"])
+            got = oracle.battery_query_batch(T, (cnt, off, pieces), g["rank"][c["qs"]], g["rank"][c["qt"]], c["b0"])
+            assert np.array_equal(got, c["ans"])
+            for j in range(c["qs"].size):
+                soc = oracle.battery_label_correcting(int(g["n"]), g["off"], g["tgt"], g["w"], float(c["M"]),
+                                                      int(c["qs"][j]), float(c["b0"][j]))
+                want = soc[c["qt"][j]]
+                assert want == c["truth"][j]
+                assert (got[j] == want == -np.inf) or abs(got[j] - want) <= 1e-6 * max(1.0, abs(want))
