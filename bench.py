@@ -346,6 +346,99 @@ def cpu_queries(W, good_host, count: int = 200):
     return dict(ms_per_query=ms, queries=int(s.size), dist=d)
 
 
+def run_battery(args, Wb, factors=(0.25, 1.0, 4.0), queries: int = 10_000):
+    """Battery-constrained profiles (python/run_nb_battery.py:62-117 as the
+    protocol): EV energies on the workload's graph, D = median unconstrained
+    energy of random reachable pairs, capacities M = 0.25 D, D, 4 D; per M
+    the customization (device time, warm), the profile sizes, and a batch of
+    queries with b0 = M and M / 2 per pair."""
+    import torch
+
+    from nwcch import battery
+    from nwcch import graphs as G
+    from nwcch.device import DeviceTopology
+    g, top = Wb["g"], Wb["top"]
+    w = G.ev_energies(g)
+    T = DeviceTopology.from_dict(top)
+    wt = battery.energies(T, w)
+    # D from the battery path itself: a capacity far above any route's energy
+    # and half of it as the start charge make every query unconstrained
+    big = 1e12
+    s, t = G.random_pairs(g["n"], 400, seed=21)
+    free = battery.customize(T, wt, big)
+    soc = free.query(top["rank"][s], top["rank"][t], big / 2).cpu().numpy()
+    free.free()
+    reach = soc > -np.inf
+    D = float(np.median((big / 2 - soc[reach])[:50]))
+    qs, qt = G.random_pairs(g["n"], queries // 2, seed=23)
+    qs = np.repeat(top["rank"][qs], 2).astype(np.int32)
+    qt = np.repeat(top["rank"][qt], 2).astype(np.int32)
+    sq, tq = torch.from_numpy(qs).cuda(), torch.from_numpy(qt).cuda()
+    out = []
+    for f in factors:
+        M = f * D
+        b0 = torch.from_numpy(np.tile([M, M / 2], queries // 2)).cuda()
+        times = []
+        for rep in range(1 + max(1, min(args.steps, 3))):
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            b = battery.customize(T, wt, M)
+            e1.record()
+            torch.cuda.synchronize()
+            if rep:
+                times.append(e0.elapsed_time(e1))
+            if rep < max(1, min(args.steps, 3)):
+                b.free()
+        res = b.query(sq, tq, b0)
+        qms = []
+        for _ in range(3):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            b.query(sq, tq, b0, out=res, sync=False)
+            e1.record()
+            torch.cuda.synchronize()
+            qms.append(e0.elapsed_time(e1))
+        lat = []
+        for j in range(50):
+            t0 = time.perf_counter()
+            b.query(sq[j:j + 1], tq[j:j + 1], b0[j:j + 1])
+            lat.append((time.perf_counter() - t0) * 1e6)
+        lat.sort()
+        r = res.cpu().numpy()
+        out.append({"factor": f, "M": M, "customize_ms": round(statistics.median(times), 3),
+                    "pieces": b.pieces, "largest_profile": b.largest,
+                    "size_histogram": [int(v) for v in b.size_histogram()],
+                    "queries": int(qs.size), "queries_per_s": round(qs.size / (statistics.median(qms) / 1000), 1),
+                    "query_latency_us": {"p50": round(lat[len(lat) // 2], 1), "p99": round(lat[-1], 1)},
+                    "infeasible": int(np.count_nonzero(r == -np.inf)), "_profiles": b, "_answers": r,
+                    "_b0": b0.cpu().numpy()})
+    return {"workload": Wb["name"], "energies": "EV model: L + 1.0 x climb - 0.6 x descent (float64)",
+            "D": D, "capacities": out, "_T": T, "_w": w, "_qs": qs, "_qt": qt}
+
+
+def cpu_battery(Wb, B, budget_s: float = 30.0):
+    """The oracle's battery customization (python/cch_nb_battery.py:48-183
+    as plain C, one thread) at M = D, and its queries on the same pairs;
+    checks the device profiles and answers against it."""
+    import oracle as orc
+    OT = orc.Topo.from_dict(Wb["top"])
+    cap = next(c for c in B["capacities"] if c["factor"] == 1.0)
+    t0 = time.perf_counter()
+    prof = orc.battery_customize(OT, B["_w"], cap["M"])
+    cust_s = time.perf_counter() - t0
+    dev = cap["_profiles"].export()
+    equal = all(np.array_equal(a, b) for a, b in zip(dev, prof))
+    n = max(1, min(B["_qs"].size, int(budget_s / max(cust_s, 1e-3) * 200)))
+    t0 = time.perf_counter()
+    ans = orc.battery_query_batch(OT, prof, B["_qs"][:n], B["_qt"][:n], cap["_b0"][:n], threads=1)
+    qs_s = time.perf_counter() - t0
+    return {"customize_s_M_eq_D": round(cust_s, 3), "queries": n,
+            "queries_per_s_1_thread": round(n / qs_s, 1), "threads": 1,
+            "profiles_equal_device": bool(equal),
+            "answers_equal_device": bool(np.array_equal(ans, cap["_answers"][:n]))}
+
+
 def batched_bytes(n, m, m_plus, triangles, k, s_w=4):
     """Per batched customization of k metrics: the topology (heads, first,
     arc map) is read once, weights and up/dn once per metric."""
@@ -422,6 +515,12 @@ def run_batch(args, Wd, K):
     L = g["L"].astype(np.int64)
     heights = w_cur - L  # w = length + height difference; lengths change, heights stay
     full = T.customize(m0.w, "int32")
+    upd_tuning = None
+    if not args.no_tune:
+        # sweep budget and dense threshold of this topology (raise-and-restore
+        # pairs on other arcs; the metric ends as it began)
+        from nwcch import tune
+        upd_tuning = tune.tune_update(T, m0, sizes=(1, 100, 1000), factors=(0.25, 0.5, 1.0), seed=9)["best"]
     updates = {}
     for size in (1, 100, 1000):
         wall, dev_ms, ev = [], [], []
@@ -453,7 +552,7 @@ def run_batch(args, Wd, K):
             "equal_to_singles": equal, "achieved_gbs": round(B / (bm / 1000) / 1e9, 1),
             "algorithmic_bytes": int(B),
             "l2": "flushed between steps" if fits_l2 else "inputs larger than L2",
-            "partial_updates": updates}
+            "partial_updates": updates, "update_schedule": upd_tuning}
 
 
 def run_serving(args, Ws, loads):
@@ -481,7 +580,8 @@ def run_serving(args, Ws, loads):
         rq = tune.tune_queries(T, m0, top["rank"][sq], top["rank"][tq], reps=2, dense_rows=(1, 8, 16),
                                labels=("auto", "shared"))
         ru = tune.tune_update(T, m0, sizes=(1, 10, 100, 1000), factors=(0.1, 0.25, 0.5, 1.0))
-        tuned = {"customize": rc["best"], "queries": rq["best"], "update_budget_ns": ru["best"]["budget_ns"]}
+        tuned = {"customize": rc["best"], "queries": rq["best"], "update_budget_ns": ru["best"]["budget_ns"],
+                 "update_dense_min": ru["best"]["dense_min"]}
         log(f"serving schedules: {tuned}")
         del m0
     # one customization of this topology, for scale (events, warm)
@@ -596,6 +696,8 @@ def main():
     ap.add_argument("--serve-workload", default="delaunay1m", choices=list(WORKLOADS) + ["none"])
     ap.add_argument("--serve-loads", default="1e4,1e5,1e6", help="offered query loads (queries/s)")
     ap.add_argument("--serve-seconds", type=float, default=1.0)
+    ap.add_argument("--battery-workload", default="delaunay264k", choices=list(WORKLOADS) + ["none"],
+                    help="graph of the battery-constrained profiles section")
     ap.add_argument("--no-tune", action="store_true", help="keep the default query schedule")
     ap.add_argument("--plain-steps", type=int, default=-1,
                     help="plain per-level customizations to time (-1: one, none above 5M vertices)")
@@ -648,6 +750,16 @@ def main():
         Ws = W if args.serve_workload == args.workload else make_workload(args.serve_workload, seed=0)
         serving = run_serving(args, Ws, [float(x) for x in args.serve_loads.split(",") if x])
         del Ws
+    bat = None
+    if args.battery_workload != "none":
+        Wb = W if args.battery_workload == args.workload else make_workload(args.battery_workload, seed=0)
+        B = run_battery(args, Wb)
+        cpu = cpu_battery(Wb, B, args.cpu_budget)
+        bat = {k: v for k, v in B.items() if not k.startswith("_")}
+        bat["capacities"] = [{k: v for k, v in c.items() if not k.startswith("_")} for c in B["capacities"]]
+        bat["cpu_oracle"] = cpu
+        log(f"battery: {bat}")
+        del Wb, B
     T = R["T"]
     nq = int(W["qs"].size)
     qms = statistics.median(R["q_ms"])
@@ -707,6 +819,7 @@ def main():
                       "equal": cp["equal"], "metric": "conservative (no injected cycle)"},
         "batched_customization": batch,
         "serving": serving,
+        "battery": bat,
     }
     print(json.dumps(line), flush=True)
 

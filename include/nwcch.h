@@ -152,6 +152,14 @@ int nwcch_check(nwcch_topology* t, void* stream);
  * QUERY_CTA_WIDE_MAX queries (else 8); its own row-by-row threshold. */
 #define NWCCH_TUNE_QUERY_CTA_WIDE_MAX 9
 #define NWCCH_TUNE_QUERY_CTA_DENSE_ROWS 10
+/* Battery customization: initial piece pool (0: 1.5 pieces a direction) and
+ * initial per-warp buffer of profiles longer than 32 pieces (64..2^22
+ * pieces); both grow, and the customization reruns, when outgrown. */
+#define NWCCH_TUNE_BATTERY_POOL 11
+#define NWCCH_TUNE_BATTERY_BUFFER 12
+/* Updates of at least this many (distinct) arcs skip the level sweep and
+ * finish densely at once (0: never; the sweep budget decides). */
+#define NWCCH_TUNE_UPDATE_DENSE_MIN 13
 int nwcch_tune_set(nwcch_topology* t, int key, int64_t value);
 int nwcch_tune_get(const nwcch_topology* t, int key, int64_t* value);
 
@@ -312,6 +320,41 @@ int nwcch_potential_async(nwcch_topology* t, const int32_t* up_dev, const int32_
                           void* stream);
 int nwcch_potential_i64(nwcch_topology* t, const int64_t* up_dev, const int64_t* dn_dev, int64_t* p_dev,
                         void* stream);
+
+/* ------------------------------------------------------------------------
+ * Battery-constrained profiles (float64)
+ *
+ * An arc of energy c maps a state of charge b to b - c when c >= 0 (and
+ * b >= c), to min(M, b - c) when c < 0; every path induces a piece
+ * (in, cost, out): f(b) = min(out, b - cost) for b >= in. A shortcut
+ * direction d = 2*arc + (0 up, 1 down) holds a profile, the pieces left after
+ * merging its candidates in the reference's order (the original arcs in input
+ * order, then its lower triangles by ascending lowest vertex): a candidate
+ * that a kept piece dominates is dropped, otherwise the pieces it dominates
+ * are removed, order kept, and it is appended. Same float64 operations as
+ * the reference, so the profiles are its profiles piece for piece.
+ * ---------------------------------------------------------------------- */
+typedef struct nwcch_battery nwcch_battery;
+
+/* Replaces battery_customize (python/cch_nb_battery.py:48-183): w_dev
+ * float64[m] arc energies (original arc order), battery capacity M > 0.
+ * Synchronous on `stream`; device buffers grow and the customization reruns
+ * if a profile outgrows them. *out is freed with nwcch_battery_free. */
+int nwcch_battery_customize(nwcch_topology* t, const double* w_dev, double capacity, void* stream,
+                            nwcch_battery** out);
+/* Total pieces and the largest profile. */
+int nwcch_battery_info(const nwcch_battery* b, int64_t* pieces, int32_t* largest);
+/* Canonical HOST copy: cnt int32[2m+], off int64[2m+ + 1] (direction
+ * order), pieces float64[total][3] as (in, cost, out); pieces may be NULL
+ * (counts and offsets only). */
+int nwcch_battery_export(const nwcch_battery* b, int32_t* cnt, int64_t* off, double* pieces);
+/* Replaces battery_query (python/cch_nb_battery.py:296-343) for a batch:
+ * best charge at t leaving s with charge b0 (-inf if infeasible), one warp
+ * per query. s/t int32 rank ids, b0_dev/out_dev float64[nq]. */
+int nwcch_battery_query(nwcch_topology* t, const nwcch_battery* b, const int32_t* s_rank_dev,
+                        const int32_t* t_rank_dev, const double* b0_dev, int64_t nq, double* out_dev,
+                        void* stream);
+void nwcch_battery_free(nwcch_battery* b);
 
 #ifdef __cplusplus
 }

@@ -32,6 +32,7 @@ int upload(nwcch_topology* t, const T* src, size_t count, T** dst) {
 
 void release(nwcch_topology* t) {
     if (t->free_plans) t->free_plans(t);
+    if (t->free_battery_plan) t->free_battery_plan(t);
     free_supernodal_plan(static_cast<SnPlan*>(t->sn_plan));
     t->sn_plan = nullptr;
     for (void* p : t->allocations) cudaFree(p);
@@ -307,6 +308,18 @@ extern "C" int nwcch_tune_set(nwcch_topology* t, int key, int64_t value) {
             if (value < 1 || value > 33) return NWCCH_ERR_ARG;
             t->tune.query_cta_dense_rows = (int32_t)value;
             return NWCCH_OK;
+        case NWCCH_TUNE_UPDATE_DENSE_MIN:
+            if (value < 0) return NWCCH_ERR_ARG;
+            t->tune.update_dense_min = value;
+            return NWCCH_OK;
+        case NWCCH_TUNE_BATTERY_POOL:
+            if (value < 0) return NWCCH_ERR_ARG;
+            t->tune.battery_pool = value;
+            return NWCCH_OK;
+        case NWCCH_TUNE_BATTERY_BUFFER:
+            if (value < 64 || value > (1 << 22)) return NWCCH_ERR_ARG;
+            t->tune.battery_buffer = (int32_t)value;
+            return NWCCH_OK;
         default:
             return NWCCH_ERR_ARG;
     }
@@ -323,6 +336,9 @@ extern "C" int nwcch_tune_get(const nwcch_topology* t, int key, int64_t* value) 
         case NWCCH_TUNE_PDL: *value = t->tune.pdl; return NWCCH_OK;
         case NWCCH_TUNE_QUERY_CTA_WIDE_MAX: *value = t->tune.query_cta_wide_max; return NWCCH_OK;
         case NWCCH_TUNE_QUERY_CTA_DENSE_ROWS: *value = t->tune.query_cta_dense_rows; return NWCCH_OK;
+        case NWCCH_TUNE_UPDATE_DENSE_MIN: *value = t->tune.update_dense_min; return NWCCH_OK;
+        case NWCCH_TUNE_BATTERY_POOL: *value = t->tune.battery_pool; return NWCCH_OK;
+        case NWCCH_TUNE_BATTERY_BUFFER: *value = t->tune.battery_buffer; return NWCCH_OK;
         case NWCCH_TUNE_SN_WARP_CAP:
         case NWCCH_TUNE_SN_WARP_MIN_COUNT: {
             if (!t->sn_plan) return NWCCH_ERR_ARG;

@@ -41,6 +41,9 @@ struct Tuning {
     int32_t query_cta_dense_rows = 1;       // the CTA form's row-by-row threshold
     int32_t pdl = 0;                        // customization kernels as programmatic dependent launches
     int64_t update_budget_ns = 0;           // level-sweep budget of an update (0: from the triangle count)
+    int64_t update_dense_min = 0;           // updates of at least this many arcs skip the sweep (0: never)
+    int64_t battery_pool = 0;               // initial battery piece pool (0: 1.5 pieces a direction)
+    int32_t battery_buffer = 256;           // initial per-warp buffer of a long battery profile (pieces)
 };
 
 // Device words private to the calls enqueued on one stream: the error word
@@ -76,6 +79,8 @@ struct nwcch_topology {
     std::mutex mu;                            // serialises lazily built plans
     void* plans = nullptr;                    // owned by the modules that build plans
     void (*free_plans)(nwcch_topology*) = nullptr;
+    void* battery_plan = nullptr;             // battery.cu: arcs in level order
+    void (*free_battery_plan)(nwcch_topology*) = nullptr;
 };
 
 namespace nwcch {

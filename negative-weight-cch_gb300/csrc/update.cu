@@ -594,7 +594,8 @@ int update(nwcch_topology* t, int32_t* w_dev, T* up_dev, T* dn_dev, const int64_
     A.k = kk;
     A.ws = *ws;
     A.err = stream_slot(t, s).err;
-    A.budget_ns = sweep_budget_ns(t);
+    // large updates touch most of the top separators: finish densely at once
+    A.budget_ns = (t->tune.update_dense_min > 0 && kk >= t->tune.update_dense_min) ? 0 : sweep_budget_ns(t);
     A.max_arcs = std::max<int64_t>(4096, t->d.m_plus / 8);
     void* args[] = {&A};
     const int blocks = sizeof(T) == 4 ? ws->blocks32 : ws->blocks64;

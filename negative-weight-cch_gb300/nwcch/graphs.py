@@ -26,7 +26,7 @@ import numpy as np
 
 __all__ = [
     "grid", "delaunay", "road_like", "scaled_metrics", "random_pairs",
-    "inject_negative_triangle", "csr_from_edges",
+    "inject_negative_triangle", "csr_from_edges", "ev_energies",
 ]
 
 
@@ -153,6 +153,18 @@ def scaled_metrics(g: dict, k: int, seed: int = 0, lo: float = 0.5, hi: float = 
         hj = np.rint(a[j] * g["h"]).astype(np.int64)
         out[j] = (g["L"].astype(np.int64) + hj[tgt] - hj[src]).astype(np.int32)
     return out
+
+
+def ev_energies(g: dict, beta_up: float = 1.0, beta_down: float = 0.6) -> np.ndarray:
+    """Electric-vehicle arc energies (the reference's EV model,
+    python/graphs.py:5-18 and 50-54): the length part plus beta_up per unit
+    of climb, minus beta_down per unit of descent (recuperation recovers less
+    than climbing costs), with the graph's own L and height field. float64[m];
+    steep descents are negative and every cycle costs energy."""
+    n, off, tgt = g["n"], g["off"], g["tgt"]
+    src = np.repeat(np.arange(n, dtype=np.int64), np.diff(off))
+    dz = (g["h"][tgt] - g["h"][src]).astype(np.float64)
+    return g["L"].astype(np.float64) + np.where(dz > 0, beta_up, beta_down) * dz
 
 
 def random_pairs(n: int, count: int, seed: int = 7) -> tuple[np.ndarray, np.ndarray]:

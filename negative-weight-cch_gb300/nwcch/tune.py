@@ -28,7 +28,7 @@ from .device import DeviceTopology, Metric
 
 KEYS = {"query_dense_rows": 1, "query_smem_labels_max": 2, "update_budget_ns": 3, "query_occupancy": 4,
         "query_cta_max": 5, "sn_warp_cap": 6, "sn_warp_min_count": 7, "pdl": 8, "query_cta_wide_max": 9,
-        "query_cta_dense_rows": 10}
+        "query_cta_dense_rows": 10, "battery_pool": 11, "battery_buffer": 12, "update_dense_min": 13}
 PLAN_KEYS = {"sn_warp_cap", "sn_warp_min_count"}
 
 _lib.register("nwcch_tune_set", [C.c_void_p, C.c_int, C.c_int64])
@@ -195,33 +195,57 @@ def tune_latency(topo: DeviceTopology, metric: Metric, s_rank, t_rank, dense_row
 def tune_update(topo: DeviceTopology, metric: Metric, sizes=(1, 10, 100), factors=(0.25, 0.5, 1.0, 2.0),
                 seed: int = 0) -> dict:
     """Times raise-and-restore update pairs of each size under sweep budgets
-    of `factors` x the default estimate (about half a full customization) and
-    keeps the budget with the least total time. The metric ends as it began."""
+    of `factors` x the default estimate (about half a full customization),
+    and with the dense finish at once; keeps the budget and the size from
+    which updates go dense at once (`update_dense_min`) with the least total
+    time over `sizes`. The metric ends as it began."""
     import torch
     rng = np.random.default_rng(seed)
     w0 = metric.w.cpu().numpy().copy()
     default = max(200_000, topo.triangles // 200)
-    before = get(topo, "update_budget_ns")
+    before = {k: get(topo, k) for k in ("update_budget_ns", "update_dense_min")}
+    picks = {k: rng.choice(topo.m, size=k, replace=False) for k in sizes}
+    raises = {k: w0[picks[k]].astype(np.int64) + 1 + rng.integers(0, 50, k) for k in sizes}
+
+    def per_size():
+        out = {}
+        for k in sizes:
+            idx = picks[k]
+            total = 0.0
+            for val in (raises[k], w0[idx]):
+                torch.cuda.synchronize()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record()
+                topo.update(metric, idx, val)
+                e1.record()
+                torch.cuda.synchronize()
+                total += e0.elapsed_time(e1)
+            out[k] = total
+        return out
+
     trials = []
     try:
+        set(topo, "update_dense_min", 0)
+        sweep = {}
         for f in factors:
             set(topo, "update_budget_ns", max(1, int(default * f)))
-            total = 0.0
-            for k in sizes:
-                idx = rng.choice(topo.m, size=k, replace=False)
-                raised = w0[idx].astype(np.int64) + 1 + rng.integers(0, 50, k)
-                for val in (raised, w0[idx]):
-                    torch.cuda.synchronize()
-                    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-                    e0.record()
-                    topo.update(metric, idx, val)
-                    e1.record()
-                    torch.cuda.synchronize()
-                    total += e0.elapsed_time(e1)
-            trials.append({"factor": f, "budget_ns": int(default * f), "ms": round(total, 3)})
+            sweep[f] = per_size()
+            trials.append({"factor": f, "budget_ns": int(default * f),
+                           "ms": {str(k): round(v, 3) for k, v in sweep[f].items()}})
+        set(topo, "update_dense_min", 1)
+        dense = per_size()
+        trials.append({"dense": True, "ms": {str(k): round(v, 3) for k, v in dense.items()}})
     except BaseException:
-        set(topo, "update_budget_ns", before)
+        for k, v in before.items():
+            set(topo, k, v)
         raise
-    best = min(trials, key=lambda r: r["ms"])
+    best = None
+    for f in factors:
+        for cut in list(sizes) + [0]:  # updates of >= cut arcs go dense at once (0: none)
+            total = sum(dense[k] if (cut and k >= cut) else sweep[f][k] for k in sizes)
+            if best is None or total < best["ms"]:
+                best = {"factor": f, "budget_ns": max(1, int(default * f)), "dense_min": int(cut),
+                        "ms": round(total, 3)}
     set(topo, "update_budget_ns", best["budget_ns"])
+    set(topo, "update_dense_min", best["dense_min"])
     return {"best": best, "trials": trials}

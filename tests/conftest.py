@@ -40,6 +40,21 @@ def load_golden(name: str) -> dict:
         return {k: z[k] for k in z.files}
 
 
+def battery_cases():
+    """battery.npz as a list of (graph dict, [per-capacity dicts])."""
+    B = load_golden("battery.npz")
+    out = []
+    for i in range(int(B["cases"])):
+        pre = f"c{i}_"
+        g = {k[len(pre):]: v for k, v in B.items() if k.startswith(pre) and not k[len(pre):].startswith("m")}
+        caps = []
+        for mi in range(int(B["capacities"])):
+            p2 = f"{pre}m{mi}_"
+            caps.append({k[len(p2):]: v for k, v in B.items() if k.startswith(p2)})
+        out.append((g, caps))
+    return out
+
+
 def family_case(F: dict, i: int) -> dict:
     pre = f"c{i}_"
     out = {k[len(pre):]: v for k, v in F.items() if k.startswith(pre)}

@@ -397,8 +397,19 @@ def test_autotuner_keeps_answers(gpu, oracle, kind, n):
     before = m.to_numpy()
     u = tune.tune_update(T, m, sizes=(1, 20), factors=(0.5, 1.0))
     assert tune.get(T, "update_budget_ns") == u["best"]["budget_ns"]
+    assert tune.get(T, "update_dense_min") == u["best"]["dense_min"] in (0, 1, 20)
+    assert len(u["trials"]) == 3
     after = m.to_numpy()
     assert np.array_equal(before[0], after[0]) and np.array_equal(before[1], after[1])
+    # an update at the dense threshold equals the oracle's
+    tune.set(T, "update_dense_min", 5)
+    w = g["w"].copy()
+    idx = np.arange(0, 50) * 7
+    val = (w[idx] + 3).astype(np.int32)
+    ev = T.update(m, idx, val)
+    oev, _, _ = oracle.update(OT, w, oup, odn, idx, val)
+    up, dn = m.to_numpy()
+    assert ev == oev and np.array_equal(up, oup) and np.array_equal(dn, odn)
 
 
 @pytest.mark.parametrize("storage", ["int32", "int64"])

@@ -101,6 +101,41 @@ def test_generators_are_conservative(oracle):
     assert oracle.has_negative_cycle(g["n"], g["off"], g["tgt"], g["w"])
 
 
+def test_battery_reference_layout_and_histogram():
+    """nwcch.cch_nb_battery's host conversion to the reference's storage
+    (inline single pieces, pooled longer profiles) keeps every profile, and
+    size_histogram counts as python/cch_nb_battery.py:354-371 does."""
+    from conftest import battery_cases
+    from nwcch import cch_nb_battery as nbb
+    for g, caps in battery_cases():
+        for c in caps:
+            cnt, I1, C1, O1, pst, PI, PC, PO = nbb._reference_layout(c["cnt"], c["poff"], c["pieces"])
+            for d in np.nonzero(cnt)[0]:
+                want = c["pieces"][c["poff"][d]:c["poff"][d + 1]]
+                if cnt[d] == 1:
+                    assert pst[d] == -1 and (I1[d], C1[d], O1[d]) == tuple(want[0])
+                else:
+                    p0 = pst[d]
+                    got = np.stack([PI[p0:p0 + cnt[d]], PC[p0:p0 + cnt[d]], PO[p0:p0 + cnt[d]]], axis=1)
+                    assert np.array_equal(got, want)
+            assert PI.size == int(cnt[cnt > 1].sum())
+            h = nbb.size_histogram(cnt)
+            assert h[0] == np.count_nonzero(cnt == 0) and h[1] == np.count_nonzero(cnt == 1)
+            assert h[2] == np.count_nonzero((cnt >= 2) & (cnt <= 5)) and h[7] == cnt.max()
+
+
+def test_ev_energies_are_conservative(oracle):
+    """The EV energies of a generated graph: steep descents are negative, and
+    no cycle gains charge (label correcting from a vertex converges to a
+    charge no higher than the start where the start is the capacity)."""
+    from nwcch import graphs as G
+    g = G.delaunay(2_000, seed=3)
+    w = G.ev_energies(g)
+    assert (w < 0).any() and (w > 0).any()
+    soc = oracle.battery_label_correcting(g["n"], g["off"], g["tgt"], w, 1e9, 0, 1e9)
+    assert soc[0] == 1e9 and np.all(soc <= 1e9)
+
+
 def test_topology_create_rejects_bad_input_without_gpu(built_lib):
     """Validation happens on the host before any device allocation."""
     import ctypes as C

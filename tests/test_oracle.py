@@ -6,7 +6,7 @@ from __future__ import annotations
 import numpy as np
 import pytest
 
-from conftest import family_case, i32_to_i64, load_golden
+from conftest import battery_cases, family_case, i32_to_i64, load_golden
 
 INF = np.iinfo(np.int64).max
 
@@ -162,21 +162,6 @@ def test_query_path_against_reference(oracle):
             assert np.array_equal(inv[pr], path[off[j]:off[j + 1]])
             if pr.size:
                 assert sum(wmap[(int(a), int(b))] for a, b in zip(inv[pr][:-1], inv[pr][1:])) == d
-
-
-def battery_cases():
-    """battery.npz as a list of (graph dict, [per-capacity dicts])."""
-    B = load_golden("battery.npz")
-    out = []
-    for i in range(int(B["cases"])):
-        pre = f"c{i}_"
-        g = {k[len(pre):]: v for k, v in B.items() if k.startswith(pre) and not k[len(pre):].startswith("m")}
-        caps = []
-        for mi in range(int(B["capacities"])):
-            p2 = f"{pre}m{mi}_"
-            caps.append({k[len(p2):]: v for k, v in B.items() if k.startswith(p2)})
-        out.append((g, caps))
-    return out
 
 
 def test_battery_against_reference(oracle):
