@@ -696,7 +696,7 @@ def main():
     ap.add_argument("--serve-workload", default="delaunay1m", choices=list(WORKLOADS) + ["none"])
     ap.add_argument("--serve-loads", default="1e4,1e5,1e6", help="offered query loads (queries/s)")
     ap.add_argument("--serve-seconds", type=float, default=1.0)
-    ap.add_argument("--battery-workload", default="delaunay264k", choices=list(WORKLOADS) + ["none"],
+    ap.add_argument("--battery-workload", default="none", choices=list(WORKLOADS) + ["none"],
                     help="graph of the battery-constrained profiles section")
     ap.add_argument("--no-tune", action="store_true", help="keep the default query schedule")
     ap.add_argument("--plain-steps", type=int, default=-1,

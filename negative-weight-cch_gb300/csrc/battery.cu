@@ -17,16 +17,28 @@
 // reference's (source piece, target piece) order. The profiles are then the
 // reference's, piece for piece.
 //
+// Float64 on GB300 runs at a small fraction of the integer rate, and the
+// dominance test is most of the work (about 46 float64 operations as
+// written). Here every comparison and minimum runs on order keys of the
+// doubles (an integer order equal to IEEE order, -0 = +0), so the branches
+// taken are the reference's; the values a test reads that depend on one
+// piece only are computed once per piece, with the reference's own
+// expressions (Rich); and the four subtractions left per test are skipped
+// when integer bounds already decide the outcome. Only additions and
+// subtractions produce doubles, each the reference's operation on the same
+// operands.
+//
 // A profile of up to 32 pieces lives in registers, piece l in lane l: one
-// merge is a ballot over the pieces that dominate the candidate, a ballot
-// over the pieces it dominates, a shuffle compaction and an append. Longer
+// merge is a vote over the pieces that dominate the candidate, a ballot over
+// the pieces it dominates, a shuffle compaction and an append. Longer
 // profiles continue in the warp's global buffer. The lower triangles of
 // (y, z) are the x of y's downward list whose rows hold z: 32 are tested at
-// a time (binary search of z in x's row), and the lanes compose the
-// candidates of single-piece sources (most of them) before the merges run in
-// order. Finished profiles are appended to a pool at atomic offsets; counts
-// and offsets index it. A pool or buffer that overflows is flagged, grown
-// by the host, and the customization runs again.
+// a time (binary search of z in x's row); the lanes compose the candidates
+// (single-piece sources, most of them, directly; longer ones 32 at a time)
+// into shared memory, and the merges then run in order. Finished profiles
+// are appended to a pool at atomic offsets; counts and offsets index it. A
+// pool or buffer that overflows is flagged, grown by the host, and the
+// customization runs again.
 //
 // Queries (python/cch_nb_battery.py:296-343): one warp per (s, t, b0). The
 // upward pass over s's ancestors in increasing rank pushes each label through
@@ -38,6 +50,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstring>
 #include <new>
 #include <vector>
 
@@ -53,11 +66,12 @@ constexpr double EPS = 1e-9;
 constexpr int BAT_POOL_OVERFLOW = 1;
 constexpr int BAT_WORK_OVERFLOW = 2;
 constexpr int LEVEL_WARPS = 4;
-constexpr int LEVEL_BLOCKS = 152 * 8;  // resident blocks of the level kernel; one buffer slot per warp
+constexpr int LEVEL_BLOCKS = 152 * 4;  // blocks of the level kernel; one buffer slot per warp
 constexpr int QUERY_WARPS = 4;
 
+// A stored piece, with in - EPS for the queries' feasibility test.
 struct Piece {
-    double i, c, o;
+    double i, c, o, ime;
 };
 
 struct BatStatus {
@@ -71,102 +85,181 @@ struct BatPlan {
     int32_t* dtail = nullptr;  // [m+] tail of darc[p] (the x of y's downward list)
 };
 
+// Integer order key of a double: key(a) < key(b) iff a < b for non-NaN
+// values, with -0 and +0 equal as in IEEE comparisons.
+__device__ __forceinline__ long long dkey(double x) {
+    const long long u = __double_as_longlong(x);
+    return u < 0 ? -(u & 0x7fffffffffffffffLL) : u;
+}
+
+// "v = x; if a < v: v = a", the reference's minimum.
+__device__ __forceinline__ double min_ref(double a, double x) { return dkey(a) < dkey(x) ? a : x; }
+
+// A piece with what the dominance tests read, for capacity M. Flags: the
+// tests' "lo <= b <= hi" and "b < in - EPS" outcomes that depend on the piece
+// alone (python/cch_nb_battery.py:16-44, b in {in, M, out + cost}).
+enum : int { R0 = 1, R1 = 2, R2 = 4, R3 = 8, MLT = 16, OCLT = 32 };
+
+struct Rich {
+    double i, c, o, oc;                                            // in, cost, out, out + cost
+    long long ki, kipe, kime, ko, koc, kv0m, kvMm, kom, kv3m, kvM, kv3;
+    int fl;
+};
+
+struct Cap {
+    double M;
+    long long kM, kMpe;  // keys of M and of M + EPS (the tests' hi)
+};
+
+__device__ __forceinline__ Rich derive(double i, double c, double o, const Cap& K) {
+    Rich r;
+    r.i = i;
+    r.c = c;
+    r.o = o;
+    r.oc = o + c;
+    r.ki = dkey(i);
+    r.kipe = dkey(i + EPS);
+    r.kime = dkey(i - EPS);
+    r.ko = dkey(o);
+    r.koc = dkey(r.oc);
+    r.kv0m = dkey(min_ref(o, i - c) - EPS);       // b = in:        min(out, b - cost) - EPS
+    const double vM = min_ref(o, K.M - c);        // b = M
+    r.kvM = dkey(vM);
+    r.kvMm = dkey(vM - EPS);
+    r.kom = dkey(o - EPS);
+    const double v3 = min_ref(o, r.oc - c);       // b = out + cost
+    r.kv3 = dkey(v3);
+    r.kv3m = dkey(v3 - EPS);
+    int fl = 0;
+    if (r.ki <= K.kMpe) fl |= R0;                 // in <= M + EPS
+    if (r.kime <= K.kM) fl |= R1;                 // in - EPS <= M
+    if (r.koc <= K.kMpe) fl |= R2;                // out + cost <= M + EPS
+    if (r.kime <= r.koc && r.koc <= K.kMpe) fl |= R3;
+    if (K.kM < r.kime) fl |= MLT;                 // M < in - EPS
+    if (r.koc < r.kime) fl |= OCLT;               // out + cost < in - EPS
+    r.fl = fl;
+    return r;
+}
+
 // python/cch_nb_battery.py:16-44: f(b) >= g(b) on [0, M] (with tolerance),
 // tested where the difference can be extreme: g's feasibility start, M and
-// either breakpoint.
-__device__ __forceinline__ bool dominates(const Piece& f, const Piece& g, double M) {
-    if (f.i > g.i + EPS) return false;
-    const double lo = g.i - EPS, hi = M + EPS;
-    const double bs[4] = {g.i, M, f.o + f.c, g.o + g.c};
-#pragma unroll
-    for (int t = 0; t < 4; t++) {
-        const double b = bs[t];
-        if (lo <= b && b <= hi) {
-            if (b < f.i - EPS) return false;
-            double vf = b - f.c;
-            if (f.o < vf) vf = f.o;
-            double vg = b - g.c;
-            if (g.o < vg) vg = g.o;
-            if (vf < vg - EPS) return false;
+// either breakpoint. The result is the conjunction of the reference's
+// checks, so their order does not matter.
+__device__ __forceinline__ bool dominates(const Rich& F, const Rich& G) {
+    if (F.ki > G.kipe) return false;  // f.in > g.in + EPS
+    if (G.fl & R0) {                  // b = g.in
+        if (G.ki < F.kime) return false;
+        if (F.ko < G.kv0m) return false;
+        if (dkey(G.i - F.c) < G.kv0m) return false;
+    }
+    if ((G.fl & R1) && ((F.fl & MLT) || F.kvM < G.kvMm)) return false;  // b = M
+    if ((F.fl & R2) && G.kime <= F.koc) {                                 // b = f.out + f.cost
+        if (F.fl & OCLT) return false;
+        if (F.kv3 < G.kom) {  // else vf >= g.out - EPS >= vg - EPS
+            const double y = F.oc - G.c;
+            const double vg = G.ko < dkey(y) ? G.o : y;
+            if (F.kv3 < dkey(vg - EPS)) return false;
         }
+    }
+    if (G.fl & R3) {  // b = g.out + g.cost
+        if (G.koc < F.kime) return false;
+        if (F.ko < G.kv3m) return false;
+        if (dkey(G.oc - F.c) < G.kv3m) return false;
     }
     return true;
 }
 
 // python/cch_nb_battery.py:159-173: f then g.
-__device__ __forceinline__ bool compose(const Piece& f, const Piece& g, double M, Piece& h) {
-    if (f.o < g.i - EPS) return false;
-    const double hi = f.i > g.i + f.c ? f.i : g.i + f.c;
-    if (hi > M + EPS) return false;
+__device__ __forceinline__ bool compose(const Piece& f, const Piece& g, const Cap& K, Rich& h) {
+    if (dkey(f.o) < dkey(g.ime)) return false;  // f.out < g.in - EPS
+    const double s = g.i + f.c;
+    const double hi = dkey(f.i) > dkey(s) ? f.i : s;
+    if (dkey(hi) > K.kMpe) return false;
     const double hc = f.c + g.c;
     double ho = g.o;
-    if (f.o - g.c < ho) ho = f.o - g.c;
-    if (M - hc < ho) ho = M - hc;
-    h.i = hi;
-    h.c = hc;
-    h.o = ho;
+    const double x = f.o - g.c;
+    if (dkey(x) < dkey(ho)) ho = x;
+    const double y = K.M - hc;
+    if (dkey(y) < dkey(ho)) ho = y;
+    h = derive(hi, hc, ho, K);
     return true;
 }
 
-// Position of the n-th (0-based) set bit of m; n < popc(m).
-__device__ __forceinline__ int nth_set_bit(unsigned m, int n) {
-    int pos = 0;
-#pragma unroll
-    for (int s = 16; s >= 1; s >>= 1) {
-        const unsigned low = m & ((1u << s) - 1u);
-        const int c = __popc(low);
-        if (n >= c) {
-            n -= c;
-            m >>= s;
-            pos += s;
-        } else {
-            m = low;
-        }
-    }
-    return pos;
+// Up to 32 pieces of a profile in shared memory, one per lane, field by
+// field (conflict-free: lane l reads word l of each field).
+struct RichSet {
+    double i[32], c[32], o[32], oc[32];
+    long long ki[32], kipe[32], kime[32], ko[32], koc[32], kv0m[32], kvMm[32], kom[32], kv3m[32], kvM[32], kv3[32];
+    int fl[32];
+};
+
+__device__ __forceinline__ Rich load_rich(const RichSet& S, int l) {
+    return Rich{S.i[l],    S.c[l],    S.o[l],    S.oc[l],   S.ki[l],   S.kipe[l], S.kime[l], S.ko[l],
+                S.koc[l],  S.kv0m[l], S.kvMm[l], S.kom[l],  S.kv3m[l], S.kvM[l],  S.kv3[l],  S.fl[l]};
 }
 
-__device__ __forceinline__ Piece shfl_piece(const Piece& p, int src) {
-    return Piece{__shfl_sync(FULL, p.i, src), __shfl_sync(FULL, p.c, src), __shfl_sync(FULL, p.o, src)};
+__device__ __forceinline__ void store_rich(RichSet& S, int l, const Rich& r) {
+    S.i[l] = r.i;
+    S.c[l] = r.c;
+    S.o[l] = r.o;
+    S.oc[l] = r.oc;
+    S.ki[l] = r.ki;
+    S.kipe[l] = r.kipe;
+    S.kime[l] = r.kime;
+    S.ko[l] = r.ko;
+    S.koc[l] = r.koc;
+    S.kv0m[l] = r.kv0m;
+    S.kvMm[l] = r.kvMm;
+    S.kom[l] = r.kom;
+    S.kv3m[l] = r.kv3m;
+    S.kvM[l] = r.kvM;
+    S.kv3[l] = r.kv3;
+    S.fl[l] = r.fl;
 }
 
-// The profile being built: in registers (lane l holds piece l) while it has
-// at most 32 pieces, else in buf. n and glob are warp-uniform.
+// The profile being built: in the warp's shared RichSet (piece l at slot l)
+// while it has at most 32 pieces, else in buf. n and glob are warp-uniform.
 struct Work {
-    Piece r;
+    RichSet* set;
     int n;
     bool glob;
-    Piece* buf;
+    Rich* buf;
 };
 
 struct BatArgs {
     const double* w;
-    double M;
+    Cap K;
     const int32_t* arcs;
     const int32_t* dtail;
     int32_t* cnt;
     int64_t* pos;
     Piece* pool;
     int64_t pool_cap;
-    Piece* gbuf;  // 2 * gcap pieces per warp slot
+    Rich* gbuf;  // gcap pieces per warp slot
     int32_t gcap;
     BatStatus* status;
     unsigned long long* next;  // per level: arcs handed out
 };
 
 // python/cch_nb_battery.py:186-254: one candidate into the profile.
-__device__ void merge(Work& W, const Piece& h, double M, int32_t gcap, int lane, int& flags) {
+__device__ __noinline__ void merge(Work& W, const Rich& h, int32_t gcap, int lane, int& flags) {
     if (!W.glob) {
         const bool live = lane < W.n;
-        if (__any_sync(FULL, live && dominates(W.r, h, M))) return;
-        const bool keep = live && !dominates(h, W.r, M);
+        Rich g;
+        if (live) g = load_rich(*W.set, lane);
+        if (__any_sync(FULL, live && dominates(g, h))) return;
+        const bool keep = live && !dominates(h, g);
         const unsigned km = __ballot_sync(FULL, keep);
         const int k = __popc(km);
-        Piece g = shfl_piece(W.r, lane < k ? nth_set_bit(km, lane) : lane);
         if (k < 32) {
-            if (lane == k) g = h;
-            W.r = g;
+            if (km != (1u << k) - 1u) {
+                __syncwarp();
+                if (keep) store_rich(*W.set, __popc(km & ((1u << lane) - 1u)), g);
+            }
+            __syncwarp();
+            if (lane == 0) store_rich(*W.set, k, h);
             W.n = k + 1;
+            __syncwarp();
         } else {  // 33 pieces: continue in the global buffer (gcap >= 64)
             W.buf[lane] = g;
             if (lane == 0) W.buf[32] = h;
@@ -178,16 +271,17 @@ __device__ void merge(Work& W, const Piece& h, double M, int32_t gcap, int lane,
     }
     for (int b = 0; b < W.n; b += 32) {
         const bool live = b + lane < W.n;
-        Piece g{0.0, 0.0, 0.0};
-        if (live) g = W.buf[b + lane];
-        if (__any_sync(FULL, live && dominates(g, h, M))) return;
+        if (__any_sync(FULL, live && dominates(W.buf[b + lane], h))) return;
     }
     int k = 0;
     for (int b = 0; b < W.n; b += 32) {
         const bool live = b + lane < W.n;
-        Piece g{0.0, 0.0, 0.0};
-        if (live) g = W.buf[b + lane];
-        const bool keep = live && !dominates(h, g, M);
+        Rich g;
+        bool keep = false;
+        if (live) {
+            g = W.buf[b + lane];
+            keep = !dominates(h, g);
+        }
         const unsigned km = __ballot_sync(FULL, keep);
         // writes land at or below every position this round has read
         if (keep) W.buf[k + __popc(km & ((1u << lane) - 1u))] = g;
@@ -203,29 +297,41 @@ __device__ void merge(Work& W, const Piece& h, double M, int32_t gcap, int lane,
     W.n = k + 1;
     __syncwarp();
     if (W.n <= 32) {
-        W.r = lane < W.n ? W.buf[lane] : Piece{0.0, 0.0, 0.0};
+        if (lane < W.n) store_rich(*W.set, lane, W.buf[lane]);
         W.glob = false;
+        __syncwarp();
+    }
+}
+
+// Merges the candidates staged in S (bits of vm, ascending lane order).
+__device__ __forceinline__ void merge_staged(Work& W, const Rich* S, unsigned vm, int32_t gcap, int lane,
+                                             int& flags) {
+    while (vm) {
+        const int src = __ffs(vm) - 1;
+        vm &= vm - 1;
+        merge(W, S[src], gcap, lane, flags);
     }
 }
 
 // The candidates of one lower triangle side with general source profiles:
 // f pieces (direction df) then g pieces (dg), f-major as the reference.
-__device__ void merge_triangle(Work& W, const BatArgs& A, int64_t df, int64_t dg, int lane, int& flags) {
+__device__ __noinline__ void merge_triangle(Work& W, const BatArgs& A, int64_t df, int64_t dg, Rich* S, int lane, int& flags) {
     const int32_t na = A.cnt[df], nb = A.cnt[dg];
     if (na == 0 || nb == 0) return;
     const int64_t fa = A.pos[df], ga = A.pos[dg];
-    const int64_t tot = (int64_t)na * nb;
-    for (int64_t qb = 0; qb < tot; qb += 32) {
-        const int64_t q = qb + lane;
-        Piece h{0.0, 0.0, 0.0};
+    const int32_t tot = na * nb;
+    for (int32_t qb = 0; qb < tot; qb += 32) {
+        const int32_t q = qb + lane;
         bool ok = false;
-        if (q < tot) ok = compose(A.pool[fa + q / nb], A.pool[ga + q % nb], A.M, h);
-        unsigned vm = __ballot_sync(FULL, ok);
-        while (vm) {
-            const int src = __ffs(vm) - 1;
-            vm &= vm - 1;
-            merge(W, shfl_piece(h, src), A.M, A.gcap, lane, flags);
+        if (q < tot) {
+            Rich h;
+            ok = compose(A.pool[fa + q / nb], A.pool[ga + q % nb], A.K, h);
+            if (ok) S[lane] = h;
         }
+        const unsigned vm = __ballot_sync(FULL, ok);
+        __syncwarp();
+        merge_staged(W, S, vm, A.gcap, lane, flags);
+        __syncwarp();
     }
 }
 
@@ -243,9 +349,15 @@ __device__ void finish(const Work& W, const BatArgs& A, int64_t d, int lane, int
         return;
     }
     if (!W.glob) {
-        if (lane < n) A.pool[p + lane] = W.r;
+        if (lane < n) {
+            const double i = W.set->i[lane];
+            A.pool[p + lane] = Piece{i, W.set->c[lane], W.set->o[lane], i - EPS};
+        }
     } else {
-        for (int t = lane; t < n; t += 32) A.pool[p + t] = W.buf[t];
+        for (int t = lane; t < n; t += 32) {
+            const Rich& r = W.buf[t];
+            A.pool[p + t] = Piece{r.i, r.c, r.o, r.i - EPS};
+        }
     }
     if (lane == 0) {
         A.cnt[d] = n;
@@ -258,25 +370,34 @@ __device__ __forceinline__ int side_kind(int32_t nf, int32_t ng) {
     return (nf == 0 || ng == 0) ? 0 : (nf == 1 && ng == 1) ? 1 : 2;
 }
 
-__device__ void customize_arc(const DevTopo& D, const BatArgs& A, int32_t j, Piece* gb, int lane, int& flags,
-                              int& seen) {
-    const double M = A.M;
+// Shared memory of one warp: the single-piece candidates of up to 32
+// triangles and a chunk of a general triangle's.
+struct WarpStage {
+    Rich s1[32], sg[32];
+    RichSet prof;
+};
+
+// One profile of arc j: side 0 = up(y, z), side 1 = down(y, z). The two
+// sides are built one after the other (the triangle search runs twice), so
+// that one profile is live in registers at a time.
+__device__ void customize_side(const DevTopo& D, const BatArgs& A, int32_t j, int side, Rich* gb, WarpStage& st,
+                               int lane, int& flags, int& seen) {
+    const double M = A.K.M;
     const int32_t y = D.tail[j], z = D.head[j];
-    Work U{Piece{0.0, 0.0, 0.0}, 0, false, gb};
-    Work V{Piece{0.0, 0.0, 0.0}, 0, false, gb + A.gcap};
+    Work W{&st.prof, 0, false, gb};
     // python/cch_nb_battery.py:67-82: the original arcs onto j, input order
     for (int64_t e = D.aeoff[j]; e < D.aeoff[j + 1]; e++) {
         const int32_t k = D.aeidx[e];
+        if ((D.e_up[k] != 0) != (side == 0)) continue;
         const double c = A.w[k];
-        Piece h;
+        Rich h;
         if (c >= 0) {
             if (c > M) continue;
-            h = Piece{c, c, M - c};
+            h = derive(c, c, M - c, A.K);
         } else {
-            h = Piece{0.0, c, M};
+            h = derive(0.0, c, M, A.K);
         }
-        if (D.e_up[k]) merge(U, h, M, A.gcap, lane, flags);
-        else merge(V, h, M, A.gcap, lane, flags);
+        merge(W, h, A.gcap, lane, flags);
     }
     // lower triangles (x; y, z), x ascending:
     //   up(y,z)   <- down(x,y) then up(x,z)
@@ -284,9 +405,9 @@ __device__ void customize_arc(const DevTopo& D, const BatArgs& A, int32_t j, Pie
     const int64_t p1 = D.doff[y + 1];
     for (int64_t pb = D.doff[y]; pb < p1; pb += 32) {
         const int64_t p = pb + lane;
-        int64_t i = -1, kk = -1;
+        int64_t df = -1, dg = -1;
         if (p < p1) {
-            i = D.darc[p];
+            const int64_t i = D.darc[p];
             const int32_t x = A.dtail[p];
             const int64_t end = D.first[x + 1];
             int64_t lo = i + 1, hi = end;
@@ -295,45 +416,50 @@ __device__ void customize_arc(const DevTopo& D, const BatArgs& A, int32_t j, Pie
                 if (D.head[mid] < z) lo = mid + 1;
                 else hi = mid;
             }
-            if (lo < end && D.head[lo] == z) kk = lo;
-        }
-        unsigned hits = __ballot_sync(FULL, kk >= 0);
-        if (!hits) continue;
-        int ku = 0, kd = 0;
-        bool oku = false, okd = false;
-        Piece hu{0.0, 0.0, 0.0}, hd{0.0, 0.0, 0.0};
-        if (kk >= 0) {
-            ku = side_kind(A.cnt[2 * i + 1], A.cnt[2 * kk]);
-            kd = side_kind(A.cnt[2 * kk + 1], A.cnt[2 * i]);
-            if (ku == 1) oku = compose(A.pool[A.pos[2 * i + 1]], A.pool[A.pos[2 * kk]], M, hu);
-            if (kd == 1) okd = compose(A.pool[A.pos[2 * kk + 1]], A.pool[A.pos[2 * i]], M, hd);
-        }
-        while (hits) {
-            const int src = __ffs(hits) - 1;
-            hits &= hits - 1;
-            const int su = __shfl_sync(FULL, ku, src), sd = __shfl_sync(FULL, kd, src);
-            const int64_t si = __shfl_sync(FULL, i, src), sk = __shfl_sync(FULL, kk, src);
-            if (su == 1) {
-                if (__shfl_sync(FULL, (int)oku, src)) merge(U, shfl_piece(hu, src), M, A.gcap, lane, flags);
-            } else if (su == 2) {
-                merge_triangle(U, A, 2 * si + 1, 2 * sk, lane, flags);
+            if (lo < end && D.head[lo] == z) {
+                df = side == 0 ? 2 * i + 1 : 2 * lo + 1;
+                dg = side == 0 ? 2 * lo : 2 * i;
             }
-            if (sd == 1) {
-                if (__shfl_sync(FULL, (int)okd, src)) merge(V, shfl_piece(hd, src), M, A.gcap, lane, flags);
-            } else if (sd == 2) {
-                merge_triangle(V, A, 2 * sk + 1, 2 * si, lane, flags);
+        }
+        int kind = 0;
+        bool ok = false;
+        if (df >= 0) {
+            kind = side_kind(A.cnt[df], A.cnt[dg]);
+            Rich h;
+            if (kind == 1 && compose(A.pool[A.pos[df]], A.pool[A.pos[dg]], A.K, h)) {
+                st.s1[lane] = h;
+                ok = true;
+            }
+        }
+        const unsigned m1 = __ballot_sync(FULL, ok);
+        unsigned mg = __ballot_sync(FULL, kind == 2);
+        __syncwarp();
+        if (!mg) {  // single-piece sources only: the staged candidates in order
+            merge_staged(W, st.s1, m1, A.gcap, lane, flags);
+            continue;
+        }
+        unsigned todo = m1 | mg;
+        while (todo) {
+            const int src = __ffs(todo) - 1;
+            todo &= todo - 1;
+            if (m1 & (1u << src)) {
+                merge(W, st.s1[src], A.gcap, lane, flags);
+            } else {
+                const int64_t sf = __shfl_sync(FULL, df, src), sg = __shfl_sync(FULL, dg, src);
+                merge_triangle(W, A, sf, sg, st.sg, lane, flags);
             }
         }
     }
-    finish(U, A, 2 * (int64_t)j, lane, flags, seen);
-    finish(V, A, 2 * (int64_t)j + 1, lane, flags, seen);
+    finish(W, A, 2 * (int64_t)j + side, lane, flags, seen);
 }
 
 __global__ void __launch_bounds__(32 * LEVEL_WARPS) k_bat_level(DevTopo D, BatArgs A, int64_t a0, int64_t a1,
                                                                  int32_t level) {
-    const int lane = threadIdx.x & 31;
-    const int64_t slot = (int64_t)blockIdx.x * LEVEL_WARPS + (threadIdx.x >> 5);
-    Piece* gb = A.gbuf + slot * 2 * (int64_t)A.gcap;
+    extern __shared__ __align__(16) unsigned char bat_smem[];
+    WarpStage* stages = reinterpret_cast<WarpStage*>(bat_smem);
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int64_t slot = (int64_t)blockIdx.x * LEVEL_WARPS + wib;
+    Rich* gb = A.gbuf + slot * (int64_t)A.gcap;
     int flags = 0, seen = 0;
     for (;;) {
         unsigned long long idx = 0;
@@ -341,7 +467,9 @@ __global__ void __launch_bounds__(32 * LEVEL_WARPS) k_bat_level(DevTopo D, BatAr
         idx = __shfl_sync(FULL, idx, 0);
         const int64_t e = a0 + (int64_t)idx;
         if (e >= a1) break;
-        customize_arc(D, A, A.arcs[e], gb, lane, flags, seen);
+        const int32_t j = A.arcs[e];
+        customize_side(D, A, j, 0, gb, stages[wib], lane, flags, seen);
+        customize_side(D, A, j, 1, gb, stages[wib], lane, flags, seen);
     }
     flags = (int)__reduce_or_sync(FULL, (unsigned)flags);
     if (flags && lane == 0) atomicOr(&A.status->flags, flags);
@@ -359,17 +487,23 @@ struct BatDev {
     const Piece* pool;
 };
 
-// python/cch_nb_battery.py:272-293
+// python/cch_nb_battery.py:272-293, comparisons on order keys.
 __device__ __forceinline__ double eval_profile(const BatDev& B, int64_t d, double b) {
     double best = -INFINITY;
+    long long kbest = dkey(-INFINITY);
+    const long long kb = dkey(b);
     const int32_t n = B.cnt[d];
     const Piece* p = B.pool + B.pos[d];
     for (int32_t t = 0; t < n; t++) {
         const Piece f = p[t];
-        if (b >= f.i - EPS) {
+        if (kb >= dkey(f.ime)) {
             double v = b - f.c;
-            if (f.o < v) v = f.o;
-            if (v > best) best = v;
+            if (dkey(f.o) < dkey(v)) v = f.o;
+            const long long kv = dkey(v);
+            if (kv > kbest) {
+                best = v;
+                kbest = kv;
+            }
         }
     }
     return best;
@@ -524,16 +658,27 @@ extern "C" void nwcch_battery_free(nwcch_battery* b) {
 
 namespace {
 
-int run_levels(nwcch_topology* t, nwcch_battery* b, const BatPlan* P, const double* w, Piece* gbuf, int32_t gcap,
+// dkey on the host (same integer order of doubles).
+long long host_key(double x) {
+    long long u;
+    std::memcpy(&u, &x, sizeof(u));
+    return u < 0 ? -(u & 0x7fffffffffffffffLL) : u;
+}
+
+int run_levels(nwcch_topology* t, nwcch_battery* b, const BatPlan* P, const double* w, Rich* gbuf, int32_t gcap,
                unsigned long long* next, cudaStream_t s, BatStatus* host) {
     NWCCH_CUDA_TRY(cudaMemsetAsync(next, 0, sizeof(unsigned long long) * std::max<int32_t>(1, t->levels), s));
     NWCCH_CUDA_TRY(cudaMemsetAsync(b->status, 0, sizeof(BatStatus), s));
-    BatArgs A{w, b->M, P->arcs, P->dtail, b->cnt, b->pos, b->pool, b->pool_cap, gbuf, gcap, b->status, next};
+    const double Mpe = b->M + EPS;  // the tests' hi, as the reference computes it
+    Cap K{b->M, host_key(b->M), host_key(Mpe)};
+    BatArgs A{w, K, P->arcs, P->dtail, b->cnt, b->pos, b->pool, b->pool_cap, gbuf, gcap, b->status, next};
+    const size_t smem = sizeof(WarpStage) * LEVEL_WARPS;
+    NWCCH_CUDA_TRY(cudaFuncSetAttribute(k_bat_level, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     for (int32_t l = 0; l < t->levels; l++) {
         const int64_t a0 = t->level_arc_off[l], a1 = t->level_arc_off[l + 1];
         if (a1 == a0) continue;
         const int64_t blocks = std::min<int64_t>((a1 - a0 + LEVEL_WARPS - 1) / LEVEL_WARPS, LEVEL_BLOCKS);
-        k_bat_level<<<(unsigned)blocks, 32 * LEVEL_WARPS, 0, s>>>(t->d, A, a0, a1, l);
+        k_bat_level<<<(unsigned)blocks, 32 * LEVEL_WARPS, smem, s>>>(t->d, A, a0, a1, l);
     }
     NWCCH_CUDA_TRY(cudaGetLastError());
     NWCCH_CUDA_TRY(cudaMemcpyAsync(host, b->status, sizeof(BatStatus), cudaMemcpyDeviceToHost, s));
@@ -572,10 +717,10 @@ extern "C" int nwcch_battery_customize(nwcch_topology* t, const double* w_dev, d
     BatStatus host{};
     rc = NWCCH_OK;
     if (cudaMallocAsync(&next, sizeof(unsigned long long) * std::max<int32_t>(1, t->levels), s) != cudaSuccess ||
-        cudaMallocAsync(&gbuf, (size_t)slots * 2 * gcap * sizeof(Piece), s) != cudaSuccess)
+        cudaMallocAsync(&gbuf, (size_t)slots * gcap * sizeof(Rich), s) != cudaSuccess)
         rc = NWCCH_ERR_NOMEM;
     for (int attempt = 0; rc == NWCCH_OK; attempt++) {
-        rc = run_levels(t, b, P, w_dev, static_cast<Piece*>(gbuf), gcap, static_cast<unsigned long long*>(next), s,
+        rc = run_levels(t, b, P, w_dev, static_cast<Rich*>(gbuf), gcap, static_cast<unsigned long long*>(next), s,
                         &host);
         if (rc || host.flags == 0) break;
         if (attempt >= 12) {
@@ -597,7 +742,7 @@ extern "C" int nwcch_battery_customize(nwcch_topology* t, const double* w_dev, d
             gcap *= 4;
             cudaFreeAsync(gbuf, s);
             gbuf = nullptr;
-            if (cudaMallocAsync(&gbuf, (size_t)slots * 2 * gcap * sizeof(Piece), s) != cudaSuccess)
+            if (cudaMallocAsync(&gbuf, (size_t)slots * gcap * sizeof(Rich), s) != cudaSuccess)
                 rc = NWCCH_ERR_NOMEM;
         }
     }

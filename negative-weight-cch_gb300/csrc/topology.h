@@ -43,7 +43,7 @@ struct Tuning {
     int64_t update_budget_ns = 0;           // level-sweep budget of an update (0: from the triangle count)
     int64_t update_dense_min = 0;           // updates of at least this many arcs skip the sweep (0: never)
     int64_t battery_pool = 0;               // initial battery piece pool (0: 1.5 pieces a direction)
-    int32_t battery_buffer = 256;           // initial per-warp buffer of a long battery profile (pieces)
+    int32_t battery_buffer = 128;           // initial per-warp buffer of a long battery profile (pieces)
 };
 
 // Device words private to the calls enqueued on one stream: the error word
