@@ -303,14 +303,78 @@ __device__ __noinline__ void merge(Work& W, const Rich& h, int32_t gcap, int lan
     }
 }
 
-// Merges the candidates staged in S (bits of vm, ascending lane order).
-__device__ __forceinline__ void merge_staged(Work& W, const Rich* S, unsigned vm, int32_t gcap, int lane,
-                                             int& flags) {
-    while (vm) {
-        const int src = __ffs(vm) - 1;
-        vm &= vm - 1;
-        merge(W, S[src], gcap, lane, flags);
+// Merges the candidates staged in S (bits of vm, ascending lane order), with
+// the outcome of merging them one at a time. In the shared-memory form the
+// lanes first test their own candidates, in parallel, against the profile P0
+// the batch starts from, newest piece first (most candidates are dominated
+// by the newest piece). Then, in order: a candidate whose dominator is still
+// present is dropped at the cost of a bit test; any other is tested exactly
+// against the pieces present at its turn (P0's survivors and the batch's
+// inserted candidates, held by their lanes), and if it is kept it removes
+// what it dominates. The result is P0's survivors, then the inserted
+// survivors, each in order: the one-at-a-time merge's profile.
+__device__ __noinline__ void merge_staged(Work& W, const Rich* S, unsigned vm, int32_t gcap, int lane,
+                                          int& flags) {
+    if (!vm) return;
+    if (W.glob) {
+        while (vm) {
+            const int src = __ffs(vm) - 1;
+            vm &= vm - 1;
+            merge(W, S[src], gcap, lane, flags);
+        }
+        return;
     }
+    const int n = W.n;
+    const bool mine = (vm >> lane) & 1u;
+    Rich h{};
+    int gj = -1;
+    if (mine) {
+        h = S[lane];
+        for (int k = n - 1; k >= 0; k--)
+            if (dominates(load_rich(*W.set, k), h)) {
+                gj = k;
+                break;
+            }
+    }
+    unsigned removed = 0;  // P0 pieces removed (bit k)
+    unsigned ins = 0;      // inserted candidates still present (bit = lane)
+    unsigned todo = vm;
+    while (todo) {
+        const int j = __ffs(todo) - 1;
+        todo &= todo - 1;
+        const int g = __shfl_sync(FULL, gj, j);
+        if (g >= 0 && !((removed >> g) & 1u)) continue;  // its dominator is present
+        const Rich& hj = S[j];
+        bool d = false;
+        if (g >= 0 && lane < n && !((removed >> lane) & 1u)) d = dominates(load_rich(*W.set, lane), hj);
+        if (((ins >> lane) & 1u) && dominates(h, hj)) d = true;
+        if (__any_sync(FULL, d)) continue;
+        const bool rp = lane < n && !((removed >> lane) & 1u) && dominates(hj, load_rich(*W.set, lane));
+        const bool ri = ((ins >> lane) & 1u) && dominates(hj, h);
+        removed |= __ballot_sync(FULL, rp);
+        ins = (ins & ~__ballot_sync(FULL, ri)) | (1u << j);
+    }
+    if (!ins && !removed) return;  // every candidate dropped
+    const unsigned keepP = (n == 32 ? FULL : ((1u << n) - 1u)) & ~removed;
+    const int np = __popc(keepP), total = np + __popc(ins);
+    const unsigned lt = (1u << lane) - 1u;
+    if (total <= 32) {
+        Rich g{};
+        const bool kp = (keepP >> lane) & 1u;
+        if (kp) g = load_rich(*W.set, lane);
+        __syncwarp();
+        if (kp) store_rich(*W.set, __popc(keepP & lt), g);
+        if ((ins >> lane) & 1u) store_rich(*W.set, np + __popc(ins & lt), h);
+        W.n = total;
+        __syncwarp();
+        return;
+    }
+    // more than 32 pieces: continue in the global buffer (gcap >= 64)
+    if ((keepP >> lane) & 1u) W.buf[__popc(keepP & lt)] = load_rich(*W.set, lane);
+    if ((ins >> lane) & 1u) W.buf[np + __popc(ins & lt)] = h;
+    W.n = total;
+    W.glob = true;
+    __syncwarp();
 }
 
 // The candidates of one lower triangle side with general source profiles:
