@@ -313,10 +313,15 @@ __device__ __noinline__ void merge(Work& W, const Rich& h, int32_t gcap, int lan
 // inserted candidates, held by their lanes), and if it is kept it removes
 // what it dominates. The result is P0's survivors, then the inserted
 // survivors, each in order: the one-at-a-time merge's profile.
+__device__ __forceinline__ Rich piece_at(const Work& W, int k) {
+    return W.glob ? W.buf[k] : load_rich(*W.set, k);
+}
+
 __device__ __noinline__ void merge_staged(Work& W, const Rich* S, unsigned vm, int32_t gcap, int lane,
                                           int& flags) {
     if (!vm) return;
-    if (W.glob) {
+    const int n = W.n;
+    if (n > 32 * 32) {  // beyond the removal bitmap: one at a time
         while (vm) {
             const int src = __ffs(vm) - 1;
             vm &= vm - 1;
@@ -324,41 +329,58 @@ __device__ __noinline__ void merge_staged(Work& W, const Rich* S, unsigned vm, i
         }
         return;
     }
-    const int n = W.n;
     const bool mine = (vm >> lane) & 1u;
     Rich h{};
     int gj = -1;
     if (mine) {
         h = S[lane];
         for (int k = n - 1; k >= 0; k--)
-            if (dominates(load_rich(*W.set, k), h)) {
+            if (dominates(piece_at(W, k), h)) {
                 gj = k;
                 break;
             }
     }
-    unsigned removed = 0;  // P0 pieces removed (bit k)
-    unsigned ins = 0;      // inserted candidates still present (bit = lane)
+    const int chunks = (n + 31) >> 5;
+    unsigned remw = 0;  // lane c: P0 pieces 32c..32c+31 removed
+    int nrem = 0;
+    unsigned ins = 0;   // inserted candidates still present (bit = lane)
     unsigned todo = vm;
     while (todo) {
         const int j = __ffs(todo) - 1;
         todo &= todo - 1;
         const int g = __shfl_sync(FULL, gj, j);
-        if (g >= 0 && !((removed >> g) & 1u)) continue;  // its dominator is present
+        if (g >= 0 && !((__shfl_sync(FULL, remw, g >> 5) >> (g & 31)) & 1u)) continue;  // dominator present
         const Rich& hj = S[j];
-        bool d = false;
-        if (g >= 0 && lane < n && !((removed >> lane) & 1u)) d = dominates(load_rich(*W.set, lane), hj);
-        if (((ins >> lane) & 1u) && dominates(h, hj)) d = true;
+        bool d = ((ins >> lane) & 1u) && dominates(h, hj);
+        if (g >= 0) {
+            for (int c = 0; c < chunks; c++) {
+                const int k = 32 * c + lane;
+                const unsigned rw = __shfl_sync(FULL, remw, c);
+                if (k < n && !((rw >> lane) & 1u) && dominates(piece_at(W, k), hj)) d = true;
+                if (__any_sync(FULL, d)) break;
+            }
+        }
         if (__any_sync(FULL, d)) continue;
-        const bool rp = lane < n && !((removed >> lane) & 1u) && dominates(hj, load_rich(*W.set, lane));
+        for (int c = 0; c < chunks; c++) {
+            const int k = 32 * c + lane;
+            const unsigned rw = __shfl_sync(FULL, remw, c);
+            const bool rp = k < n && !((rw >> lane) & 1u) && dominates(hj, piece_at(W, k));
+            const unsigned mk = __ballot_sync(FULL, rp);
+            nrem += __popc(mk);
+            if (lane == c) remw |= mk;
+        }
         const bool ri = ((ins >> lane) & 1u) && dominates(hj, h);
-        removed |= __ballot_sync(FULL, rp);
         ins = (ins & ~__ballot_sync(FULL, ri)) | (1u << j);
     }
-    if (!ins && !removed) return;  // every candidate dropped
-    const unsigned keepP = (n == 32 ? FULL : ((1u << n) - 1u)) & ~removed;
-    const int np = __popc(keepP), total = np + __popc(ins);
+    if (!ins && !nrem) return;  // every candidate dropped
+    const int np = n - nrem, total = np + __popc(ins);
     const unsigned lt = (1u << lane) - 1u;
-    if (total <= 32) {
+    if (total > gcap) {
+        flags |= BAT_WORK_OVERFLOW;
+        return;
+    }
+    if (!W.glob && total <= 32) {
+        const unsigned keepP = (n == 32 ? FULL : ((1u << n) - 1u)) & ~__shfl_sync(FULL, remw, 0);
         Rich g{};
         const bool kp = (keepP >> lane) & 1u;
         if (kp) g = load_rich(*W.set, lane);
@@ -369,12 +391,30 @@ __device__ __noinline__ void merge_staged(Work& W, const Rich* S, unsigned vm, i
         __syncwarp();
         return;
     }
-    // more than 32 pieces: continue in the global buffer (gcap >= 64)
-    if ((keepP >> lane) & 1u) W.buf[__popc(keepP & lt)] = load_rich(*W.set, lane);
+    // the global buffer: P0's survivors (compacted in place when P0 is
+    // there already: writes land at or below every position read), then the
+    // inserted candidates
+    int k0 = 0;
+    for (int c = 0; c < chunks; c++) {
+        const int k = 32 * c + lane;
+        const unsigned rw = __shfl_sync(FULL, remw, c);
+        const bool keep = k < n && !((rw >> lane) & 1u);
+        Rich g{};
+        if (keep) g = piece_at(W, k);
+        const unsigned km = __ballot_sync(FULL, keep);
+        __syncwarp();
+        if (keep) W.buf[k0 + __popc(km & lt)] = g;
+        k0 += __popc(km);
+    }
     if ((ins >> lane) & 1u) W.buf[np + __popc(ins & lt)] = h;
     W.n = total;
     W.glob = true;
     __syncwarp();
+    if (total <= 32) {
+        if (lane < total) store_rich(*W.set, lane, W.buf[lane]);
+        W.glob = false;
+        __syncwarp();
+    }
 }
 
 // The candidates of one lower triangle side with general source profiles:
