@@ -83,6 +83,7 @@ struct BatStatus {
 struct BatPlan {
     int32_t* arcs = nullptr;   // [m+] arcs by level of their tail, then tail rank
     int32_t* dtail = nullptr;  // [m+] tail of darc[p] (the x of y's downward list)
+    int64_t max_down = 0;      // longest downward list
 };
 
 // Integer order key of a double: key(a) < key(b) iff a < b for non-NaN
@@ -236,6 +237,8 @@ struct BatArgs {
     Piece* pool;
     int64_t pool_cap;
     Rich* gbuf;  // gcap pieces per warp slot
+    int2* tri;   // max_down lower triangles per warp slot
+    int64_t max_down;
     int32_t gcap;
     BatStatus* status;
     unsigned long long* next;  // per level: arcs handed out
@@ -317,7 +320,7 @@ __device__ __forceinline__ Rich piece_at(const Work& W, int k) {
     return W.glob ? W.buf[k] : load_rich(*W.set, k);
 }
 
-__device__ __noinline__ void merge_staged(Work& W, const Rich* S, unsigned vm, int32_t gcap, int lane,
+__device__ __noinline__ void merge_staged(Work& W, Rich* S, unsigned vm, const Cap& K, int32_t gcap, int lane,
                                           int& flags) {
     if (!vm) return;
     const int n = W.n;
@@ -434,7 +437,7 @@ __device__ __noinline__ void merge_triangle(Work& W, const BatArgs& A, int64_t d
         }
         const unsigned vm = __ballot_sync(FULL, ok);
         __syncwarp();
-        merge_staged(W, S, vm, A.gcap, lane, flags);
+        merge_staged(W, S, vm, A.K, A.gcap, lane, flags);
         __syncwarp();
     }
 }
@@ -481,15 +484,41 @@ struct WarpStage {
     RichSet prof;
 };
 
-// One profile of arc j: side 0 = up(y, z), side 1 = down(y, z). The two
-// sides are built one after the other (the triangle search runs twice), so
-// that one profile is live in registers at a time.
-__device__ void customize_side(const DevTopo& D, const BatArgs& A, int32_t j, int side, Rich* gb, WarpStage& st,
-                               int lane, int& flags, int& seen) {
-    const double M = A.K.M;
-    const int32_t y = D.tail[j], z = D.head[j];
-    Work W{&st.prof, 0, false, gb};
+// One chunk of lower triangles, each lane one triangle side (sources df, dg;
+// df < 0: none), in order: the candidates of single-piece sources are
+// composed by their lanes and merged as a batch; a general triangle's are
+// merged 32 at a time where it falls in the order.
+__device__ void merge_chunk(Work& W, const BatArgs& A, WarpStage& st, int64_t df, int64_t dg, int lane,
+                            int& flags) {
+    int kind = 0;
+    bool ok = false;
+    if (df >= 0) {
+        kind = side_kind(A.cnt[df], A.cnt[dg]);
+        Rich h;
+        if (kind == 1 && compose(A.pool[A.pos[df]], A.pool[A.pos[dg]], A.K, h)) {
+            st.s1[lane] = h;
+            ok = true;
+        }
+    }
+    const unsigned m1 = __ballot_sync(FULL, ok);
+    unsigned mg = __ballot_sync(FULL, kind == 2);
+    __syncwarp();
+    unsigned done = 0;  // lanes below the next general triangle are merged
+    while (mg) {
+        const int src = __ffs(mg) - 1;
+        mg &= mg - 1;
+        const unsigned below = (1u << src) - 1u;
+        merge_staged(W, st.s1, m1 & below & ~done, A.K, A.gcap, lane, flags);
+        done = below | (1u << src);
+        const int64_t sf = __shfl_sync(FULL, df, src), sg = __shfl_sync(FULL, dg, src);
+        merge_triangle(W, A, sf, sg, st.sg, lane, flags);
+    }
+    merge_staged(W, st.s1, m1 & ~done, A.K, A.gcap, lane, flags);
+}
+
+__device__ void merge_base(Work& W, const DevTopo& D, const BatArgs& A, int32_t j, int side, int lane, int& flags) {
     // python/cch_nb_battery.py:67-82: the original arcs onto j, input order
+    const double M = A.K.M;
     for (int64_t e = D.aeoff[j]; e < D.aeoff[j + 1]; e++) {
         const int32_t k = D.aeidx[e];
         if ((D.e_up[k] != 0) != (side == 0)) continue;
@@ -503,15 +532,28 @@ __device__ void customize_side(const DevTopo& D, const BatArgs& A, int32_t j, in
         }
         merge(W, h, A.gcap, lane, flags);
     }
-    // lower triangles (x; y, z), x ascending:
-    //   up(y,z)   <- down(x,y) then up(x,z)
-    //   down(y,z) <- down(x,z) then up(x,y)
+}
+
+// The two profiles of arc j = (y, z), one after the other (one profile live
+// at a time), over its lower triangles (x; y, z), x ascending:
+//   up(y,z)   <- down(x,y) then up(x,z)
+//   down(y,z) <- down(x,z) then up(x,y)
+// The up pass finds the triangles (binary search of z in the rows of y's
+// downward list) and keeps them in the warp's list tri; the down pass reads
+// them back.
+__device__ void customize_arc(const DevTopo& D, const BatArgs& A, int32_t j, Rich* gb, int2* tri, WarpStage& st,
+                              int lane, int& flags, int& seen) {
+    const int32_t y = D.tail[j], z = D.head[j];
+    const unsigned lt = (1u << lane) - 1u;
+    Work W{&st.prof, 0, false, gb};
+    merge_base(W, D, A, j, 0, lane, flags);
     const int64_t p1 = D.doff[y + 1];
+    int ntri = 0;
     for (int64_t pb = D.doff[y]; pb < p1; pb += 32) {
         const int64_t p = pb + lane;
-        int64_t df = -1, dg = -1;
+        int64_t i = -1, kk = -1;
         if (p < p1) {
-            const int64_t i = D.darc[p];
+            i = D.darc[p];
             const int32_t x = A.dtail[p];
             const int64_t end = D.first[x + 1];
             int64_t lo = i + 1, hi = end;
@@ -520,41 +562,28 @@ __device__ void customize_side(const DevTopo& D, const BatArgs& A, int32_t j, in
                 if (D.head[mid] < z) lo = mid + 1;
                 else hi = mid;
             }
-            if (lo < end && D.head[lo] == z) {
-                df = side == 0 ? 2 * i + 1 : 2 * lo + 1;
-                dg = side == 0 ? 2 * lo : 2 * i;
-            }
+            if (lo < end && D.head[lo] == z) kk = lo;
         }
-        int kind = 0;
-        bool ok = false;
-        if (df >= 0) {
-            kind = side_kind(A.cnt[df], A.cnt[dg]);
-            Rich h;
-            if (kind == 1 && compose(A.pool[A.pos[df]], A.pool[A.pos[dg]], A.K, h)) {
-                st.s1[lane] = h;
-                ok = true;
-            }
-        }
-        const unsigned m1 = __ballot_sync(FULL, ok);
-        unsigned mg = __ballot_sync(FULL, kind == 2);
-        __syncwarp();
-        if (!mg) {  // single-piece sources only: the staged candidates in order
-            merge_staged(W, st.s1, m1, A.gcap, lane, flags);
-            continue;
-        }
-        unsigned todo = m1 | mg;
-        while (todo) {
-            const int src = __ffs(todo) - 1;
-            todo &= todo - 1;
-            if (m1 & (1u << src)) {
-                merge(W, st.s1[src], A.gcap, lane, flags);
-            } else {
-                const int64_t sf = __shfl_sync(FULL, df, src), sg = __shfl_sync(FULL, dg, src);
-                merge_triangle(W, A, sf, sg, st.sg, lane, flags);
-            }
-        }
+        const unsigned hm = __ballot_sync(FULL, kk >= 0);
+        if (!hm) continue;
+        if (kk >= 0) tri[ntri + __popc(hm & lt)] = make_int2((int)i, (int)kk);
+        ntri += __popc(hm);
+        merge_chunk(W, A, st, kk >= 0 ? 2 * i + 1 : -1, 2 * kk, lane, flags);
     }
-    finish(W, A, 2 * (int64_t)j + side, lane, flags, seen);
+    finish(W, A, 2 * (int64_t)j, lane, flags, seen);
+    __syncwarp();
+    W = Work{&st.prof, 0, false, gb};
+    merge_base(W, D, A, j, 1, lane, flags);
+    for (int c = 0; c < ntri; c += 32) {
+        int64_t df = -1, dg = -1;
+        if (c + lane < ntri) {
+            const int2 t = tri[c + lane];
+            df = 2 * (int64_t)t.y + 1;
+            dg = 2 * (int64_t)t.x;
+        }
+        merge_chunk(W, A, st, df, dg, lane, flags);
+    }
+    finish(W, A, 2 * (int64_t)j + 1, lane, flags, seen);
 }
 
 __global__ void __launch_bounds__(32 * LEVEL_WARPS) k_bat_level(DevTopo D, BatArgs A, int64_t a0, int64_t a1,
@@ -571,9 +600,7 @@ __global__ void __launch_bounds__(32 * LEVEL_WARPS) k_bat_level(DevTopo D, BatAr
         idx = __shfl_sync(FULL, idx, 0);
         const int64_t e = a0 + (int64_t)idx;
         if (e >= a1) break;
-        const int32_t j = A.arcs[e];
-        customize_side(D, A, j, 0, gb, stages[wib], lane, flags, seen);
-        customize_side(D, A, j, 1, gb, stages[wib], lane, flags, seen);
+        customize_arc(D, A, A.arcs[e], gb, A.tri + slot * A.max_down, stages[wib], lane, flags, seen);
     }
     flags = (int)__reduce_or_sync(FULL, (unsigned)flags);
     if (flags && lane == 0) atomicOr(&A.status->flags, flags);
@@ -591,14 +618,15 @@ struct BatDev {
     const Piece* pool;
 };
 
-// python/cch_nb_battery.py:272-293, comparisons on order keys.
-__device__ __forceinline__ double eval_profile(const BatDev& B, int64_t d, double b) {
+// python/cch_nb_battery.py:272-293, comparisons on order keys: the best
+// value over pieces [t0, n) step dt of direction d at charge b.
+__device__ __forceinline__ double eval_pieces(const BatDev& B, int64_t d, double b, int t0, int dt, long long& kbest) {
     double best = -INFINITY;
-    long long kbest = dkey(-INFINITY);
+    kbest = dkey(-INFINITY);
     const long long kb = dkey(b);
     const int32_t n = B.cnt[d];
     const Piece* p = B.pool + B.pos[d];
-    for (int32_t t = 0; t < n; t++) {
+    for (int32_t t = t0; t < n; t += dt) {
         const Piece f = p[t];
         if (kb >= dkey(f.ime)) {
             double v = b - f.c;
@@ -613,6 +641,22 @@ __device__ __forceinline__ double eval_profile(const BatDev& B, int64_t d, doubl
     return best;
 }
 
+// Warp maximum of (key, value) pairs; every lane gets it.
+__device__ __forceinline__ double warp_max(double v, long long k) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const long long ko = __shfl_xor_sync(FULL, k, o);
+        const double vo = __shfl_xor_sync(FULL, v, o);
+        if (ko > k) {
+            k = ko;
+            v = vo;
+        }
+    }
+    return v;
+}
+
+constexpr int32_t QUERY_WIDE = 8;  // profiles longer than this are evaluated by the whole warp
+
 __global__ void __launch_bounds__(32 * QUERY_WARPS)
     k_bat_query(DevTopo D, BatDev B, const int32_t* __restrict__ s_rank, const int32_t* __restrict__ t_rank,
                 const double* __restrict__ b0, int64_t nq, double* __restrict__ out, unsigned char* scratch,
@@ -625,6 +669,7 @@ __global__ void __launch_bounds__(32 * QUERY_WARPS)
     double* dsoc = soc + Dp;
     int32_t* cs = reinterpret_cast<int32_t*>(dsoc + Dp);
     int32_t* ct = cs + Dp;
+    const long long kneg = dkey(-INFINITY);
     int e = 0;
     for (int64_t q = gw; q < nq; q += nw) {
         const int32_t s = s_rank[q], t = t_rank[q];
@@ -638,16 +683,36 @@ __global__ void __launch_bounds__(32 * QUERY_WARPS)
         __syncwarp();
         if (lane == 0) soc[ds] = b0[q];
         __syncwarp();
+        // upward: s's ancestors in increasing rank; lanes over arcs, long
+        // profiles by the whole warp
         int32_t d = ds;
         for (int32_t x = s; x >= 0; x = D.parent[x], d--) {
             if (lane == 0) cs[d] = x;
             const double bx = soc[d];
-            if (bx > -INFINITY) {
+            if (dkey(bx) > kneg) {
                 const int64_t a1 = D.first[x + 1];
-                for (int64_t a = D.first[x] + lane; a < a1; a += 32) {
-                    const double v = eval_profile(B, 2 * a, bx);
-                    const int32_t hd = D.hdep[a];
-                    if (v > soc[hd]) soc[hd] = v;
+                for (int64_t ab = D.first[x]; ab < a1; ab += 32) {
+                    const int64_t a = ab + lane;
+                    const int32_t n = a < a1 ? B.cnt[2 * a] : 0;
+                    const bool wide = n > QUERY_WIDE;
+                    if (a < a1 && !wide && n > 0) {
+                        long long kv;
+                        const double v = eval_pieces(B, 2 * a, bx, 0, 1, kv);
+                        const int32_t hd = D.hdep[a];
+                        if (kv > dkey(soc[hd])) soc[hd] = v;
+                    }
+                    unsigned wm = __ballot_sync(FULL, wide);
+                    while (wm) {
+                        const int src = __ffs(wm) - 1;
+                        wm &= wm - 1;
+                        const int64_t aa = ab + src;
+                        long long kv;
+                        const double v = warp_max(eval_pieces(B, 2 * aa, bx, lane, 32, kv), kv);
+                        if (lane == 0) {
+                            const int32_t hd = D.hdep[aa];
+                            if (dkey(v) > dkey(soc[hd])) soc[hd] = v;
+                        }
+                    }
                 }
             }
             __syncwarp();
@@ -656,19 +721,44 @@ __global__ void __launch_bounds__(32 * QUERY_WARPS)
         for (int32_t x = t; x >= 0; x = D.parent[x], d--)
             if (lane == 0) ct[d] = x;
         __syncwarp();
+        // downward: t's ancestors in decreasing rank
         for (d = 0; d <= dt; d++) {
             const int32_t x = ct[d];
             double best = (d <= ds && cs[d] == x) ? soc[d] : -INFINITY;
+            long long kb = dkey(best);
             const int64_t a1 = D.first[x + 1];
-            for (int64_t a = D.first[x] + lane; a < a1; a += 32) {
-                const double by = dsoc[D.hdep[a]];
-                if (by > -INFINITY) {
-                    const double v = eval_profile(B, 2 * a + 1, by);
-                    if (v > best) best = v;
+            for (int64_t ab = D.first[x]; ab < a1; ab += 32) {
+                const int64_t a = ab + lane;
+                double by = -INFINITY;
+                int32_t n = 0;
+                if (a < a1) {
+                    by = dsoc[D.hdep[a]];
+                    if (dkey(by) > kneg) n = B.cnt[2 * a + 1];
+                }
+                const bool wide = n > QUERY_WIDE;
+                if (n > 0 && !wide) {
+                    long long kv;
+                    const double v = eval_pieces(B, 2 * a + 1, by, 0, 1, kv);
+                    if (kv > kb) {
+                        best = v;
+                        kb = kv;
+                    }
+                }
+                unsigned wm = __ballot_sync(FULL, wide);
+                while (wm) {
+                    const int src = __ffs(wm) - 1;
+                    wm &= wm - 1;
+                    const double bys = __shfl_sync(FULL, by, src);
+                    long long kv;
+                    const double v = warp_max(eval_pieces(B, 2 * (ab + src) + 1, bys, lane, 32, kv), kv);
+                    const long long kw = dkey(v);
+                    if (lane == 0 && kw > kb) {
+                        best = v;
+                        kb = kw;
+                    }
                 }
             }
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) best = fmax(best, __shfl_xor_sync(FULL, best, o));
+            best = warp_max(best, kb);
             if (lane == 0) dsoc[d] = best;
             __syncwarp();
         }
@@ -694,9 +784,12 @@ int get_plan(nwcch_topology* t, BatPlan** out) {
         return NWCCH_OK;
     }
     const int64_t n = t->d.n, mp = t->d.m_plus;
-    std::vector<int64_t> first(n + 1);
+    std::vector<int64_t> first(n + 1), doff(n + 1);
     std::vector<int32_t> verts(n);
     NWCCH_CUDA_TRY(cudaMemcpy(first.data(), t->d.first, sizeof(int64_t) * (n + 1), cudaMemcpyDeviceToHost));
+    NWCCH_CUDA_TRY(cudaMemcpy(doff.data(), t->d.doff, sizeof(int64_t) * (n + 1), cudaMemcpyDeviceToHost));
+    int64_t max_down = 0;
+    for (int64_t v = 0; v < n; v++) max_down = std::max(max_down, doff[v + 1] - doff[v]);
     if (n) NWCCH_CUDA_TRY(cudaMemcpy(verts.data(), t->level_verts, sizeof(int32_t) * n, cudaMemcpyDeviceToHost));
     std::vector<int32_t> arcs;
     arcs.reserve(mp);
@@ -705,6 +798,7 @@ int get_plan(nwcch_topology* t, BatPlan** out) {
     if ((int64_t)arcs.size() != mp) return NWCCH_ERR_TOPOLOGY;
     auto* P = new (std::nothrow) BatPlan();
     if (!P) return NWCCH_ERR_NOMEM;
+    P->max_down = max_down;
     const size_t bytes = sizeof(int32_t) * std::max<int64_t>(1, mp);
     if (cudaMalloc(&P->arcs, bytes) != cudaSuccess || cudaMalloc(&P->dtail, bytes) != cudaSuccess) {
         cudaFree(P->arcs);
@@ -770,12 +864,13 @@ long long host_key(double x) {
 }
 
 int run_levels(nwcch_topology* t, nwcch_battery* b, const BatPlan* P, const double* w, Rich* gbuf, int32_t gcap,
-               unsigned long long* next, cudaStream_t s, BatStatus* host) {
+               int2* tri, unsigned long long* next, cudaStream_t s, BatStatus* host) {
     NWCCH_CUDA_TRY(cudaMemsetAsync(next, 0, sizeof(unsigned long long) * std::max<int32_t>(1, t->levels), s));
     NWCCH_CUDA_TRY(cudaMemsetAsync(b->status, 0, sizeof(BatStatus), s));
     const double Mpe = b->M + EPS;  // the tests' hi, as the reference computes it
     Cap K{b->M, host_key(b->M), host_key(Mpe)};
-    BatArgs A{w, K, P->arcs, P->dtail, b->cnt, b->pos, b->pool, b->pool_cap, gbuf, gcap, b->status, next};
+    BatArgs A{w,    K,     P->arcs, P->dtail,    b->cnt,    b->pos,   b->pool,
+              b->pool_cap, gbuf, tri, P->max_down, gcap, b->status, next};
     const size_t smem = sizeof(WarpStage) * LEVEL_WARPS;
     NWCCH_CUDA_TRY(cudaFuncSetAttribute(k_bat_level, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     for (int32_t l = 0; l < t->levels; l++) {
@@ -818,14 +913,16 @@ extern "C" int nwcch_battery_customize(nwcch_topology* t, const double* w_dev, d
     const int64_t slots = (int64_t)LEVEL_BLOCKS * LEVEL_WARPS;
     void* gbuf = nullptr;
     void* next = nullptr;
+    void* tri = nullptr;
     BatStatus host{};
     rc = NWCCH_OK;
     if (cudaMallocAsync(&next, sizeof(unsigned long long) * std::max<int32_t>(1, t->levels), s) != cudaSuccess ||
+        cudaMallocAsync(&tri, (size_t)slots * std::max<int64_t>(1, P->max_down) * sizeof(int2), s) != cudaSuccess ||
         cudaMallocAsync(&gbuf, (size_t)slots * gcap * sizeof(Rich), s) != cudaSuccess)
         rc = NWCCH_ERR_NOMEM;
     for (int attempt = 0; rc == NWCCH_OK; attempt++) {
-        rc = run_levels(t, b, P, w_dev, static_cast<Rich*>(gbuf), gcap, static_cast<unsigned long long*>(next), s,
-                        &host);
+        rc = run_levels(t, b, P, w_dev, static_cast<Rich*>(gbuf), gcap, static_cast<int2*>(tri),
+                        static_cast<unsigned long long*>(next), s, &host);
         if (rc || host.flags == 0) break;
         if (attempt >= 12) {
             rc = NWCCH_ERR_CAPACITY;
@@ -851,6 +948,7 @@ extern "C" int nwcch_battery_customize(nwcch_topology* t, const double* w_dev, d
         }
     }
     if (gbuf) cudaFreeAsync(gbuf, s);
+    if (tri) cudaFreeAsync(tri, s);
     if (next) cudaFreeAsync(next, s);
     if (rc == NWCCH_OK && cudaStreamSynchronize(s) != cudaSuccess) rc = NWCCH_ERR_CUDA;
     if (rc) {
