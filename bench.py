@@ -56,6 +56,9 @@ WORKLOADS = {
     "delaunay1m": dict(kind="delaunay", n=1_100_000, queries=10_000, inject=False),
     # CPU configuration: 64x64 grid
     "grid64": dict(kind="grid", n=4096, queries=1_000, inject=False),
+    # battery-constrained profiles in the default run (a quarter of the 264k
+    # case, whose CPU reference takes about a minute per capacity)
+    "delaunay66k": dict(kind="delaunay", n=66_000, queries=1_000, inject=False),
 }
 
 
@@ -379,7 +382,8 @@ def run_battery(args, Wb, factors=(0.25, 1.0, 4.0), queries: int = 10_000):
         M = f * D
         b0 = torch.from_numpy(np.tile([M, M / 2], queries // 2)).cuda()
         times = []
-        for rep in range(1 + max(1, min(args.steps, 3))):
+        reps = max(1, min(args.steps, 2))
+        for rep in range(1 + reps):
             torch.cuda.synchronize()
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record()
@@ -388,7 +392,7 @@ def run_battery(args, Wb, factors=(0.25, 1.0, 4.0), queries: int = 10_000):
             torch.cuda.synchronize()
             if rep:
                 times.append(e0.elapsed_time(e1))
-            if rep < max(1, min(args.steps, 3)):
+            if rep < reps:
                 b.free()
         res = b.query(sq, tq, b0)
         qms = []
@@ -648,6 +652,17 @@ def profile_part(args):
         "queries": lambda i: T.query_batch(m, qs, qt),
         "update": lambda i: T.update(m, idx, w0 + (1 + i % 2)),
     }
+    if args.profile == "battery":
+        # battery profiles at M = D (the median unconstrained route energy,
+        # read off a customization with an unbounded capacity)
+        from nwcch import battery
+        from nwcch import graphs as G
+        wb = battery.energies(T, G.ev_energies(W["g"]))
+        free = battery.customize(T, wb, 1e12)
+        soc = free.query(W["qs"][:400], W["qt"][:400], 5e11).cpu().numpy()
+        free.free()
+        D = float(np.median((5e11 - soc[soc > -np.inf])[:50]))
+        parts["battery"] = lambda i: battery.customize(T, wb, D).free()
     fn = parts[args.profile]
     for i in range(args.warmup):
         fn(i)
@@ -696,12 +711,12 @@ def main():
     ap.add_argument("--serve-workload", default="delaunay1m", choices=list(WORKLOADS) + ["none"])
     ap.add_argument("--serve-loads", default="1e4,1e5,1e6", help="offered query loads (queries/s)")
     ap.add_argument("--serve-seconds", type=float, default=1.0)
-    ap.add_argument("--battery-workload", default="none", choices=list(WORKLOADS) + ["none"],
+    ap.add_argument("--battery-workload", default="delaunay66k", choices=list(WORKLOADS) + ["none"],
                     help="graph of the battery-constrained profiles section")
     ap.add_argument("--no-tune", action="store_true", help="keep the default query schedule")
     ap.add_argument("--plain-steps", type=int, default=-1,
                     help="plain per-level customizations to time (-1: one, none above 5M vertices)")
-    ap.add_argument("--profile", choices=["customize", "potential", "queries", "update"],
+    ap.add_argument("--profile", choices=["customize", "potential", "queries", "update", "battery"],
                     help="run only this part, --steps times after --warmup (for ncu captures); no bench line")
     ap.add_argument("--sn-warp-cap", type=int, default=None, help="customization plan: warp-kernel trapezoid cap")
     ap.add_argument("--sn-warp-min-count", type=int, default=None, help="customization plan: level threshold")

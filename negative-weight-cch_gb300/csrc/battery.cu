@@ -28,17 +28,17 @@
 // subtractions produce doubles, each the reference's operation on the same
 // operands.
 //
-// A profile of up to 32 pieces lives in registers, piece l in lane l: one
-// merge is a vote over the pieces that dominate the candidate, a ballot over
-// the pieces it dominates, a shuffle compaction and an append. Longer
-// profiles continue in the warp's global buffer. The lower triangles of
-// (y, z) are the x of y's downward list whose rows hold z: 32 are tested at
-// a time (binary search of z in x's row); the lanes compose the candidates
-// (single-piece sources, most of them, directly; longer ones 32 at a time)
-// into shared memory, and the merges then run in order. Finished profiles
+// A profile of up to 32 pieces lives in the warp's shared memory, piece l
+// at slot l; longer profiles continue in the warp's global buffer. The lower
+// triangles of (y, z) are the x of y's downward list whose rows hold z: 32
+// are tested at a time (binary search of z in x's row) and kept for the
+// second direction; the lanes compose the candidates (single-piece sources,
+// most of them, directly; longer ones 32 at a time) into shared memory, and
+// each batch is merged as if one at a time (merge_staged). Finished profiles
 // are appended to a pool at atomic offsets; counts and offsets index it. A
 // pool or buffer that overflows is flagged, grown by the host, and the
-// customization runs again.
+// customization runs again; the grown sizes are kept for the topology's
+// next customization.
 //
 // Queries (python/cch_nb_battery.py:296-343): one warp per (s, t, b0). The
 // upward pass over s's ancestors in increasing rank pushes each label through
@@ -901,7 +901,8 @@ extern "C" int nwcch_battery_customize(nwcch_topology* t, const double* w_dev, d
     b->M = capacity;
     b->nd = 2 * t->d.m_plus;
     const size_t nd1 = (size_t)std::max<int64_t>(1, b->nd);
-    b->pool_cap = t->tune.battery_pool > 0 ? t->tune.battery_pool : b->nd + b->nd / 2 + 1024;
+    b->pool_cap = t->tune.battery_pool > 0 ? t->tune.battery_pool
+                                           : std::max<int64_t>(b->nd + b->nd / 2 + 1024, t->battery_pool_hint);
     if (cudaMalloc(&b->cnt, nd1 * sizeof(int32_t)) != cudaSuccess ||
         cudaMalloc(&b->pos, nd1 * sizeof(int64_t)) != cudaSuccess ||
         cudaMalloc(&b->pool, (size_t)b->pool_cap * sizeof(Piece)) != cudaSuccess ||
@@ -957,6 +958,10 @@ extern "C" int nwcch_battery_customize(nwcch_topology* t, const double* w_dev, d
     }
     b->pieces = (int64_t)host.pool_used;
     b->largest = host.largest;
+    // the next customization of this topology starts with buffers that fit
+    // (an overflow costs a whole rerun)
+    t->tune.battery_buffer = std::max<int32_t>(t->tune.battery_buffer, gcap);
+    t->battery_pool_hint = std::max<int64_t>(t->battery_pool_hint, b->pieces + b->pieces / 8);
     *out = b;
     return NWCCH_OK;
 }

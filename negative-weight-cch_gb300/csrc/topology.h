@@ -43,7 +43,7 @@ struct Tuning {
     int64_t update_budget_ns = 0;           // level-sweep budget of an update (0: from the triangle count)
     int64_t update_dense_min = 0;           // updates of at least this many arcs skip the sweep (0: never)
     int64_t battery_pool = 0;               // initial battery piece pool (0: 1.5 pieces a direction)
-    int32_t battery_buffer = 128;           // initial per-warp buffer of a long battery profile (pieces)
+    int32_t battery_buffer = 512;           // initial per-warp buffer of a long battery profile (pieces)
 };
 
 // Device words private to the calls enqueued on one stream: the error word
@@ -80,6 +80,7 @@ struct nwcch_topology {
     void* plans = nullptr;                    // owned by the modules that build plans
     void (*free_plans)(nwcch_topology*) = nullptr;
     void* battery_plan = nullptr;             // battery.cu: arcs in level order
+    int64_t battery_pool_hint = 0;            // pieces of the largest battery customization so far (+1/8)
     void (*free_battery_plan)(nwcch_topology*) = nullptr;
 };
 

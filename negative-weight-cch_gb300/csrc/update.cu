@@ -62,6 +62,9 @@ struct UpdateWorkspace {
     // [8], [9] stop requests by level parity
     unsigned long long* stats = nullptr;
     int blocks32 = 0, blocks64 = 0;
+    int2* tiles = nullptr;            // dense finish: (supernode, 32-column tile) work items
+    int64_t ntiles = 0;
+    const void* tiles_plan = nullptr; // the supernodal plan the tiles were made for
 };
 
 template <class T>
@@ -343,40 +346,70 @@ __global__ void __launch_bounds__(256) k_dense_diff(int64_t m_plus, T* __restric
 //  - every row of S holds all of B, so S is the bottom of a triangle below
 //    every boundary pair (B[p], B[q]): marked if column k+p or k+q of S
 //    has a changed arc. Every lower triangle is one of the two kinds.
-__global__ void __launch_bounds__(256) k_dense_mark(DevTopo D, SnDev S, int64_t nsn, const uint8_t* __restrict__ chg,
-                                                    uint8_t* __restrict__ dq, uint8_t* __restrict__ acol) {
-    extern __shared__ uint8_t anyc[];  // [b]: column of the boundary has a changed arc
-    for (int64_t sn = blockIdx.x; sn < nsn; sn += gridDim.x) {
-        const int32_t s0 = S.s0[sn], k = S.k[sn], b = S.b[sn];
-        const int32_t width = k + b;
-        for (int32_t p = 1 + threadIdx.x; p < k; p += blockDim.x) {
-            uint8_t a = 0;
-            for (int32_t i = 0; i < p && !a; i++) a = chg[D.first[s0 + i] + (p - i - 1)];
-            acol[s0 + p] = a;
+// Two passes over (supernode, 32-column tile) blocks: a lane per column, the
+// block's 8 warps each over an eighth of the rows (coalesced across the
+// tile), combined through shared memory: the column flags first (acol[s0 + j]
+// inside, bflag at the column's last-row arc on the boundary), then the
+// marks, each warp starting from the OR of the row segments above its own.
+constexpr int kMarkWarps = 8;
+
+__global__ void __launch_bounds__(32 * kMarkWarps)
+    k_dense_cols(DevTopo D, SnDev S, const int2* __restrict__ tiles, int64_t ntiles, const uint8_t* __restrict__ chg,
+                 uint8_t* __restrict__ acol, uint8_t* __restrict__ bflag) {
+    __shared__ uint8_t seg[kMarkWarps][32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int64_t it = blockIdx.x; it < ntiles; it += gridDim.x) {
+        const int2 tl = tiles[it];
+        const int32_t s0 = S.s0[tl.x], k = S.k[tl.x], b = S.b[tl.x];
+        const int32_t j = tl.y * 32 + lane;
+        const int32_t rows = j < k + b ? min(j, k) : 0;
+        const int32_t per = (k + kMarkWarps - 1) / kMarkWarps, p0 = w * per, p1 = min(rows, p0 + per);
+        uint8_t r = 0;
+        for (int32_t p = p0; p < p1; p++) r |= chg[D.first[s0 + p] + (j - p - 1)];
+        seg[w][lane] = r;
+        __syncthreads();
+        if (w == 0 && j < k + b) {
+            uint8_t t = 0;
+#pragma unroll
+            for (int i = 0; i < kMarkWarps; i++) t |= seg[i][lane];
+            if (j < k) acol[s0 + j] = t;
+            else bflag[D.first[s0 + k - 1] + (j - k)] = t;
         }
         __syncthreads();
-        int any = 0;
-        for (int32_t j = 1 + threadIdx.x; j < width; j += blockDim.x) {
-            uint8_t r = 0;
-            const int32_t rows = min(j, k);
-            for (int32_t p = 0; p < rows; p++) {
-                const int64_t a = D.first[s0 + p] + (j - p - 1);
-                if (r || (p > 0 && acol[s0 + p])) dq[a] = 1;
-                r |= chg[a];
-            }
-            if (j >= k) {
-                anyc[j - k] = r;
-                any |= r;
-            }
+    }
+}
+
+__global__ void __launch_bounds__(32 * kMarkWarps)
+    k_dense_mark(DevTopo D, SnDev S, const int2* __restrict__ tiles, int64_t ntiles, const uint8_t* __restrict__ chg,
+                 uint8_t* __restrict__ dq, const uint8_t* __restrict__ acol, const uint8_t* __restrict__ bflag) {
+    __shared__ uint8_t seg[kMarkWarps][32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int64_t it = blockIdx.x; it < ntiles; it += gridDim.x) {
+        const int2 tl = tiles[it];
+        const int32_t s0 = S.s0[tl.x], k = S.k[tl.x], b = S.b[tl.x];
+        const int32_t j = tl.y * 32 + lane;
+        const int32_t rows = j < k + b ? min(j, k) : 0;
+        const int32_t per = (k + kMarkWarps - 1) / kMarkWarps, p0 = w * per, p1 = min(rows, p0 + per);
+        uint8_t r = 0;
+        for (int32_t p = p0; p < p1; p++) r |= chg[D.first[s0 + p] + (j - p - 1)];
+        seg[w][lane] = r;
+        __syncthreads();
+        r = 0;
+        for (int i = 0; i < w; i++) r |= seg[i][lane];
+        for (int32_t p = p0; p < p1; p++) {
+            const int64_t a = D.first[s0 + p] + (j - p - 1);
+            if (r || (p > 0 && acol[s0 + p])) dq[a] = 1;
+            r |= chg[a];
         }
-        if (__syncthreads_or(any)) {
-            const int64_t ro = S.rel_off[sn];
-            for (int32_t p = 0; p + 1 < b; p++) {
-                const uint8_t ap = anyc[p];
-                const int64_t row = ro + (int64_t)p * (2 * b - p - 1) / 2 - p - 1;  // + q: pair (p, q)
-                for (int32_t q = p + 1 + threadIdx.x; q < b; q += blockDim.x)
-                    if (ap | anyc[q]) dq[S.rel[row + q]] = 1;
-            }
+        if (j >= k && j < k + b) {
+            // boundary pairs (B[p], B[q]) with q = j - k: marked if either
+            // column of S has a changed arc
+            const int32_t q = j - k;
+            const int64_t last = D.first[s0 + k - 1];
+            const uint8_t aq = bflag[last + q];
+            const int64_t ro = S.rel_off[tl.x];
+            for (int32_t p = w; p < q; p += kMarkWarps)
+                if (aq | bflag[last + p]) dq[S.rel[ro + (int64_t)p * (2 * b - p - 1) / 2 + (q - p - 1)]] = 1;
         }
         __syncthreads();
     }
@@ -417,6 +450,7 @@ __global__ void __launch_bounds__(256) k_update_clean(UpdateWorkspace ws, const 
 
 static void free_workspace(UpdateWorkspace* ws) {
     if (!ws) return;
+    cudaFree(ws->tiles);
     cudaFree(ws->chg);
     cudaFree(ws->dq);
     cudaFree(ws->acol);
@@ -541,12 +575,30 @@ int finish_dense(nwcch_topology* t, UpdateWorkspace* ws, const int32_t* w_dev, T
     int rc = launch_supernodal<T>(t, P, w_dev, up2, dn2, s);
     if (rc) return rc;
     k_dense_diff<T><<<grid_for(mp, 256), 256, 0, s>>>(mp, up_dev, dn_dev, up2, dn2, ws->chg, ws->changed, ws->stats);
-    const size_t smem = (size_t)std::max(1, P->max_b);
-    if (smem > 227 * 1024) return NWCCH_ERR_CAPACITY;
-    if (smem > 48 * 1024)
-        NWCCH_CUDA_TRY(cudaFuncSetAttribute(k_dense_mark, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    const unsigned blocks = (unsigned)std::max<int64_t>(1, std::min<int64_t>(P->nsn, 152 * 8));
-    k_dense_mark<<<blocks, 256, smem, s>>>(t->d, P->dev, P->nsn, ws->chg, ws->dq, ws->acol);
+    // up2 is free after the diff: its first m+ bytes hold the boundary
+    // column flags
+    uint8_t* bflag = static_cast<uint8_t*>(ws->up2);
+    if (ws->tiles_plan != P) {  // (supernode, 32-column tile) list of this plan
+        cudaFree(ws->tiles);
+        ws->tiles = nullptr;
+        ws->tiles_plan = nullptr;
+        std::vector<int32_t> kk(P->nsn), bb(P->nsn);
+        NWCCH_CUDA_TRY(cudaMemcpy(kk.data(), P->dev.k, sizeof(int32_t) * P->nsn, cudaMemcpyDeviceToHost));
+        NWCCH_CUDA_TRY(cudaMemcpy(bb.data(), P->dev.b, sizeof(int32_t) * P->nsn, cudaMemcpyDeviceToHost));
+        std::vector<int2> tl;
+        for (int64_t sn = 0; sn < P->nsn; sn++)
+            for (int32_t c = 0; c * 32 < kk[sn] + bb[sn]; c++) tl.push_back(make_int2((int)sn, c));
+        if (cudaMalloc(&ws->tiles, sizeof(int2) * std::max<size_t>(1, tl.size())) != cudaSuccess)
+            return NWCCH_ERR_NOMEM;
+        if (!tl.empty())
+            NWCCH_CUDA_TRY(cudaMemcpy(ws->tiles, tl.data(), sizeof(int2) * tl.size(), cudaMemcpyHostToDevice));
+        ws->ntiles = (int64_t)tl.size();
+        ws->tiles_plan = P;
+    }
+    const unsigned grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>(ws->ntiles, 152 * 8));
+    k_dense_cols<<<grid, 32 * kMarkWarps, 0, s>>>(t->d, P->dev, ws->tiles, ws->ntiles, ws->chg, ws->acol, bflag);
+    k_dense_mark<<<grid, 32 * kMarkWarps, 0, s>>>(t->d, P->dev, ws->tiles, ws->ntiles, ws->chg, ws->dq, ws->acol,
+                                                  bflag);
     k_dense_count<<<grid_for(mp, 256), 256, 0, s>>>(t->d, L, ws->queued, ws->dq, ws->stats);
     k_update_clean<<<152 * 4, 256, 0, s>>>(*ws, t->d_level_arc_off, mp);
     NWCCH_CUDA_TRY(cudaGetLastError());
