@@ -583,7 +583,7 @@ def run_serving(args, Ws, loads):
         sq, tq = G.random_pairs(top["n"], 512, seed=3)
         rq = tune.tune_queries(T, m0, top["rank"][sq], top["rank"][tq], reps=2, dense_rows=(1, 8, 16),
                                labels=("auto", "shared"))
-        ru = tune.tune_update(T, m0, sizes=(1, 10, 100, 1000), factors=(0.1, 0.25, 0.5, 1.0))
+        ru = tune.tune_update(T, m0, sizes=(1, 10, 100, 1000), factors=(0.1, 0.25, 0.5, 1.0), picks_per_size=3)
         tuned = {"customize": rc["best"], "queries": rq["best"], "update_budget_ns": ru["best"]["budget_ns"],
                  "update_dense_min": ru["best"]["dense_min"]}
         log(f"serving schedules: {tuned}")

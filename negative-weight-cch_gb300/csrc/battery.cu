@@ -656,6 +656,139 @@ __device__ __forceinline__ double warp_max(double v, long long k) {
 }
 
 constexpr int32_t QUERY_WIDE = 8;  // profiles longer than this are evaluated by the whole warp
+constexpr int QUERY_CTA_WARPS = 8;      // the single-query form: a CTA of 8 warps per query
+constexpr int64_t QUERY_CTA_MAX = 304;  // batches up to this size use it
+
+// The same query with a CTA per (s, t, b0), for small batches (latency):
+// the 256 threads split each vertex's arcs, each warp evaluates the long
+// profiles among its own 32 arcs, and the downward maximum is reduced
+// across the warps through shared memory.
+__global__ void __launch_bounds__(32 * QUERY_CTA_WARPS)
+    k_bat_query_cta(DevTopo D, BatDev B, const int32_t* __restrict__ s_rank, const int32_t* __restrict__ t_rank,
+                    const double* __restrict__ b0, int64_t nq, double* __restrict__ out, unsigned char* scratch,
+                    int64_t per_cta, int* err) {
+    __shared__ double red_v[QUERY_CTA_WARPS];
+    __shared__ long long red_k[QUERY_CTA_WARPS];
+    constexpr int NT = 32 * QUERY_CTA_WARPS;
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, tid = threadIdx.x;
+    const int64_t Dp = D.max_depth + 1;
+    double* soc = reinterpret_cast<double*>(scratch + blockIdx.x * per_cta);
+    double* dsoc = soc + Dp;
+    int32_t* cs = reinterpret_cast<int32_t*>(dsoc + Dp);
+    int32_t* ct = cs + Dp;
+    const long long kneg = dkey(-INFINITY);
+    int e = 0;
+    for (int64_t q = blockIdx.x; q < nq; q += gridDim.x) {
+        const int32_t s = s_rank[q], t = t_rank[q];
+        if (s < 0 || s >= D.n || t < 0 || t >= D.n) {
+            if (tid == 0) out[q] = -INFINITY;
+            e |= ERR_ARG;
+            continue;
+        }
+        const int32_t ds = D.depth[s], dt = D.depth[t];
+        for (int32_t d = tid; d <= ds; d += NT) soc[d] = -INFINITY;
+        __syncthreads();
+        if (tid == 0) soc[ds] = b0[q];
+        __syncthreads();
+        int32_t d = ds;
+        for (int32_t x = s; x >= 0; x = D.parent[x], d--) {
+            if (tid == 0) cs[d] = x;
+            const double bx = soc[d];
+            if (dkey(bx) > kneg) {
+                const int64_t a1 = D.first[x + 1];
+                for (int64_t ab = D.first[x] + 32 * wib; ab < a1; ab += NT) {
+                    const int64_t a = ab + lane;
+                    const int32_t n = a < a1 ? B.cnt[2 * a] : 0;
+                    const bool wide = n > QUERY_WIDE;
+                    if (a < a1 && !wide && n > 0) {
+                        long long kv;
+                        const double v = eval_pieces(B, 2 * a, bx, 0, 1, kv);
+                        const int32_t hd = D.hdep[a];
+                        if (kv > dkey(soc[hd])) soc[hd] = v;
+                    }
+                    unsigned wm = __ballot_sync(FULL, wide);
+                    while (wm) {
+                        const int src = __ffs(wm) - 1;
+                        wm &= wm - 1;
+                        const int64_t aa = ab + src;
+                        long long kv;
+                        const double v = warp_max(eval_pieces(B, 2 * aa, bx, lane, 32, kv), kv);
+                        if (lane == 0) {
+                            const int32_t hd = D.hdep[aa];
+                            if (dkey(v) > dkey(soc[hd])) soc[hd] = v;
+                        }
+                    }
+                }
+            }
+            __syncthreads();
+        }
+        d = dt;
+        for (int32_t x = t; x >= 0; x = D.parent[x], d--)
+            if (tid == 0) ct[d] = x;
+        __syncthreads();
+        for (d = 0; d <= dt; d++) {
+            const int32_t x = ct[d];
+            double best = -INFINITY;
+            long long kb = kneg;
+            if (tid == 0 && d <= ds && cs[d] == x) {
+                best = soc[d];
+                kb = dkey(best);
+            }
+            const int64_t a1 = D.first[x + 1];
+            for (int64_t ab = D.first[x] + 32 * wib; ab < a1; ab += NT) {
+                const int64_t a = ab + lane;
+                double by = -INFINITY;
+                int32_t n = 0;
+                if (a < a1) {
+                    by = dsoc[D.hdep[a]];
+                    if (dkey(by) > kneg) n = B.cnt[2 * a + 1];
+                }
+                const bool wide = n > QUERY_WIDE;
+                if (n > 0 && !wide) {
+                    long long kv;
+                    const double v = eval_pieces(B, 2 * a + 1, by, 0, 1, kv);
+                    if (kv > kb) {
+                        best = v;
+                        kb = kv;
+                    }
+                }
+                unsigned wm = __ballot_sync(FULL, wide);
+                while (wm) {
+                    const int src = __ffs(wm) - 1;
+                    wm &= wm - 1;
+                    const double bys = __shfl_sync(FULL, by, src);
+                    long long kv;
+                    const double v = warp_max(eval_pieces(B, 2 * (ab + src) + 1, bys, lane, 32, kv), kv);
+                    const long long kw = dkey(v);
+                    if (lane == 0 && kw > kb) {
+                        best = v;
+                        kb = kw;
+                    }
+                }
+            }
+            best = warp_max(best, kb);
+            if (lane == 0) {
+                red_v[wib] = best;
+                red_k[wib] = dkey(best);
+            }
+            __syncthreads();
+            if (tid == 0) {
+                double bv = red_v[0];
+                long long bk = red_k[0];
+                for (int w2 = 1; w2 < QUERY_CTA_WARPS; w2++)
+                    if (red_k[w2] > bk) {
+                        bk = red_k[w2];
+                        bv = red_v[w2];
+                    }
+                dsoc[d] = bv;
+            }
+            __syncthreads();
+        }
+        if (tid == 0) out[q] = dsoc[dt];
+        __syncthreads();
+    }
+    if (e && tid == 0) atomicOr(err, e);
+}
 
 __global__ void __launch_bounds__(32 * QUERY_WARPS)
     k_bat_query(DevTopo D, BatDev B, const int32_t* __restrict__ s_rank, const int32_t* __restrict__ t_rank,
@@ -1010,15 +1143,21 @@ extern "C" int nwcch_battery_query(nwcch_topology* t, const nwcch_battery* b, co
     if (nq == 0) return NWCCH_OK;
     const cudaStream_t s = (cudaStream_t)stream;
     const int64_t Dp = t->d.max_depth + 1;
-    const int64_t per_warp = (24 * Dp + 64 + 255) & ~255LL;
-    const int64_t warps = std::max<int64_t>(1, std::min<int64_t>(nq, 152 * 16));
-    const int64_t blocks = (warps + QUERY_WARPS - 1) / QUERY_WARPS;
+    const int64_t per_query = (24 * Dp + 64 + 255) & ~255LL;  // labels and chains of one query in flight
+    const BatDev B{b->cnt, b->pos, b->pool};
+    int* err = stream_slot(t, s).err;
     void* scratch = nullptr;
-    NWCCH_CUDA_TRY(cudaMallocAsync(&scratch, (size_t)(blocks * QUERY_WARPS * per_warp), s));
-    k_bat_query<<<(unsigned)blocks, 32 * QUERY_WARPS, 0, s>>>(t->d, BatDev{b->cnt, b->pos, b->pool}, s_rank_dev,
-                                                             t_rank_dev, b0_dev, nq, out_dev,
-                                                             static_cast<unsigned char*>(scratch), per_warp,
-                                                             stream_slot(t, s).err);
+    if (nq <= QUERY_CTA_MAX) {
+        NWCCH_CUDA_TRY(cudaMallocAsync(&scratch, (size_t)(nq * per_query), s));
+        k_bat_query_cta<<<(unsigned)nq, 32 * QUERY_CTA_WARPS, 0, s>>>(
+            t->d, B, s_rank_dev, t_rank_dev, b0_dev, nq, out_dev, static_cast<unsigned char*>(scratch), per_query, err);
+    } else {
+        const int64_t warps = std::min<int64_t>(nq, 152 * 16);
+        const int64_t blocks = (warps + QUERY_WARPS - 1) / QUERY_WARPS;
+        NWCCH_CUDA_TRY(cudaMallocAsync(&scratch, (size_t)(blocks * QUERY_WARPS * per_query), s));
+        k_bat_query<<<(unsigned)blocks, 32 * QUERY_WARPS, 0, s>>>(
+            t->d, B, s_rank_dev, t_rank_dev, b0_dev, nq, out_dev, static_cast<unsigned char*>(scratch), per_query, err);
+    }
     const cudaError_t launch = cudaGetLastError();
     NWCCH_CUDA_TRY(cudaFreeAsync(scratch, s));
     NWCCH_CUDA_TRY(launch);

@@ -13,7 +13,8 @@ the same answers, and leaves the fastest one set on the topology
 * queries: chunks below `dense_rows` rows go row by row instead of the
   32-row (min,+) form; labels in shared memory or in global scratch; the
   32-bit kernel with or without a 64-register cap; a warp or a CTA per query;
-* updates: the time the level sweep may spend before the dense finish.
+* updates: the time the level sweep may spend before the dense finish, and
+  the update size from which the sweep is skipped.
 """
 from __future__ import annotations
 
@@ -193,34 +194,38 @@ def tune_latency(topo: DeviceTopology, metric: Metric, s_rank, t_rank, dense_row
 
 
 def tune_update(topo: DeviceTopology, metric: Metric, sizes=(1, 10, 100), factors=(0.25, 0.5, 1.0, 2.0),
-                seed: int = 0) -> dict:
+                seed: int = 0, picks_per_size: int = 5) -> dict:
     """Times raise-and-restore update pairs of each size under sweep budgets
     of `factors` x the default estimate (about half a full customization),
     and with the dense finish at once; keeps the budget and the size from
     which updates go dense at once (`update_dense_min`) with the least total
-    time over `sizes`. The metric ends as it began."""
+    time over `sizes`. Each size is timed on `picks_per_size` random arc sets
+    and counts with its median pair (one arc can be cheap or reach the top
+    separators). The metric ends as it began."""
     import torch
     rng = np.random.default_rng(seed)
     w0 = metric.w.cpu().numpy().copy()
     default = max(200_000, topo.triangles // 200)
     before = {k: get(topo, k) for k in ("update_budget_ns", "update_dense_min")}
-    picks = {k: rng.choice(topo.m, size=k, replace=False) for k in sizes}
-    raises = {k: w0[picks[k]].astype(np.int64) + 1 + rng.integers(0, 50, k) for k in sizes}
+    picks = {k: [rng.choice(topo.m, size=k, replace=False) for _ in range(picks_per_size)] for k in sizes}
+    raises = {k: [w0[ix].astype(np.int64) + 1 + rng.integers(0, 50, k) for ix in picks[k]] for k in sizes}
 
     def per_size():
         out = {}
         for k in sizes:
-            idx = picks[k]
-            total = 0.0
-            for val in (raises[k], w0[idx]):
-                torch.cuda.synchronize()
-                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-                e0.record()
-                topo.update(metric, idx, val)
-                e1.record()
-                torch.cuda.synchronize()
-                total += e0.elapsed_time(e1)
-            out[k] = total
+            pairs = []
+            for idx, up in zip(picks[k], raises[k]):
+                total = 0.0
+                for val in (up, w0[idx]):
+                    torch.cuda.synchronize()
+                    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                    e0.record()
+                    topo.update(metric, idx, val)
+                    e1.record()
+                    torch.cuda.synchronize()
+                    total += e0.elapsed_time(e1)
+                pairs.append(total)
+            out[k] = statistics.median(pairs)
         return out
 
     trials = []

@@ -84,6 +84,9 @@ def test_battery_against_oracle_delaunay(gpu, oracle, factor):
     got = b.query(top["rank"][s], top["rank"][t], b0).cpu().numpy()
     want = oracle.battery_query_batch(OT, (ocnt, ooff, opieces), top["rank"][s], top["rank"][t], b0)
     assert np.array_equal(got, want)
+    # small batches take the CTA-per-query form: same answers
+    small = b.query(top["rank"][s[:100]], top["rank"][t[:100]], b0[:100]).cpu().numpy()
+    assert np.array_equal(small, want[:100])
     truth = np.array([oracle.battery_label_correcting(g["n"], g["off"], g["tgt"], w, M, int(s[j]),
                                                       float(b0[j]))[t[j]] for j in range(20)])
     assert close(got[:20], truth)
