@@ -150,25 +150,60 @@ __device__ void panel_compute(PanelSmem<V, CT>& sm, int pn, bool hasj, int& e) {
 template <class P, class T, class V, int CT>
 __device__ bool panel_load(PanelSmem<V, CT>& sm, const T* __restrict__ up, const T* __restrict__ dn, int pn,
                            int i0, int j, bool hasj) {
+    // every load of a group is issued before its values are used, so the
+    // group's global latencies overlap instead of adding up
     const int tid = threadIdx.x;
     bool bad = false;
-    for (int t = tid; t < SN_P * SN_P; t += CT) {
-        const int a = t >> 5, c = t & 31;
-        if (a < c && c < pn) {
-            const T u = up[sm.rowb[a] + c - a - 1], d = dn[sm.rowb[a] + c - a - 1];
-            if constexpr (std::is_same<P, FastI32>::value) bad |= !P::in(u) || !P::in(d);
-            sm.Ud[a][c] = P::from(u);
-            sm.Dd[a][c] = P::from(d);
+    constexpr int DI = SN_P * SN_P / CT;  // diagonal entries per thread
+    {
+        T du[DI], dd[DI];
+#pragma unroll
+        for (int q = 0; q < DI; q++) {
+            const int t = tid + q * CT, a = t >> 5, c = t & 31;
+            du[q] = Lim<T>::INF;
+            dd[q] = Lim<T>::INF;
+            if (a < c && c < pn) {
+                du[q] = up[sm.rowb[a] + c - a - 1];
+                dd[q] = dn[sm.rowb[a] + c - a - 1];
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < DI; q++) {
+            const int t = tid + q * CT, a = t >> 5, c = t & 31;
+            if (a < c && c < pn) {
+                if constexpr (std::is_same<P, FastI32>::value) bad |= !P::in(du[q]) || !P::in(dd[q]);
+                sm.Ud[a][c] = P::from(du[q]);
+                sm.Dd[a][c] = P::from(dd[q]);
+            }
         }
     }
-    if (hasj)
-        for (int a = 0; a < pn; a++) {
-            const int64_t idx = sm.rowb[a] + (j - (i0 + a)) - 1;
-            const T u = up[idx], d = dn[idx];
-            if constexpr (std::is_same<P, FastI32>::value) bad |= !P::in(u) || !P::in(d);
-            sm.cU[a][tid] = P::from(u);
-            sm.cD[a][tid] = P::from(d);
+    if (hasj) {
+        constexpr int G = 8;  // column loads in flight per group
+#pragma unroll
+        for (int a0 = 0; a0 < SN_P; a0 += G) {
+            T cu[G], cd[G];
+#pragma unroll
+            for (int q = 0; q < G; q++) {
+                const int a = a0 + q;
+                cu[q] = Lim<T>::INF;
+                cd[q] = Lim<T>::INF;
+                if (a < pn) {
+                    const int64_t idx = sm.rowb[a] + (j - (i0 + a)) - 1;
+                    cu[q] = up[idx];
+                    cd[q] = dn[idx];
+                }
+            }
+#pragma unroll
+            for (int q = 0; q < G; q++) {
+                const int a = a0 + q;
+                if (a < pn) {
+                    if constexpr (std::is_same<P, FastI32>::value) bad |= !P::in(cu[q]) || !P::in(cd[q]);
+                    sm.cU[a][tid] = P::from(cu[q]);
+                    sm.cD[a][tid] = P::from(cd[q]);
+                }
+            }
         }
+    }
     return bad;
 }
 
@@ -326,20 +361,31 @@ __device__ bool tile_product(const DevTopo& D, const TileCtx<T, TILE, MT, OUT>& 
         if (tid < CH) sm.rowb[tid] = tid < nch ? D.first[c.s0 + i0 + tid] : 0;
         __syncthreads();
         bool bad = false;
-        for (int t = tid; t < CH * TILE; t += NT) {
-            const int a = t / TILE, cc = t % TILE;
+        // all of a thread's loads are issued before any is used (their
+        // global latencies overlap), then converted into shared memory
+        constexpr int NL = CH * TILE / NT;
+        static_assert(CH * TILE % NT == 0, "tile loads split evenly");
+        T ad[NL], au[NL], bu[NL], bd[NL];
+#pragma unroll
+        for (int q = 0; q < NL; q++) {
+            const int t = tid + q * NT, a = t / TILE, cc = t % TILE;
             const int ac = c.abase + cc, bc = c.bbase + cc;
             const bool okr = a < nch;
             const int64_t rb = sm.rowb[a] - (i0 + a) - 1;
-            const T ad = (okr && ac < c.alim) ? dn[rb + ac] : Lim<T>::INF;
-            const T au = (okr && ac < c.alim) ? up[rb + ac] : Lim<T>::INF;
-            const T bu = (okr && bc < c.cols) ? up[rb + bc] : Lim<T>::INF;
-            const T bd = (okr && bc < c.cols) ? dn[rb + bc] : Lim<T>::INF;
-            if constexpr (FAST) bad |= !FastI32::in(ad) || !FastI32::in(au) || !FastI32::in(bu) || !FastI32::in(bd);
-            sm.Ad[a][cc] = P::from(ad);
-            sm.Au[a][cc] = P::from(au);
-            sm.Bu[a][cc] = P::from(bu);
-            sm.Bd[a][cc] = P::from(bd);
+            ad[q] = (okr && ac < c.alim) ? dn[rb + ac] : Lim<T>::INF;
+            au[q] = (okr && ac < c.alim) ? up[rb + ac] : Lim<T>::INF;
+            bu[q] = (okr && bc < c.cols) ? up[rb + bc] : Lim<T>::INF;
+            bd[q] = (okr && bc < c.cols) ? dn[rb + bc] : Lim<T>::INF;
+        }
+#pragma unroll
+        for (int q = 0; q < NL; q++) {
+            const int t = tid + q * NT, a = t / TILE, cc = t % TILE;
+            if constexpr (FAST)
+                bad |= !FastI32::in(ad[q]) || !FastI32::in(au[q]) || !FastI32::in(bu[q]) || !FastI32::in(bd[q]);
+            sm.Ad[a][cc] = P::from(ad[q]);
+            sm.Au[a][cc] = P::from(au[q]);
+            sm.Bu[a][cc] = P::from(bu[q]);
+            sm.Bd[a][cc] = P::from(bd[q]);
         }
         if constexpr (FAST) {
             if (__syncthreads_or(bad)) return false;
@@ -456,9 +502,23 @@ __global__ void __launch_bounds__(32 * WARPS) k_sn_warp(DevTopo D, SnDev S, cons
         const int32_t width = k + b;
         const int64_t base = D.first[s0];
         const int32_t total = (int32_t)(D.first[s0 + k] - base);
-        for (int x = lane; x < total; x += 32) {
-            U[x] = up[base + x];
-            Dn[x] = dn[base + x];
+        // staged 4 loads deep per array, so their latencies overlap
+        for (int x0 = 0; x0 < total; x0 += 128) {
+            T vu[4], vd[4];
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const int x = x0 + 32 * q + lane;
+                vu[q] = x < total ? up[base + x] : Lim<T>::INF;
+                vd[q] = x < total ? dn[base + x] : Lim<T>::INF;
+            }
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const int x = x0 + 32 * q + lane;
+                if (x < total) {
+                    U[x] = vu[q];
+                    Dn[x] = vd[q];
+                }
+            }
         }
         __syncwarp();
         auto ro = [&](int i) { return i * (width - 1) - i * (i - 1) / 2; };  // row i's first arc
