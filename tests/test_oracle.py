@@ -164,6 +164,32 @@ def test_query_path_against_reference(oracle):
                 assert sum(wmap[(int(a), int(b))] for a, b in zip(inv[pr][:-1], inv[pr][1:])) == d
 
 
+@pytest.mark.parametrize("seed", [0, 1, 2])
+def test_battery_queries_match_label_correcting(oracle, seed):
+    """On this project's own orders (the topologies the device path runs on),
+    the oracle's battery queries equal the label-correcting search within
+    the reference's tolerance, infeasible exactly when it is."""
+    from nwcch import graphs as G
+    from nwcch import topology as T
+    g = G.delaunay(400, seed=seed)
+    w = G.ev_energies(g)
+    top = T.build_topology(g)
+    OT = oracle.Topo.from_dict(top)
+    rng = np.random.default_rng(seed)
+    for M in (150.0, 600.0, 2400.0):
+        prof = oracle.battery_customize(OT, w, M)
+        s = rng.integers(g["n"], size=25)
+        t = rng.integers(g["n"], size=25)
+        b0 = rng.uniform(0, M, size=25)
+        got = oracle.battery_query_batch(OT, prof, top["rank"][s], top["rank"][t], b0)
+        for j in range(25):
+            want = oracle.battery_label_correcting(g["n"], g["off"], g["tgt"], w, M, int(s[j]), float(b0[j]))[t[j]]
+            if want == -np.inf:
+                assert got[j] == -np.inf
+            else:
+                assert abs(got[j] - want) <= 1e-6 * max(1.0, abs(want))
+
+
 def test_battery_against_reference(oracle):
     """python/cch_nb_battery.py: the oracle's profiles are the reference's
     piece for piece (same float64 operations, same merge order), its queries
