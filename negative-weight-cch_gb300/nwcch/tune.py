@@ -200,8 +200,10 @@ def tune_update(topo: DeviceTopology, metric: Metric, sizes=(1, 10, 100), factor
     and with the dense finish at once; keeps the budget and the size from
     which updates go dense at once (`update_dense_min`) with the least total
     time over `sizes`. Each size is timed on `picks_per_size` random arc sets
-    and counts with its median pair (one arc can be cheap or reach the top
-    separators). The metric ends as it began."""
+    and counts with its mean pair, the expected cost: a single arc's update
+    is either local (a fraction of a millisecond on the sweep) or reaches
+    the top separators (the sweep's budget, then the dense finish), and the
+    mix decides. The metric ends as it began."""
     import torch
     rng = np.random.default_rng(seed)
     w0 = metric.w.cpu().numpy().copy()
@@ -225,7 +227,7 @@ def tune_update(topo: DeviceTopology, metric: Metric, sizes=(1, 10, 100), factor
                     torch.cuda.synchronize()
                     total += e0.elapsed_time(e1)
                 pairs.append(total)
-            out[k] = statistics.median(pairs)
+            out[k] = statistics.fmean(pairs)
         return out
 
     trials = []
