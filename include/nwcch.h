@@ -349,8 +349,9 @@ int nwcch_battery_info(const nwcch_battery* b, int64_t* pieces, int32_t* largest
  * (counts and offsets only). */
 int nwcch_battery_export(const nwcch_battery* b, int32_t* cnt, int64_t* off, double* pieces);
 /* Replaces battery_query (python/cch_nb_battery.py:296-343) for a batch:
- * best charge at t leaving s with charge b0 (-inf if infeasible), one warp
- * per query. s/t int32 rank ids, b0_dev/out_dev float64[nq]. */
+ * best charge at t leaving s with charge b0 (-inf if infeasible); a CTA per
+ * query for batches of up to 304, else a warp per query. s/t int32 rank
+ * ids, b0_dev/out_dev float64[nq]. Synchronous (reads the error word). */
 int nwcch_battery_query(nwcch_topology* t, const nwcch_battery* b, const int32_t* s_rank_dev,
                         const int32_t* t_rank_dev, const double* b0_dev, int64_t nq, double* out_dev,
                         void* stream);

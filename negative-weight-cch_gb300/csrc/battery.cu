@@ -40,13 +40,15 @@
 // customization runs again; the grown sizes are kept for the topology's
 // next customization.
 //
-// Queries (python/cch_nb_battery.py:296-343): one warp per (s, t, b0). The
-// upward pass over s's ancestors in increasing rank pushes each label through
-// the up profiles of the vertex's arcs (lanes over arcs; the heads of a row
-// are distinct); the downward pass over t's ancestors in decreasing rank
-// takes the warp maximum of the down profiles applied to the labels above.
-// Labels are indexed by depth. Maxima do not depend on the order, so the
-// answers equal the reference's exactly on the same profiles.
+// Queries (python/cch_nb_battery.py:296-343): one warp per (s, t, b0), or a
+// CTA of 8 warps for small batches. The upward pass over s's ancestors in
+// increasing rank pushes each label through the up profiles of the vertex's
+// arcs (threads over arcs; the heads of a row are distinct; profiles longer
+// than 8 pieces evaluated by a whole warp); the downward pass over t's
+// ancestors in decreasing rank takes the maximum of the down profiles
+// applied to the labels above. Labels are indexed by depth. Maxima (on order
+// keys) do not depend on the order, so the answers equal the reference's
+// exactly on the same profiles.
 
 #include <algorithm>
 #include <cmath>
