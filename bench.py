@@ -288,6 +288,24 @@ def run_ours(args, W, world):
     torch.cuda.synchronize()
     plain_q_ms = e0.elapsed_time(e1)
     assert torch.equal(ref_d, plain_d), "batched and plain queries differ"
+    # the same batch as one captured CUDA graph, replayed
+    graph_q = None
+    try:
+        qg = T.query_graph(good, int(qs.numel()))
+        gms = []
+        for _ in range(3):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            gd = qg.run(qs, qt)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            gms.append(e0.elapsed_time(e1))
+        assert torch.equal(gd, ref_d), "graph-replayed and direct queries differ"
+        graph_q = {"ms": round(statistics.median(gms), 4),
+                   "queries_per_s": round(qs.numel() / (statistics.median(gms) / 1000), 1)}
+        del qg
+    except Exception as exc:  # reported, not fatal: the direct form is the measured one
+        graph_q = {"error": f"{type(exc).__name__}: {exc}"[:200]}
     # end to end through the public API: weights from pinned host memory,
     # customization, scan, count read back
     e2e_ms = []
@@ -320,7 +338,7 @@ def run_ours(args, W, world):
         pot_ms.append(e0.elapsed_time(e1))
     good_host = good.to_numpy()
     return dict(T=T, tuned=tuned, cust_tuned=cust_tuned, cust_ms=cust_ms, q_ms=q_ms, wall=wall, plain_ms=plain_ms, plain_equal=same,
-                e2e_ms=e2e_ms,
+                e2e_ms=e2e_ms, graph_q=graph_q,
                 plain_q_ms=plain_q_ms, lat_dist=lat_dist, pot_ms=pot_ms, pot=pot.cpu().numpy(), good_host=good_host,
                 lat_us=lat, clocks=clocks.summary(), neg=neg_k, saturated=bool(sat))
 
@@ -807,6 +825,7 @@ def main():
         "query_schedule": R["tuned"],
         "customize_schedule": R["cust_tuned"],
         "plain_queries_per_s": round(nq / (R["plain_q_ms"] / 1000) * world, 1),
+        "query_batch_graph": R["graph_q"],
         "query_latency_us": {"p50": round(lat[len(lat) // 2], 2), "p99": round(lat[max(0, int(len(lat) * 0.99) - 1)], 2),
                              "mode": "one query per call, host-timed",
                              "cpu_oracle_us_per_query": round(cq["ms_per_query"] * 1000, 2),

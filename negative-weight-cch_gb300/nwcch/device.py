@@ -358,6 +358,12 @@ class DeviceTopology:
                    out.data_ptr(), _stream(torch)), "query_batch")
         return out
 
+    def query_graph(self, m: Metric, size: int) -> "QueryGraph":
+        """A captured CUDA graph of one batch of `size` queries on metric m
+        (int32 storage): its launches are recorded once and replayed for
+        every batch copied into its input buffers."""
+        return QueryGraph(self, m, size)
+
     def query_paths(self, m: Metric, s_rank, t_rank, cap: int = 0):
         """Distances (int64 tensor) and shortest paths (python/cch.py:406-507)
         as (dist, off, path): path[off[i]:off[i+1]] are the ranks of pair i's
@@ -396,6 +402,46 @@ class DeviceTopology:
         if _status(fn(self.handle, m.up.data_ptr(), m.dn.data_ptr(), out.data_ptr(), _stream(torch)), "potential"):
             warnings.warn("potential saturated: some sums left the int64 range", SaturationWarning, stacklevel=2)
         return out[:self.n]
+
+
+class QueryGraph:
+    """Batches of a fixed size as one CUDA graph replay: the batched query's
+    launches (range check, 32-bit and wide kernels) captured on a side stream
+    over fixed input and output buffers. run() copies a batch in (device
+    copies on the current stream), replays, and returns the output buffer
+    (int64 distances, INT64_MAX = unreachable); the answers are those of
+    query_batch on the same pairs."""
+
+    def __init__(self, topo: DeviceTopology, m: Metric, size: int):
+        torch = topo._torch
+        if m.storage != "int32":
+            raise ValueError("the captured query reads int32 storage")
+        if size < 1:
+            raise ValueError("size must be positive")
+        self.topo, self.metric, self.size = topo, m, int(size)
+        self.s = torch.zeros(self.size, dtype=torch.int32, device="cuda")
+        self.t = torch.zeros(self.size, dtype=torch.int32, device="cuda")
+        self.out = torch.empty(self.size, dtype=torch.int64, device="cuda")
+        # warm-up outside the capture: plans, kernel attributes, scratch pools
+        topo.query_batch(m, self.s, self.t, out=self.out, sync=False)
+        torch.cuda.synchronize()
+        self.graph = torch.cuda.CUDAGraph()
+        side = torch.cuda.Stream()
+        with torch.cuda.stream(side):
+            with torch.cuda.graph(self.graph, stream=side):
+                topo.query_batch(m, self.s, self.t, out=self.out, sync=False)
+        torch.cuda.synchronize()
+
+    def run(self, s_rank, t_rank):
+        torch = self.topo._torch
+        s = torch.as_tensor(s_rank).to(device="cuda", dtype=torch.int32)
+        t = torch.as_tensor(t_rank).to(device="cuda", dtype=torch.int32)
+        if s.numel() != self.size or t.numel() != self.size:
+            raise ValueError(f"batches of this graph hold {self.size} queries")
+        self.s.copy_(s)
+        self.t.copy_(t)
+        self.graph.replay()
+        return self.out
 
 
 def distances_to_float(d) -> np.ndarray:

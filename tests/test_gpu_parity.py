@@ -370,6 +370,25 @@ def test_potential_against_oracle(gpu, oracle, kind, n):
 
 
 @pytest.mark.parametrize("kind,n", [("delaunay", 30_000), ("road", 60_000)])
+def test_query_graph_replays(gpu, oracle, kind, n):
+    """Batches replayed from one captured CUDA graph give the oracle's
+    distances, batch after batch (inputs copied into the graph's buffers)."""
+    from nwcch import graphs as G
+    from nwcch.device import DeviceTopology
+    g, top = _seeded(kind, n, seed=21)
+    T = DeviceTopology.from_dict(top)
+    OT = oracle.Topo.from_dict(top)
+    oup, odn = oracle.customize(OT, g["w"])
+    m = T.customize(g["w"], "int32")
+    qg = T.query_graph(m, 2000)
+    for seed in (1, 2, 3):
+        s, t = G.random_pairs(g["n"], 2000, seed=seed)
+        s, t = top["rank"][s], top["rank"][t]
+        d = qg.run(s, t).cpu().numpy()
+        assert np.array_equal(d, oracle.query_batch(OT, oup, odn, s, t))
+
+
+@pytest.mark.parametrize("kind,n", [("delaunay", 30_000), ("road", 60_000)])
 def test_autotuner_keeps_answers(gpu, oracle, kind, n):
     """Every query schedule the autotuner tries gives the same answers (it
     asserts so), the chosen one equals the oracle, and an update budget is
