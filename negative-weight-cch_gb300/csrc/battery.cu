@@ -926,6 +926,13 @@ int get_plan(nwcch_topology* t, BatPlan** out) {
     int64_t max_down = 0;
     for (int64_t v = 0; v < n; v++) max_down = std::max(max_down, doff[v + 1] - doff[v]);
     if (n) NWCCH_CUDA_TRY(cudaMemcpy(verts.data(), t->level_verts, sizeof(int32_t) * n, cudaMemcpyDeviceToHost));
+    // within a level, the arcs of the tails with the longest downward lists
+    // (the most lower triangles to search) first: the warps fetch arcs in
+    // this order, so the longest candidate streams start early instead of
+    // finishing the level alone
+    for (int32_t l = 0; l < t->levels; l++)
+        std::stable_sort(verts.begin() + t->level_off[l], verts.begin() + t->level_off[l + 1],
+                         [&](int32_t a, int32_t b) { return doff[a + 1] - doff[a] > doff[b + 1] - doff[b]; });
     std::vector<int32_t> arcs;
     arcs.reserve(mp);
     for (int64_t p = 0; p < n; p++)
