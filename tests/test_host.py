@@ -124,6 +124,96 @@ def test_battery_reference_layout_and_histogram():
             assert h[2] == np.count_nonzero((cnt >= 2) & (cnt <= 5)) and h[7] == cnt.max()
 
 
+def test_double_order_key():
+    """The integer order key the battery kernels compare doubles with
+    (negative values: minus their magnitude bits; others: their bits) orders
+    like IEEE comparison on every non-NaN value, -0 equal to +0."""
+    rng = np.random.default_rng(4)
+    vals = np.concatenate([rng.normal(0, 1e3, 4000), rng.normal(0, 1e-9, 1000),
+                           np.array([0.0, -0.0, np.inf, -np.inf, 1e-308, -1e-308, 5e-324, -5e-324,
+                                     1.7976931348623157e308, -1.7976931348623157e308])])
+    bits = vals.view(np.int64)
+    keys = np.where(bits < 0, -(bits & np.int64(0x7FFFFFFFFFFFFFFF)), bits)
+    i, j = rng.integers(vals.size, size=(2, 200_000))
+    assert np.array_equal(keys[i] < keys[j], vals[i] < vals[j])
+    assert np.array_equal(keys[i] == keys[j], vals[i] == vals[j])
+
+
+def _dominates(f, g, M, eps=1e-9):
+    # python/cch_nb_battery.py:16-44
+    fi, fc, fo = f
+    gi, gc, go = g
+    if fi > gi + eps:
+        return False
+    lo, hi = gi - eps, M + eps
+    for b in (gi, M, fo + fc, go + gc):
+        if lo <= b <= hi:
+            if b < fi - eps:
+                return False
+            vf = min(fo, b - fc) if fo < b - fc else b - fc
+            vg = min(go, b - gc) if go < b - gc else b - gc
+            if vf < vg - eps:
+                return False
+    return True
+
+
+def _merge_one(P, h, M):
+    # python/cch_nb_battery.py:186-254, storage aside
+    if any(_dominates(g, h, M) for g in P):
+        return P
+    return [g for g in P if not _dominates(h, g, M)] + [h]
+
+
+def _merge_batch(P, cands, M):
+    """The device's batch merge (csrc/battery.cu merge_staged), step by step:
+    each candidate's first dominator in P scanning from the newest piece,
+    then the in-order resolution with removal sets, then the compaction."""
+    n = len(P)
+    gj = []
+    for h in cands:
+        g = -1
+        for k in range(n - 1, -1, -1):
+            if _dominates(P[k], h, M):
+                g = k
+                break
+        gj.append(g)
+    removed, ins = set(), []
+    for j, h in enumerate(cands):
+        g = gj[j]
+        if g >= 0 and g not in removed:
+            continue
+        d = g >= 0 and any(_dominates(P[k], h, M) for k in range(n) if k not in removed)
+        d = d or any(_dominates(cands[i], h, M) for i in ins)
+        if d:
+            continue
+        removed |= {k for k in range(n) if k not in removed and _dominates(h, P[k], M)}
+        ins = [i for i in ins if not _dominates(h, cands[i], M)] + [j]
+    return [P[k] for k in range(n) if k not in removed] + [cands[i] for i in ins]
+
+
+def test_battery_batch_merge_equals_one_at_a_time():
+    """The batch merge the battery kernel runs on 32 staged candidates gives
+    the one-at-a-time merge's profile, also where the 1e-9 tolerance makes
+    dominance non-transitive (pieces a fraction of the tolerance apart)."""
+    rng = np.random.default_rng(12)
+    M = 50.0
+    jit = np.array([0.0, 0.4e-9, -0.4e-9, 0.9e-9, -0.9e-9, 1.6e-9])
+    for _ in range(300):
+        def piece():
+            i = float(rng.integers(0, 6)) + float(rng.choice(jit))
+            c = float(rng.integers(-3, 8)) + float(rng.choice(jit))
+            o = min(M, float(rng.integers(5, 40)) + float(rng.choice(jit)))
+            return (max(0.0, i), c, o)
+        P = []
+        for _ in range(int(rng.integers(0, 12))):
+            P = _merge_one(P, piece(), M)
+        cands = [piece() for _ in range(int(rng.integers(1, 33)))]
+        want = P
+        for h in cands:
+            want = _merge_one(want, h, M)
+        assert _merge_batch(P, cands, M) == want
+
+
 def test_ev_energies_are_conservative(oracle):
     """The EV energies of a generated graph: steep descents are negative, and
     no cycle gains charge (label correcting from a vertex converges to a
