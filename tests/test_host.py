@@ -214,6 +214,97 @@ def test_battery_batch_merge_equals_one_at_a_time():
         assert _merge_batch(P, cands, M) == want
 
 
+def _key(x):
+    b = int(np.array([x], np.float64).view(np.int64)[0])
+    return -(b & 0x7FFFFFFFFFFFFFFF) if b < 0 else b
+
+
+def _derive(p, M, eps=1e-9):
+    """csrc/battery.cu derive(): the per-piece values of the dominance test."""
+    i, c, o = p
+    oc = o + c
+
+    def mref(a, x):
+        return a if _key(a) < _key(x) else x
+    vM = mref(o, M - c)
+    v3 = mref(o, oc - c)
+    r = dict(i=i, c=c, o=o, oc=oc, ki=_key(i), kipe=_key(i + eps), kime=_key(i - eps), ko=_key(o), koc=_key(oc),
+             kv0m=_key(mref(o, i - c) - eps), kvM=_key(vM), kvMm=_key(vM - eps), kom=_key(o - eps), kv3=_key(v3),
+             kv3m=_key(v3 - eps))
+    kM, kMpe = _key(M), _key(M + eps)
+    r.update(R0=r["ki"] <= kMpe, R1=r["kime"] <= kM, R2=r["koc"] <= kMpe,
+             R3=r["kime"] <= r["koc"] and r["koc"] <= kMpe, MLT=kM < r["kime"], OCLT=r["koc"] < r["kime"])
+    return r
+
+
+def _dominates_keys(F, G, eps=1e-9):
+    """csrc/battery.cu dominates(): keys, precomputed values, skipped
+    subtractions."""
+    if F["ki"] > G["kipe"]:
+        return False
+    if G["R0"]:
+        if G["ki"] < F["kime"] or F["ko"] < G["kv0m"] or _key(G["i"] - F["c"]) < G["kv0m"]:
+            return False
+    if G["R1"] and (F["MLT"] or F["kvM"] < G["kvMm"]):
+        return False
+    if F["R2"] and G["kime"] <= F["koc"]:
+        if F["OCLT"]:
+            return False
+        if F["kv3"] < G["kom"]:
+            y = F["oc"] - G["c"]
+            vg = G["o"] if G["ko"] < _key(y) else y
+            if F["kv3"] < _key(vg - eps):
+                return False
+    if G["R3"]:
+        if G["koc"] < F["kime"] or F["ko"] < G["kv3m"] or _key(G["oc"] - F["c"]) < G["kv3m"]:
+            return False
+    return True
+
+
+def test_battery_dominance_restatement():
+    """The device's dominance test (order keys, per-piece values, skipped
+    subtractions) answers as the reference's on random pieces, near-ties of
+    a fraction of the tolerance and signed zeros included."""
+    rng = np.random.default_rng(8)
+    jit = [0.0, 0.3e-9, -0.3e-9, 1e-9, -1e-9, 2.2e-9]
+    for M in (7.0, 40.0, 1e3):
+        for _ in range(4000):
+            def piece():
+                i = abs(float(rng.integers(0, 9)) + float(rng.choice(jit)))
+                c = float(rng.integers(-6, 10)) + float(rng.choice(jit))
+                o = min(M, float(rng.integers(-2, 30)) + float(rng.choice(jit)))
+                return (i, -0.0 if c == 0 and rng.random() < 0.5 else c, o)
+            f, g = piece(), piece()
+            assert _dominates_keys(_derive(f, M), _derive(g, M)) == _dominates(f, g, M), (f, g, M)
+            # compose (python/cch_nb_battery.py:159-173) on keys, bit for bit
+            want = None
+            if not f[2] < g[0] - 1e-9:
+                hi = f[0] if f[0] > g[0] + f[1] else g[0] + f[1]
+                if not hi > M + 1e-9:
+                    hc = f[1] + g[1]
+                    ho = g[2]
+                    if f[2] - g[1] < ho:
+                        ho = f[2] - g[1]
+                    if M - hc < ho:
+                        ho = M - hc
+                    want = (hi, hc, ho)
+            got = None
+            if not _key(f[2]) < _key(g[0] - 1e-9):
+                s = g[0] + f[1]
+                hi = f[0] if _key(f[0]) > _key(s) else s
+                if not _key(hi) > _key(M + 1e-9):
+                    hc = f[1] + g[1]
+                    ho = g[2]
+                    if _key(f[2] - g[1]) < _key(ho):
+                        ho = f[2] - g[1]
+                    if _key(M - hc) < _key(ho):
+                        ho = M - hc
+                    got = (hi, hc, ho)
+            assert (got is None) == (want is None)
+            if got is not None:
+                assert np.array(got).view(np.int64).tolist() == np.array(want).view(np.int64).tolist()
+
+
 def test_ev_energies_are_conservative(oracle):
     """The EV energies of a generated graph: steep descents are negative, and
     no cycle gains charge (label correcting from a vertex converges to a
