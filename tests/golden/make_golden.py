@@ -36,11 +36,16 @@ Fixtures (np.savez_compressed):
 * paths.npz       - the reference's shortest paths, CCH.query_path
   (python/cch.py:406-507), for the 50 query pairs of every family.npz graph:
   distance and vertex list (original ids), the reference's choice among
-  equal-length paths.
+  equal-length paths;
+* battery.npz     - python/cch_nb_battery.py (un-jitted) on the graphs of
+  test_cch_battery.py with the reference's order: profiles for three
+  capacities and 30 queries each (battery_query and battery_reference);
+* battery_long.npz - the same on a 6,000-point Delaunay graph with steep
+  terrain and this project's order, where profiles outgrow 32 pieces.
 
 `--only NAME[,NAME]` regenerates some fixtures (techniques, family, grid64,
-delaunay_negcycle, potential, paths); potential and paths read family.npz
-(potential also grid64.npz).
+delaunay_negcycle, potential, paths, battery, battery_long); potential and
+paths read family.npz (potential also grid64.npz).
 """
 from __future__ import annotations
 
@@ -495,6 +500,43 @@ def make_battery(R):
     print(f"battery.npz: {len(cases)} graphs x 3 capacities")
 
 
+def make_battery_long(R):
+    """battery_long.npz: python/cch_nb_battery.py, run un-jitted, on a graph
+    whose profiles outgrow 32 pieces (the device keeps those in global
+    memory): a 6,000-point Delaunay graph with steep terrain (this project's
+    generator, heights in [-3000, 3000], EV energies) and this project's
+    order; capacity 3000: the reference's profiles and 20 queries answered by
+    battery_query and by battery_reference."""
+    from nwcch import graphs as G
+    from nwcch import topology as T
+    nbb = importlib.import_module("cch_nb_battery")
+    g = G.delaunay(6000, seed=5, hmax=3000)
+    w = G.ev_energies(g)
+    top = T.build_topology(g)
+    first, head = np.asarray(top["first"], np.int64), np.asarray(top["head"], np.int64)
+    parent, rank = np.asarray(top["parent"], np.int64), np.asarray(top["rank"], np.int64)
+    e_arc, e_up = np.asarray(top["e_arc"], np.int64), np.asarray(top["e_up"]).astype(np.bool_)
+    M = 3000.0
+    prof = nbb.battery_customize(g["n"], first, head, e_arc, e_up, w, M)
+    cnt, poff, pieces = canonical_profiles(*prof)
+    rng = random.Random(17)
+    n = int(g["n"])
+    qs = np.array([rng.randrange(n) for _ in range(20)], np.int64)
+    qt = np.array([rng.randrange(n) for _ in range(20)], np.int64)
+    b0 = np.array([rng.uniform(0, M) for _ in range(20)], np.float64)
+    soc, dsoc, mark = np.full(n, -np.inf), np.full(n, -np.inf), np.zeros(n, np.int64)
+    ans, truth = [], []
+    for q, (s, t, b) in enumerate(zip(qs, qt, b0)):
+        ans.append(nbb.battery_query(rank[s], rank[t], b, first, head, parent, *prof, soc, dsoc, mark, q + 1))
+        truth.append(nbb.battery_reference(n, g["off"], g["tgt"], w, M, s, b)[t])
+    np.savez_compressed(HERE / "battery_long.npz", n=np.int64(n), off=g["off"], tgt=g["tgt"], w=w, rank=rank,
+                        first=first, head=head.astype(np.int32), parent=parent, e_arc=e_arc,
+                        e_up=e_up.astype(np.int8), M=np.float64(M), cnt=cnt, poff=poff, pieces=pieces, qs=qs, qt=qt,
+                        b0=b0, ans=np.array(ans, np.float64), truth=np.array(truth, np.float64))
+    print(f"battery_long.npz: {int(poff[-1])} pieces, largest profile {int(cnt.max())}, "
+          f"{int((cnt > 32).sum())} directions above 32 pieces")
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default="/root/reference")
@@ -503,7 +545,7 @@ def main():
     R = import_reference(Path(args.reference))
     makers = dict(techniques=make_techniques, family=make_family, grid64=make_grid64,
                   delaunay_negcycle=make_delaunay_negcycle, potential=make_potential, paths=make_paths,
-                  battery=make_battery)
+                  battery=make_battery, battery_long=make_battery_long)
     only = [s for s in args.only.split(",") if s] or list(makers)
     for name in only:
         makers[name](R)

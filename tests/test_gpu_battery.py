@@ -44,6 +44,20 @@ def test_battery_golden(gpu):
             assert close(got, c["truth"])
 
 
+def test_battery_golden_long_profiles(gpu):
+    """battery_long.npz: profiles of up to 72 pieces, built partly in the
+    warps' global buffers, equal to the reference's piece for piece."""
+    from conftest import load_golden
+    from nwcch import battery
+    z = load_golden("battery_long.npz")
+    T = dev_topo(z)
+    b = battery.customize(T, z["w"], float(z["M"]))
+    cnt, off, pieces = b.export()
+    assert np.array_equal(cnt, z["cnt"]) and np.array_equal(off, z["poff"]) and np.array_equal(pieces, z["pieces"])
+    got = b.query(z["rank"][z["qs"]], z["rank"][z["qt"]], z["b0"]).cpu().numpy()
+    assert np.array_equal(got, z["ans"])
+
+
 @functools.lru_cache(maxsize=None)
 def _ev_case(n: int):
     import oracle as orc

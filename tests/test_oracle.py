@@ -164,6 +164,21 @@ def test_query_path_against_reference(oracle):
                 assert sum(wmap[(int(a), int(b))] for a, b in zip(inv[pr][:-1], inv[pr][1:])) == d
 
 
+def test_battery_long_profiles_against_reference(oracle):
+    """battery_long.npz: profiles of up to 72 pieces (the reference's, run
+    un-jitted) equal the oracle's piece for piece; answers equal too."""
+    z = load_golden("battery_long.npz")
+    T = oracle.Topo(int(z["n"]), z["first"], z["head"], z["parent"], z["e_arc"], z["e_up"])
+    cnt, off, pieces = oracle.battery_customize(T, z["w"], float(z["M"]))
+    assert int(cnt.max()) > 32
+    assert np.array_equal(cnt, z["cnt"]) and np.array_equal(off, z["poff"]) and np.array_equal(pieces, z["pieces"])
+    got = oracle.battery_query_batch(T, (cnt, off, pieces), z["rank"][z["qs"]], z["rank"][z["qt"]], z["b0"])
+    assert np.array_equal(got, z["ans"])
+    fin = z["truth"] > -np.inf
+    assert np.array_equal(got == -np.inf, ~fin)
+    assert np.all(np.abs(got[fin] - z["truth"][fin]) <= 1e-6 * np.maximum(1.0, np.abs(z["truth"][fin])))
+
+
 @pytest.mark.parametrize("seed", [0, 1, 2])
 def test_battery_queries_match_label_correcting(oracle, seed):
     """On this project's own orders (the topologies the device path runs on),
