@@ -331,3 +331,22 @@ def test_topology_create_rejects_bad_input_without_gpu(built_lib):
     rc = built_lib.nwcch_topology_create(2, _lib.ptr(first), _lib.ptr(head), _lib.ptr(parent), 0, _lib.ptr(e_arc),
                                          _lib.ptr(e_up), C.byref(h))
     assert rc == -4  # NWCCH_ERR_TOPOLOGY
+
+
+def test_battery_entry_points_reject_null_handles_without_gpu(built_lib):
+    """The battery C ABI checks its handles before any device work."""
+    import ctypes as C
+    L = built_lib
+    L.nwcch_battery_customize.argtypes = [C.c_void_p, C.c_void_p, C.c_double, C.c_void_p,
+                                          C.POINTER(C.c_void_p)]
+    L.nwcch_battery_info.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+    L.nwcch_battery_export.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+    L.nwcch_battery_query.argtypes = [C.c_void_p] * 5 + [C.c_int64, C.c_void_p, C.c_void_p]
+    L.nwcch_battery_free.argtypes = [C.c_void_p]
+    L.nwcch_battery_free.restype = None
+    out = C.c_void_p()
+    assert L.nwcch_battery_customize(None, None, 1.0, None, C.byref(out)) == -1
+    assert L.nwcch_battery_info(None, None, None) == -1
+    assert L.nwcch_battery_export(None, None, None, None) == -1
+    assert L.nwcch_battery_query(None, None, None, None, None, 0, None, None) == -1
+    L.nwcch_battery_free(None)  # no-op
