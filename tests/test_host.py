@@ -336,7 +336,7 @@ def test_topology_create_rejects_bad_input_without_gpu(built_lib):
 def test_battery_entry_points_reject_null_handles_without_gpu(built_lib):
     """The battery C ABI checks its handles before any device work."""
     import ctypes as C
-    L = built_lib
+    L = C.CDLL(built_lib._name)  # own function objects: the package's signatures stay as registered
     L.nwcch_battery_customize.argtypes = [C.c_void_p, C.c_void_p, C.c_double, C.c_void_p,
                                           C.POINTER(C.c_void_p)]
     L.nwcch_battery_info.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
