@@ -288,7 +288,7 @@ __device__ __noinline__ void merge(Work& W, const Rich& h, int32_t gcap, int lan
             keep = !dominates(h, g);
         }
         const unsigned km = __ballot_sync(FULL, keep);
-        // writes land at or below every position this round has read
+        // writes land at or below every position this chunk has read
         if (keep) W.buf[k + __popc(km & ((1u << lane) - 1u))] = g;
         k += __popc(km);
     }
