@@ -150,6 +150,29 @@ def test_battery_drop_in(gpu):
     assert h[:7].sum() == cnt.size and h[7] == cnt.max()
 
 
+def test_battery_cch_class(gpu):
+    """nwcch.cch_battery.BatteryCCH (python/cch_battery.py's class shape)
+    over nwcch.cch.CCH with the fixture's order: the reference's profiles,
+    answers by original vertex ids, the reference's (largest, mean) pair."""
+    from nwcch.cch import CCH
+    from nwcch.cch_battery import BatteryCCH
+    g, caps = battery_cases()[4]
+    c = CCH(int(g["n"]), g["off"], g["tgt"], order=g["rank"])
+    assert np.array_equal(c.first, g["first"]) and np.array_equal(c.head, g["head"])
+    bc = BatteryCCH(c)
+    for cap in caps:
+        largest, mean = bc.customize(g["w"], float(cap["M"]))
+        assert largest == int(cap["cnt"].max())
+        assert abs(mean - cap["poff"][-1] / cap["cnt"].size) < 1e-12
+        up, down = bc.profiles()
+        for a in (0, len(up) // 2, len(up) - 1):
+            assert up[a] == [tuple(p) for p in cap["pieces"][cap["poff"][2 * a]:cap["poff"][2 * a + 1]]]
+            assert down[a] == [tuple(p) for p in cap["pieces"][cap["poff"][2 * a + 1]:cap["poff"][2 * a + 2]]]
+        got = bc.query_batch(cap["qs"], cap["qt"], cap["b0"])
+        assert np.array_equal(got, cap["ans"])
+        assert bc.query(int(cap["qs"][0]), int(cap["qt"][0]), float(cap["b0"][0])) == cap["ans"][0]
+
+
 def test_battery_edges(gpu):
     """A single vertex, an empty query batch, capacity 0 (only free arcs and
     recuperation are feasible) and out-of-range ids."""
