@@ -9,8 +9,9 @@ battery-constrained layer over a CCH, customized and queried on the device.
     soc = bc.query(s, t, b0)                   # best charge at t, -inf if infeasible
 
 Differences a caller sees:
-* customize takes the arc energies as an array in CSR edge order (the
-  reference's g.adj order), or a graph dict holding them under "w_energy";
+* customize takes the arc energies as the reference's Graph object, as an
+  array in CSR edge order (the reference's g.adj order), or as a graph dict
+  holding them under "w_energy";
 * the profiles are those of the reference's Numba customization
   (python/cch_nb_battery.py: candidates merged for ascending lowest vertex);
   the pure-Python class merges in its triangle-list order, so near-equal
@@ -25,7 +26,18 @@ import numpy as np
 
 from . import battery as _bat
 
-__all__ = ["BatteryCCH"]
+__all__ = ["BatteryCCH", "energies_of"]
+
+
+def energies_of(g) -> np.ndarray:
+    """float64 arc energies in edge order from an array, a graph dict
+    ("w_energy") or the reference's Graph object (g.adj[u] = [(v, w), ...],
+    edge index = position in that order, python/graphs.py:21-33)."""
+    if hasattr(g, "adj"):
+        return np.fromiter((w for nb in g.adj for _, w in nb), np.float64)
+    if isinstance(g, dict):
+        g = g["w_energy"]
+    return np.ascontiguousarray(g, np.float64)
 
 
 class BatteryCCH:
@@ -39,11 +51,10 @@ class BatteryCCH:
     def customize(self, w, M):
         """Profiles for energies w and capacity M; returns the reference's
         (largest profile, mean pieces per direction)."""
-        if isinstance(w, dict):
-            w = w["w_energy"]
+        w = energies_of(w)
         if self._prof is not None:
             self._prof.free()
-        self._prof = _bat.customize(self.c.dev, np.asarray(w, np.float64), float(M))
+        self._prof = _bat.customize(self.c.dev, w, float(M))
         self.M = float(M)
         nd = 2 * self.c.m
         return self._prof.largest, (self._prof.pieces / nd if nd else 0.0)

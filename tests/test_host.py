@@ -124,6 +124,18 @@ def test_battery_reference_layout_and_histogram():
             assert h[2] == np.count_nonzero((cnt >= 2) & (cnt <= 5)) and h[7] == cnt.max()
 
 
+def test_battery_energies_from_graph_objects():
+    """nwcch.cch_battery reads energies in the reference's edge order from a
+    Graph-like object (adjacency lists of (v, w)), a dict or an array."""
+    from nwcch.cch_battery import energies_of
+
+    class FakeGraph:
+        adj = [[(1, 2.5), (2, -1.0)], [], [(0, 3.25)]]
+    assert energies_of(FakeGraph()).tolist() == [2.5, -1.0, 3.25]
+    assert energies_of({"w_energy": [1, 2]}).tolist() == [1.0, 2.0]
+    assert energies_of(np.array([0.5])).dtype == np.float64
+
+
 def test_double_order_key():
     """The integer order key the battery kernels compare doubles with
     (negative values: minus their magnitude bits; others: their bits) orders
