@@ -69,21 +69,52 @@ def log(msg):
 
 # --------------------------------------------------------------- workload
 
+def _cache_key(name: str, seed: int) -> str:
+    """Names what a cached workload was built from: its spec, seed and the
+    sources of the generators and the host preprocessing."""
+    import hashlib
+    h = hashlib.sha256(json.dumps([name, seed, WORKLOADS[name]], sort_keys=True).encode())
+    pkg = ROOT / "negative-weight-cch_gb300"
+    for p in [pkg / "nwcch" / "graphs.py", pkg / "nwcch" / "delaunay.py", pkg / "nwcch" / "topology.py",
+              *sorted((pkg / "csrc").glob("host_*"))]:
+        h.update(p.read_bytes())
+    return h.hexdigest()[:32]
+
+
 def make_workload(name: str, seed: int = 0):
+    """Graph, topology (order, symbolic contraction, arc map: host C++ in
+    libnwcch_host.so, no device code), metrics and query pairs of a workload.
+    Workloads of 1M vertices and more are cached under NWCCH_CACHE_DIR
+    (default _cache/ beside this file), so a second run on the same machine
+    skips the minutes the 24M topology takes to build."""
     from nwcch import graphs as G
     from nwcch import topology as T
     spec = WORKLOADS[name]
-    t0 = time.time()
-    if spec["kind"] == "grid":
-        g = G.grid(64, seed=seed)
-    elif spec["kind"] == "delaunay":
-        g = G.delaunay(spec["n"], seed=seed)
+    cache = None
+    if spec["n"] >= 1_000_000 and os.environ.get("NWCCH_CACHE_DIR", "x") != "":
+        cache = Path(os.environ.get("NWCCH_CACHE_DIR", str(ROOT / "_cache"))) / f"{name}_seed{seed}"
+    key = _cache_key(name, seed) if cache else None
+    hit = T.load_cache(cache, key) if cache else None
+    if hit is not None:
+        g, top = hit
+        log(f"graph {g['kind']} + topology from {cache}: n={g['n']:,} arcs={g['tgt'].size:,} "
+            f"m+={top['head'].size:,}")
     else:
-        g = G.road_like(spec["n"], arcs=spec["arcs"], seed=seed)
-    log(f"graph {g['kind']}: n={g['n']:,} arcs={g['tgt'].size:,} ({time.time() - t0:.1f}s)")
-    t0 = time.time()
-    top = T.build_topology(g)
-    log(f"order + symbolic + arc map: m+={top['head'].size:,} ({time.time() - t0:.1f}s)")
+        t0 = time.time()
+        if spec["kind"] == "grid":
+            g = G.grid(64, seed=seed)
+        elif spec["kind"] == "delaunay":
+            g = G.delaunay(spec["n"], seed=seed)
+        else:
+            g = G.road_like(spec["n"], arcs=spec["arcs"], seed=seed)
+        log(f"graph {g['kind']}: n={g['n']:,} arcs={g['tgt'].size:,} ({time.time() - t0:.1f}s)")
+        t0 = time.time()
+        top = T.build_topology(g)
+        log(f"order + symbolic + arc map: m+={top['head'].size:,} ({time.time() - t0:.1f}s)")
+        if cache:
+            t0 = time.time()
+            ok = T.save_cache(cache, key, g, top)
+            log(f"topology cache {'written' if ok else 'not written'}: {cache} ({time.time() - t0:.1f}s)")
     w_bad, cyc = None, None
     if spec["inject"]:
         gb, cyc = G.inject_negative_triangle(g, seed=seed + 1)
@@ -337,8 +368,9 @@ def run_ours(args, W, world):
         torch.cuda.synchronize()
         pot_ms.append(e0.elapsed_time(e1))
     good_host = good.to_numpy()
+    bad_host = metric.to_numpy()  # the timed metric, compared with the oracle's in full
     return dict(T=T, tuned=tuned, cust_tuned=cust_tuned, cust_ms=cust_ms, q_ms=q_ms, wall=wall, plain_ms=plain_ms, plain_equal=same,
-                e2e_ms=e2e_ms, graph_q=graph_q,
+                e2e_ms=e2e_ms, graph_q=graph_q, bad_host=bad_host, batch_dist=ref_d.cpu().numpy(),
                 plain_q_ms=plain_q_ms, lat_dist=lat_dist, pot_ms=pot_ms, pot=pot.cpu().numpy(), good_host=good_host,
                 lat_us=lat, clocks=clocks.summary(), neg=neg_k, saturated=bool(sat))
 
@@ -529,6 +561,7 @@ def run_batch(args, Wd, K):
         T.customize(w1.copy_(w_dev[k]), "int32", out=single, sync=False)
         equal &= bool(torch.equal(single.up, b.up[k]) and torch.equal(single.dn, b.dn[k]))
     assert equal, "batched customization differs from single customization"
+    b0_host = b.metric(0).to_numpy()
     # partial re-customization of metric 0: new lengths L' in [1, 2L] keep the
     # metric conservative (w' = height difference + L')
     rng = np.random.default_rng(5)
@@ -566,6 +599,9 @@ def run_batch(args, Wd, K):
                               "device_ms_median": round(statistics.median(dev_ms), 3),
                               "evaluated_median": int(statistics.median(ev)), "reps": 5,
                               "equal_full_recompute": True}
+    # parity at this size: metric 0 of the batch (before the updates) and 10k
+    # queries on it against the oracle
+    par = batch_parity(Wd, Wk[0], b0_host, qs=Wd["qs"], qt=Wd["qt"], T=T, m=b.metric(0))
     bm = statistics.median(batch_ms)
     B = batched_bytes(top["n"], top["e_arc"].size, T.m_plus, T.triangles, K)
     return {"workload": Wd["name"], "metrics": K, "batch_ms": round(bm, 3), "ms_per_metric": round(bm / K, 4),
@@ -574,7 +610,23 @@ def run_batch(args, Wd, K):
             "equal_to_singles": equal, "achieved_gbs": round(B / (bm / 1000) / 1e9, 1),
             "algorithmic_bytes": int(B),
             "l2": "flushed between steps" if fits_l2 else "inputs larger than L2",
-            "partial_updates": updates, "update_schedule": upd_tuning}
+            "partial_updates": updates, "update_schedule": upd_tuning, "parity": par}
+
+
+def batch_parity(Wd, w0, arcs0, qs, qt, T, m):
+    """Metric 0 of the batch as customized by the device equal to the
+    oracle's level-parallel customization, and the device's answers on the
+    workload's query pairs (after the updates, on the updated metric) equal
+    to the oracle's on the same metric."""
+    import oracle as orc
+    OT = orc.Topo.from_dict(Wd["top"])
+    up, dn = orc.customize_parallel(OT, w0, threads=orc.cpu_count())
+    cust_eq = bool(np.array_equal(up, arcs0[0]) and np.array_equal(dn, arcs0[1]))
+    d_dev = T.query_batch(m, qs, qt).cpu().numpy()
+    d_orc = orc.query_batch(OT, *m.to_numpy(), qs.astype(np.int64), qt.astype(np.int64), threads=orc.cpu_count())
+    q_eq = bool(np.array_equal(d_dev, d_orc))
+    return {"workload": Wd["name"], "customize_equal": cust_eq, "arcs_compared": int(up.size),
+            "queries_checked": int(qs.size), "queries_equal": q_eq, "equal": cust_eq and q_eq}
 
 
 def run_serving(args, Ws, loads):
@@ -698,21 +750,64 @@ def profile_part(args):
                       "sn_warp_min_count": tune.get(T, "sn_warp_min_count")}), flush=True)
 
 
-def cpu_baseline(W, budget_s: float):
-    """The oracle port of the reference customization (level-parallel, every
-    host core) plus the scan, on the same metric, repeated within budget_s."""
+def cpu_baseline(W, budget_s: float, forms=("parallel",)):
+    """The oracle ports of the reference customization plus the scan on the
+    same metric, each repeated within budget_s (at least once): "serial" is
+    CCH::customize (cpp/cch.cpp:437-463, one core), "parallel" the
+    level-parallel customize_parallel (cpp/cch.cpp:468-529, OpenMP on every
+    host core). The reference's results lead with the serial form, which is
+    the faster of the two on road graphs (results/cpp_USA.txt:7,22), so
+    `value` is the faster form's median. Returns the customized arcs of the
+    last run for the parity check."""
     import oracle as orc
     OT = orc.Topo.from_dict(W["top"])
     cores = orc.cpu_count()
     w = W["w_bad"] if W["w_bad"] is not None else W["w"]
-    times = []
-    t_start = time.perf_counter()
-    while not times or (time.perf_counter() - t_start < budget_s and len(times) < 5):
-        t0 = time.perf_counter()
-        up, dn = orc.customize_parallel(OT, w, threads=cores)
-        neg = orc.negative_cycle_arcs(up, dn)
-        times.append((time.perf_counter() - t0) * 1000)
-    return dict(value=statistics.median(times), cores=cores, runs=len(times), neg=neg)
+    res = {}
+    up = dn = neg = None
+    for form in forms:
+        times = []
+        t_start = time.perf_counter()
+        while not times or (time.perf_counter() - t_start < budget_s and len(times) < 5):
+            t0 = time.perf_counter()
+            if form == "serial":
+                up, dn = orc.customize(OT, w)
+            else:
+                up, dn = orc.customize_parallel(OT, w, threads=cores)
+            neg = orc.negative_cycle_arcs(up, dn)
+            times.append((time.perf_counter() - t0) * 1000)
+        res[form] = {"ms": round(statistics.median(times), 3), "runs": len(times),
+                     "cores": 1 if form == "serial" else cores}
+        log(f"cpu {form} customization + scan: {res[form]}")
+    best = min(res, key=lambda f: res[f]["ms"])
+    return dict(value=res[best]["ms"], cores=res[best]["cores"], runs=res[best]["runs"], form=best, forms=res,
+                neg=neg, up=up, dn=dn)
+
+
+def check_parity(W, top_cb, device_arcs, good_host, device_dist, qs, qt, count: int):
+    """Full-size parity of the benchmark's own workload (the reference
+    drivers' own check, python/run_nb.py:136-141 and cpp/cch.cpp:896-903,
+    against the oracle): every customized arc of the timed metric equal to
+    the oracle's, and the first `count` answers of the device's query batch
+    equal to the oracle's ET query on every host core."""
+    import oracle as orc
+    OT = orc.Topo.from_dict(W["top"])
+    up, dn = device_arcs
+    cust_eq = bool(np.array_equal(up, top_cb["up"]) and np.array_equal(dn, top_cb["dn"]))
+    mism = 0 if cust_eq else int(np.count_nonzero(up != top_cb["up"]) + np.count_nonzero(dn != top_cb["dn"]))
+    k = min(count, int(device_dist.size))
+    t0 = time.perf_counter()
+    d = orc.query_batch(OT, *good_host, qs[:k].astype(np.int64), qt[:k].astype(np.int64), threads=orc.cpu_count())
+    q_eq = bool(np.array_equal(d, device_dist[:k]))
+    out = {"workload": W["name"], "customize_equal": cust_eq, "arcs_compared": int(up.size),
+           "queries_checked": int(k), "queries_equal": q_eq,
+           "oracle_query_s": round(time.perf_counter() - t0, 2)}
+    if not cust_eq:
+        out["arcs_differing"] = mism
+    if not q_eq:
+        out["queries_differing"] = int(np.count_nonzero(d != device_dist[:k]))
+    log(f"parity: {out}")
+    return out
 
 
 def main():
@@ -723,6 +818,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default=os.environ.get("NWCCH_BENCH_WORKLOAD", "usa24m"), choices=list(WORKLOADS))
     ap.add_argument("--cpu-budget", type=float, default=20.0)
+    ap.add_argument("--parity-queries", type=int, default=10_000,
+                    help="answers of the timed query batch checked against the oracle (all host cores)")
     ap.add_argument("--batch-metrics", type=int, default=64,
                     help="metrics of the batched customization (0: skip it)")
     ap.add_argument("--batch-workload", default="delaunay264k", choices=list(WORKLOADS))
@@ -748,15 +845,22 @@ def main():
         if rank != 0:
             return
         W = make_workload(args.workload)
-        cb = cpu_baseline(W, args.cpu_budget)
+        cb = cpu_baseline(W, args.cpu_budget, forms=("serial", "parallel"))
+        top = W["top"]
+        form = {"serial": "serial CCH::customize (cpp/cch.cpp:437-463), 1 core",
+                "parallel": f"level-parallel customize_parallel (cpp/cch.cpp:468-529), {cb['cores']} cores"}
         line = {"metric": METRIC, "impl": "reference", "value": round(cb["value"], 3), "unit": UNIT,
                 "higher_is_better": False, "n_gpus": args.gpus, "steps": cb["runs"], "warmup": 0,
                 "dtype": "int64", "data": "synthetic",
-                "config": {"workload": args.workload, "n": W["top"]["n"], "m_plus": int(W["top"]["head"].size),
+                "config": {"workload": args.workload, "n": top["n"], "arcs": int(W["g"]["tgt"].size),
+                           "m_plus": int(top["head"].size),
+                           "triangles": int(count_triangles(top)),
                            "negative_cycle_injected": W["w_bad"] is not None},
                 "negative_cycle_arcs": cb["neg"],
+                "reference_forms": cb["forms"],
                 "cpu_baseline": {"value": round(cb["value"], 3), "unit": "ms", "cores": cb["cores"], "kind": "port",
-                                 "sample": f"{cb['runs']} level-parallel customizations + scans of the full metric"},
+                                 "sample": f"{cb['runs']} x {form[cb['form']]} + scan of the full metric "
+                                           f"(the faster of the two forms; both in reference_forms)"},
                 "e2e": {"value": round(cb["value"], 3), "unit": "ms", "h2d_bytes_per_step": 0,
                         "d2h_bytes_per_step": 0}}
         print(json.dumps(line), flush=True)
@@ -803,9 +907,15 @@ def main():
     B = algorithmic_bytes(top["n"], top["e_arc"].size, T.m_plus, T.triangles)
     achieved = B / (cust / 1000) / 1e9
     cb = cpu_baseline(W, args.cpu_budget)
+    parity = check_parity(W, cb, R["bad_host"], R["good_host"], R["batch_dist"], W["qs"], W["qt"],
+                          args.parity_queries)
+    del cb["up"], cb["dn"]
     cp = cpu_potential(W, R["good_host"], R["pot"])
     cq = cpu_queries(W, R["good_host"])
-    assert np.array_equal(cq["dist"], R["lat_dist"][:cq["queries"]]), "device and oracle distances differ"
+    parity["single_queries_equal"] = bool(np.array_equal(cq["dist"], R["lat_dist"][:cq["queries"]]))
+    parity["potential_equal"] = bool(cp["equal"])
+    if batch is not None:
+        parity["batched_section"] = batch.pop("parity")
     line = {
         "metric": METRIC, "value": round(cust_total * 1000 / replica_units(args.steps, world), 4), "unit": UNIT,
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -846,7 +956,9 @@ def main():
                      "algorithmic_bytes_per_launch": int(B),
                      "launch": "one customization: CUDA graph of k_fill2, k_base, k_sn_warp, k_sn_panel, k_sn_tile"},
         "cpu_baseline": {"value": round(cb["value"], 3), "unit": "ms", "cores": cb["cores"], "kind": "port",
-                         "sample": f"{cb['runs']} level-parallel customizations + scans of the same metric"},
+                         "sample": f"{cb['runs']} level-parallel customizations (cpp/cch.cpp:468-529) + scans "
+                                   f"of the same metric"},
+        "parity": parity,
         "clocks": R["clocks"],
         "potential": {"gpu_ms": round(statistics.median(R["pot_ms"]), 3),
                       "cpu_ms": round(cp["ms"], 1), "cpu_cores": 1, "cpu_kind": "port of cpp/cch.cpp:631-655",
@@ -856,6 +968,16 @@ def main():
         "battery": bat,
     }
     print(json.dumps(line), flush=True)
+    ok = (parity["customize_equal"] and parity["queries_equal"] and parity["single_queries_equal"]
+          and parity["potential_equal"] and parity.get("batched_section", {}).get("equal", True))
+    if not ok:
+        log("PARITY FAILURE: device results differ from the oracle's")
+        sys.exit(3)
+
+
+def count_triangles(top) -> int:
+    d = np.diff(np.asarray(top["first"], dtype=np.int64))
+    return int((d * (d - 1) // 2).sum())
 
 
 if __name__ == "__main__":

@@ -160,6 +160,15 @@ int nwcch_check(nwcch_topology* t, void* stream);
 /* Updates of at least this many (distinct) arcs skip the level sweep and
  * finish densely at once (0: never; the sweep budget decides). */
 #define NWCCH_TUNE_UPDATE_DENSE_MIN 13
+/* Failure detection of the update's bounded grid barrier: the spin limit of
+ * one wait (iterations of about 100 ns; default 2^24, a few seconds), and a
+ * test hook that makes every barrier wait for this many blocks more than the
+ * launch has (default 0), so that the wait runs out: the call then returns
+ * NWCCH_ERR_TIMEOUT with w updated and up/dn partly re-customized (customize
+ * again before use), and the handle's update workspace is reset so that the
+ * next update is exact. */
+#define NWCCH_TUNE_UPDATE_SPIN_LIMIT 14
+#define NWCCH_TUNE_TEST_BARRIER_EXTRA 15
 int nwcch_tune_set(nwcch_topology* t, int key, int64_t value);
 int nwcch_tune_get(const nwcch_topology* t, int key, int64_t* value);
 
@@ -279,7 +288,9 @@ int nwcch_query_batch_plain(nwcch_topology* t, const int32_t* up_dev, const int3
  * 8 * (2.5 * (depth + 1) + 1) bytes and whole blocks of 4 warps must fit, so
  * an elimination tree deeper than about 419,000 returns NWCCH_ERR_CAPACITY;
  * deeper trees just run fewer queries at a time. The first call on a device
- * looks up the scratch's device address (make it before any stream capture).
+ * looks up the scratch's device address (make it before any stream capture;
+ * the address is cached for the process, so do not call this entry point on
+ * a device again after cudaDeviceReset).
  * All calls on a device share the scratch: calls that overlap on the GPU
  * (other streams, other threads) race and must be serialized by the caller.
  * Synchronous; same results as nwcch_query_batch. */

@@ -1,11 +1,15 @@
-"""Builds libnwcch.so (CUDA kernels for sm_103a + host C++ + the C ABI) in-tree.
+"""Builds libnwcch.so (CUDA kernels for sm_103a + host C++ + the C ABI) in-tree,
+and libnwcch_host.so (the weight-independent host preprocessing alone).
 
     python negative-weight-cch_gb300/build.py [--force]
 
 Every .cu is compiled by nvcc for sm_103a only, every .cpp by g++, in
 parallel; the shared library links the CUDA runtime statically so that it
-loads with no GPU present. The build is skipped when a stamp of the sources
-and flags is unchanged.
+loads with no GPU present. The host library holds only the .cpp objects (no
+device code, no CUDA runtime): ordering, symbolic contraction, arc mapping and
+graph generation helpers, for processes that prepare topologies without
+touching the GPU. The build is skipped when a stamp of the sources and flags
+is unchanged.
 """
 from __future__ import annotations
 
@@ -23,6 +27,7 @@ CSRC = PKG / "csrc"
 INCLUDE = ROOT / "include"
 OUT_DIR = PKG / "_build"
 LIB = OUT_DIR / "libnwcch.so"
+HOST_LIB = OUT_DIR / "libnwcch_host.so"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
@@ -60,7 +65,8 @@ def _run(cmd):
 def build(force: bool = False, verbose: bool = False) -> Path:
     stamp_file = OUT_DIR / "stamp"
     stamp = _stamp()
-    if not force and LIB.exists() and stamp_file.exists() and stamp_file.read_text() == stamp:
+    if (not force and LIB.exists() and HOST_LIB.exists() and stamp_file.exists()
+            and stamp_file.read_text() == stamp):
         return LIB
     OUT_DIR.mkdir(parents=True, exist_ok=True)
     nvcc = _nvcc()
@@ -83,6 +89,10 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     _run([nvcc, *ARCH, "-shared", "-cudart", "static", "-o", str(tmp), *map(str, objs),
           "-lpthread", "-ldl", "-lrt"])
     os.replace(tmp, LIB)
+    host_objs = [o for o, src in zip(objs, _sources()) if src.suffix == ".cpp"]
+    tmp = HOST_LIB.with_suffix(".so.tmp")
+    _run([os.environ.get("CXX", "g++"), "-shared", "-pthread", "-o", str(tmp), *map(str, host_objs)])
+    os.replace(tmp, HOST_LIB)
     stamp_file.write_text(stamp)
     return LIB
 

@@ -68,7 +68,7 @@ constexpr double EPS = 1e-9;
 constexpr int BAT_POOL_OVERFLOW = 1;
 constexpr int BAT_WORK_OVERFLOW = 2;
 constexpr int LEVEL_WARPS = 4;
-constexpr int LEVEL_BLOCKS = 152 * 4;  // blocks of the level kernel; one buffer slot per warp
+constexpr int LEVEL_BLOCKS_PER_SM = 4;  // blocks of the level kernel per SM; one buffer slot per warp
 constexpr int QUERY_WARPS = 4;
 
 // A stored piece, with in - EPS for the queries' feasibility test.
@@ -954,7 +954,7 @@ int get_plan(nwcch_topology* t, BatPlan** out) {
             delete P;
             return NWCCH_ERR_CUDA;
         }
-        k_dtail<<<152 * 4, 256>>>(t->d.darc, t->d.tail, mp, P->dtail);
+        k_dtail<<<t->sms * 4, 256>>>(t->d.darc, t->d.tail, mp, P->dtail);
         if (cudaDeviceSynchronize() != cudaSuccess) {
             cudaFree(P->arcs);
             cudaFree(P->dtail);
@@ -1018,7 +1018,8 @@ int run_levels(nwcch_topology* t, nwcch_battery* b, const BatPlan* P, const doub
     for (int32_t l = 0; l < t->levels; l++) {
         const int64_t a0 = t->level_arc_off[l], a1 = t->level_arc_off[l + 1];
         if (a1 == a0) continue;
-        const int64_t blocks = std::min<int64_t>((a1 - a0 + LEVEL_WARPS - 1) / LEVEL_WARPS, LEVEL_BLOCKS);
+        const int64_t blocks = std::min<int64_t>((a1 - a0 + LEVEL_WARPS - 1) / LEVEL_WARPS,
+                                               (int64_t)LEVEL_BLOCKS_PER_SM * t->sms);
         k_bat_level<<<(unsigned)blocks, 32 * LEVEL_WARPS, smem, s>>>(t->d, A, a0, a1, l);
     }
     NWCCH_CUDA_TRY(cudaGetLastError());
@@ -1043,8 +1044,15 @@ extern "C" int nwcch_battery_customize(nwcch_topology* t, const double* w_dev, d
     b->M = capacity;
     b->nd = 2 * t->d.m_plus;
     const size_t nd1 = (size_t)std::max<int64_t>(1, b->nd);
-    b->pool_cap = t->tune.battery_pool > 0 ? t->tune.battery_pool
-                                           : std::max<int64_t>(b->nd + b->nd / 2 + 1024, t->battery_pool_hint);
+    int32_t gcap = 64;
+    {
+        // the sizes learned by earlier customizations of this handle (which
+        // may run concurrently on other streams)
+        std::lock_guard<std::mutex> lock(t->mu);
+        b->pool_cap = t->tune.battery_pool > 0 ? t->tune.battery_pool
+                                               : std::max<int64_t>(b->nd + b->nd / 2 + 1024, t->battery_pool_hint);
+        gcap = std::max<int32_t>(64, t->tune.battery_buffer);
+    }
     if (cudaMalloc(&b->cnt, nd1 * sizeof(int32_t)) != cudaSuccess ||
         cudaMalloc(&b->pos, nd1 * sizeof(int64_t)) != cudaSuccess ||
         cudaMalloc(&b->pool, (size_t)b->pool_cap * sizeof(Piece)) != cudaSuccess ||
@@ -1052,8 +1060,7 @@ extern "C" int nwcch_battery_customize(nwcch_topology* t, const double* w_dev, d
         nwcch_battery_free(b);
         return NWCCH_ERR_NOMEM;
     }
-    int32_t gcap = std::max<int32_t>(64, t->tune.battery_buffer);
-    const int64_t slots = (int64_t)LEVEL_BLOCKS * LEVEL_WARPS;
+    const int64_t slots = (int64_t)LEVEL_BLOCKS_PER_SM * t->sms * LEVEL_WARPS;
     void* gbuf = nullptr;
     void* next = nullptr;
     void* tri = nullptr;
@@ -1102,8 +1109,11 @@ extern "C" int nwcch_battery_customize(nwcch_topology* t, const double* w_dev, d
     b->largest = host.largest;
     // the next customization of this topology starts with buffers that fit
     // (an overflow costs a whole rerun)
-    t->tune.battery_buffer = std::max<int32_t>(t->tune.battery_buffer, gcap);
-    t->battery_pool_hint = std::max<int64_t>(t->battery_pool_hint, b->pieces + b->pieces / 8);
+    {
+        std::lock_guard<std::mutex> lock(t->mu);
+        t->tune.battery_buffer = std::max<int32_t>(t->tune.battery_buffer, gcap);
+        t->battery_pool_hint = std::max<int64_t>(t->battery_pool_hint, b->pieces + b->pieces / 8);
+    }
     *out = b;
     return NWCCH_OK;
 }
@@ -1161,7 +1171,7 @@ extern "C" int nwcch_battery_query(nwcch_topology* t, const nwcch_battery* b, co
         k_bat_query_cta<<<(unsigned)nq, 32 * QUERY_CTA_WARPS, 0, s>>>(
             t->d, B, s_rank_dev, t_rank_dev, b0_dev, nq, out_dev, static_cast<unsigned char*>(scratch), per_query, err);
     } else {
-        const int64_t warps = std::min<int64_t>(nq, 152 * 16);
+        const int64_t warps = std::min<int64_t>(nq, (int64_t)t->sms * 16);
         const int64_t blocks = (warps + QUERY_WARPS - 1) / QUERY_WARPS;
         NWCCH_CUDA_TRY(cudaMallocAsync(&scratch, (size_t)(blocks * QUERY_WARPS * per_query), s));
         k_bat_query<<<(unsigned)blocks, 32 * QUERY_WARPS, 0, s>>>(

@@ -116,6 +116,19 @@ cudaError_t launch_pdl(bool pdl, void (*kernel)(KArgs...), dim3 grid, dim3 block
     return cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
 }
 
+// SMs of the current device, cached per device: grids are sized in multiples
+// of it (1 if the device cannot be queried; the launch then reports the error).
+inline int device_sms() {
+    static int cache[64] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 1;
+    if (dev >= 0 && dev < 64 && cache[dev] > 0) return cache[dev];
+    int sms = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms < 1) return 1;
+    if (dev >= 0 && dev < 64) cache[dev] = sms;
+    return sms;
+}
+
 #define NWCCH_CUDA_TRY(expr)                            \
     do {                                                \
         cudaError_t _e = (expr);                        \

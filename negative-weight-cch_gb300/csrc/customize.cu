@@ -148,7 +148,7 @@ __global__ void k_negloops(const int32_t* __restrict__ loops, int64_t nloops, co
 
 int grid_for(int64_t count, int block) {
     const int64_t g = (count + block - 1) / block;
-    return (int)std::max<int64_t>(1, std::min<int64_t>(g, 152 * 32));
+    return (int)std::max<int64_t>(1, std::min<int64_t>(g, (int64_t)device_sms() * 32));
 }
 
 template <class T>

@@ -278,7 +278,7 @@ int query_paths(nwcch_topology* t, const T* up, const T* dn, const int32_t* s_ra
                 cudaStream_t s) {
     const int64_t Dp = t->d.max_depth + 1;
     const int64_t per_warp = (path_scratch_bytes(Dp, t->levels) + 255) & ~255LL;
-    const int64_t warps = std::max<int64_t>(1, std::min<int64_t>(nq, 152 * 16));
+    const int64_t warps = std::max<int64_t>(1, std::min<int64_t>(nq, (int64_t)t->sms * 16));
     const int64_t blocks = (warps + 3) / 4;
     void* scratch = nullptr;
     NWCCH_CUDA_TRY(cudaMallocAsync(&scratch, (size_t)(blocks * 4 * per_warp), s));

@@ -301,11 +301,11 @@ __global__ void __launch_bounds__(256) k_pot_down_single(DevTopo D, SnDev S, con
 }
 
 int thread_grid(int64_t count) {
-    return (int)std::max<int64_t>(1, std::min<int64_t>((count + 255) / 256, 152 * 16));
+    return (int)std::max<int64_t>(1, std::min<int64_t>((count + 255) / 256, (int64_t)device_sms() * 16));
 }
 
 int warp_grid(int64_t count) {
-    return (int)std::max<int64_t>(1, std::min<int64_t>((count + 3) / 4, 152 * 64));
+    return (int)std::max<int64_t>(1, std::min<int64_t>((count + 3) / 4, (int64_t)device_sms() * 64));
 }
 
 }  // namespace
@@ -320,10 +320,10 @@ int potential_launches(nwcch_topology* t, SnPlan* P, const T* up, const T* dn, i
         const int64_t cnt = P->sn_level_off[l + 1] - off;
         const int32_t* o = P->d_sn_order + off;
         if (big) {
-            k_pot_up_cta<T><<<(unsigned)std::min<int64_t>(big, 152 * 8), 256, 0, s>>>(D, P->dev, o, big, up, p, err);
+            k_pot_up_cta<T><<<(unsigned)std::min<int64_t>(big, (int64_t)t->sms * 8), 256, 0, s>>>(D, P->dev, o, big, up, p, err);
             const int64_t bo = P->pot_bu_off[l], bn = P->pot_bu_off[l + 1] - bo;
             if (bn)
-                k_pot_up_bnd<T><<<(unsigned)std::min<int64_t>(bn, 152 * 16), 256, 0, s>>>(D, P->dev, P->d_pot_bu + 2 * bo,
+                k_pot_up_bnd<T><<<(unsigned)std::min<int64_t>(bn, (int64_t)t->sms * 16), 256, 0, s>>>(D, P->dev, P->d_pot_bu + 2 * bo,
                                                                                         bn, up, p, err);
         }
         if (single > big)
@@ -339,9 +339,9 @@ int potential_launches(nwcch_topology* t, SnPlan* P, const T* up, const T* dn, i
         if (big) {
             const int64_t bo = P->pot_bd_off[l], bn = P->pot_bd_off[l + 1] - bo;
             if (bn)
-                k_pot_down_bnd<T><<<(unsigned)std::min<int64_t>(bn, 152 * 16), 256, 0, s>>>(
+                k_pot_down_bnd<T><<<(unsigned)std::min<int64_t>(bn, (int64_t)t->sms * 16), 256, 0, s>>>(
                     D, P->dev, P->d_pot_bd + 2 * bo, bn, dn, p, err);
-            k_pot_down_cta<T><<<(unsigned)std::min<int64_t>(big, 152 * 8), 256, 0, s>>>(D, P->dev, o, big, dn, p, err);
+            k_pot_down_cta<T><<<(unsigned)std::min<int64_t>(big, (int64_t)t->sms * 8), 256, 0, s>>>(D, P->dev, o, big, dn, p, err);
         }
         if (single > big)
             k_pot_down_warp<T><<<warp_grid(single - big), 128, 0, s>>>(D, P->dev, o + big, single - big, dn, p, err);

@@ -94,7 +94,7 @@ int query_plain(nwcch_topology* t, const T* up, const T* dn, const int32_t* s_ra
                 int64_t* dist, cudaStream_t s) {
     const int64_t Dp = t->d.max_depth + 1;
     const int64_t per_warp = 2 * Dp + (Dp + 1) / 2 + 1;  // int64 words: F, R, chain (int32)
-    const int64_t warps = std::min<int64_t>(nq, 152 * 32);
+    const int64_t warps = std::min<int64_t>(nq, (int64_t)t->sms * 32);
     const int block = 128;
     const int64_t blocks = (warps * 32 + block - 1) / block;
     void* scratch = nullptr;
@@ -186,7 +186,9 @@ int64_t* g_scratch_addr[256];  // device address of g_query_scratch, per device
 
 // The host cannot name a __device__ array directly (its host-side symbol is
 // only a stand-in), so its device address is looked up once per device, with
-// that device current, and cached.
+// that device current, and cached. The cache belongs to the device's primary
+// context: after cudaDeviceReset the process must not call this entry point
+// again on that device (the cached address would be stale).
 static int static_query_scratch(int64_t** out) {
     int dev = 0;
     NWCCH_CUDA_TRY(cudaGetDevice(&dev));
@@ -194,7 +196,10 @@ static int static_query_scratch(int64_t** out) {
     std::lock_guard<std::mutex> lock(g_scratch_mu);
     if (!g_scratch_addr[dev]) {
         void* p = nullptr;
-        if (cudaGetSymbolAddress(&p, g_query_scratch) != cudaSuccess || !p) return NWCCH_ERR_CUDA;
+        if (cudaGetSymbolAddress(&p, g_query_scratch) != cudaSuccess || !p) {
+            cudaGetLastError();  // a failed lookup must not surface as a later launch's error
+            return NWCCH_ERR_CUDA;
+        }
         g_scratch_addr[dev] = static_cast<int64_t*>(p);
     }
     *out = g_scratch_addr[dev];
@@ -218,7 +223,7 @@ extern "C" int nwcch_query_batch_noalloc(nwcch_topology* t, const int32_t* up_de
     int64_t* scratch = nullptr;
     const int rc = static_query_scratch(&scratch);
     if (rc) return rc;
-    const int64_t want_blocks = (std::min<int64_t>(nq, 152 * 32) + warps_per_block - 1) / warps_per_block;
+    const int64_t want_blocks = (std::min<int64_t>(nq, (int64_t)t->sms * 32) + warps_per_block - 1) / warps_per_block;
     const int64_t blocks = std::min(want_blocks, max_blocks);
     cudaStream_t s = (cudaStream_t)stream;
     // no state in the scratch survives between queries: every label and chain

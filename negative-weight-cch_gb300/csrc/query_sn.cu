@@ -525,7 +525,7 @@ __global__ void k_query_sn(DevTopo D, SnDev S, const T* __restrict__ up, const T
 }
 
 static unsigned grid_for_queries(int64_t count) {
-    return (unsigned)std::max<int64_t>(1, std::min<int64_t>((count + 255) / 256, 152 * 8));
+    return (unsigned)std::max<int64_t>(1, std::min<int64_t>((count + 255) / 256, (int64_t)device_sms() * 8));
 }
 
 // Shared-memory budget per block and warps (queries in flight) per block,

@@ -309,7 +309,7 @@ int run_supernodal(nwcch_topology* t, SnPlan* P, const int32_t* w, T* up, T* dn,
                 break;
             case SN_WARP: {
                 constexpr int WARPS = sizeof(T) == 4 ? 8 : 4;
-                const int64_t blocks = std::min<int64_t>((la.count + WARPS - 1) / WARPS, 152 * 64);
+                const int64_t blocks = std::min<int64_t>((la.count + WARPS - 1) / WARPS, (int64_t)device_sms() * 64);
                 e = launch_pdl(pdl, k_sn_warp<T, WARPS>, dim3((unsigned)blocks, metrics), dim3(32 * WARPS), 0, s, D,
                                P->dev, it, la.count, up, dn, err);
                 break;

@@ -94,8 +94,14 @@ extern "C" int nwcch_topology_create(int64_t n, const int64_t* first, const int3
     for (int64_t k = 0; k < m; k++)
         if (e_arc[k] < -1 || e_arc[k] >= mp) return NWCCH_ERR_TOPOLOGY;
 
+    int dev = 0, sms = 0;
+    NWCCH_CUDA_TRY(cudaGetDevice(&dev));
+    NWCCH_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     auto* t = new (std::nothrow) nwcch_topology();
     if (!t) return NWCCH_ERR_NOMEM;
+    t->sms = std::max(1, sms);
+    t->tune.query_cta_max = 8 * (int64_t)t->sms;
+    t->tune.query_cta_wide_max = t->sms;
     int rc = NWCCH_OK;
     do {
         std::vector<int32_t> tail(mp), depth(n, 0), hdep(mp), lvl(n, 0);
@@ -312,13 +318,27 @@ extern "C" int nwcch_tune_set(nwcch_topology* t, int key, int64_t value) {
             if (value < 0) return NWCCH_ERR_ARG;
             t->tune.update_dense_min = value;
             return NWCCH_OK;
+        case NWCCH_TUNE_UPDATE_SPIN_LIMIT:
+            if (value < 1) return NWCCH_ERR_ARG;
+            t->tune.update_spin_limit = value;
+            return NWCCH_OK;
+        case NWCCH_TUNE_TEST_BARRIER_EXTRA:
+            if (value < 0 || value > 1024) return NWCCH_ERR_ARG;
+            t->tune.test_barrier_extra = (int32_t)value;
+            return NWCCH_OK;
         case NWCCH_TUNE_BATTERY_POOL:
             if (value < 0) return NWCCH_ERR_ARG;
-            t->tune.battery_pool = value;
+            {
+                std::lock_guard<std::mutex> lock(t->mu);  // read by battery customizations
+                t->tune.battery_pool = value;
+            }
             return NWCCH_OK;
         case NWCCH_TUNE_BATTERY_BUFFER:
             if (value < 64 || value > (1 << 22)) return NWCCH_ERR_ARG;
-            t->tune.battery_buffer = (int32_t)value;
+            {
+                std::lock_guard<std::mutex> lock(t->mu);
+                t->tune.battery_buffer = (int32_t)value;
+            }
             return NWCCH_OK;
         default:
             return NWCCH_ERR_ARG;
@@ -337,6 +357,8 @@ extern "C" int nwcch_tune_get(const nwcch_topology* t, int key, int64_t* value) 
         case NWCCH_TUNE_QUERY_CTA_WIDE_MAX: *value = t->tune.query_cta_wide_max; return NWCCH_OK;
         case NWCCH_TUNE_QUERY_CTA_DENSE_ROWS: *value = t->tune.query_cta_dense_rows; return NWCCH_OK;
         case NWCCH_TUNE_UPDATE_DENSE_MIN: *value = t->tune.update_dense_min; return NWCCH_OK;
+        case NWCCH_TUNE_UPDATE_SPIN_LIMIT: *value = t->tune.update_spin_limit; return NWCCH_OK;
+        case NWCCH_TUNE_TEST_BARRIER_EXTRA: *value = t->tune.test_barrier_extra; return NWCCH_OK;
         case NWCCH_TUNE_BATTERY_POOL: *value = t->tune.battery_pool; return NWCCH_OK;
         case NWCCH_TUNE_BATTERY_BUFFER: *value = t->tune.battery_buffer; return NWCCH_OK;
         case NWCCH_TUNE_SN_WARP_CAP:

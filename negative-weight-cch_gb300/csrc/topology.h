@@ -36,12 +36,14 @@ struct Tuning {
     int32_t query_dense_rows = 16;          // query chunks with fewer rows go row by row
     int64_t query_smem_labels_max = 8192;   // per-warp query labels above this go to global scratch
     int32_t query_occupancy = 1;            // 2: 32-bit query kernel capped at 64 registers
-    int64_t query_cta_max = 152 * 8;        // batches up to this many queries: a CTA per query
-    int64_t query_cta_wide_max = 152;       // ... of 16 warps up to this many, else of 8
+    int64_t query_cta_max = 0;              // batches up to this many queries: a CTA per query (8 per SM)
+    int64_t query_cta_wide_max = 0;         // ... of 16 warps up to this many (one per SM), else of 8
     int32_t query_cta_dense_rows = 1;       // the CTA form's row-by-row threshold
     int32_t pdl = 0;                        // customization kernels as programmatic dependent launches
     int64_t update_budget_ns = 0;           // level-sweep budget of an update (0: from the triangle count)
     int64_t update_dense_min = 0;           // updates of at least this many arcs skip the sweep (0: never)
+    int64_t update_spin_limit = 1 << 24;    // spins (about 100 ns each) of one update barrier wait
+    int32_t test_barrier_extra = 0;         // test hook: barrier waits for this many extra blocks
     int64_t battery_pool = 0;               // initial battery piece pool (0: 1.5 pieces a direction)
     int32_t battery_buffer = 512;           // initial per-warp buffer of a long battery profile (pieces)
 };
@@ -58,6 +60,7 @@ struct StreamSlot {
 
 struct nwcch_topology {
     nwcch::DevTopo d{};
+    int32_t sms = 0;                          // SMs of the device the handle was created on
     int64_t triangles = 0;
     int32_t levels = 0;
     int32_t max_deg = 0;

@@ -12,7 +12,8 @@
 //
 // One cooperative launch runs the whole update: its blocks are co-resident,
 // and a level ends with a grid barrier whose spin is bounded (on timeout the
-// kernel records ERR_TIMEOUT and every block returns). The kernel cleans its
+// kernel records ERR_TIMEOUT and every block returns; the host then resets
+// the workspace and reports NWCCH_ERR_TIMEOUT). The kernel cleans its
 // workspace (queued flags, bucket counts, pending bits) before it exits.
 //
 // The level sweep pays a barrier per level and a row search per lower
@@ -80,6 +81,8 @@ struct UpdateArgs {
     int* err;
     long long budget_ns;  // sweep time before the dense finish (0: dense from the start)
     int64_t max_arcs;     // evaluated arcs before the dense finish
+    long long spin_limit; // spins of one barrier wait before ERR_TIMEOUT
+    int barrier_extra;    // test hook: arrivals a barrier waits for beyond the grid (0)
 };
 
 static constexpr int kStatWords = 16;
@@ -118,7 +121,7 @@ static __device__ bool grid_sync(const UpdateArgs<T>& A) {
         const unsigned long long g = *gen;
         __threadfence();
         ok = 1;
-        if (atomicAdd(count, 1ull) == (unsigned long long)gridDim.x - 1) {
+        if (atomicAdd(count, 1ull) == (unsigned long long)gridDim.x + A.barrier_extra - 1) {
             *count = 0;
             __threadfence();
             atomicAdd((unsigned long long*)gen, 1ull);
@@ -126,7 +129,7 @@ static __device__ bool grid_sync(const UpdateArgs<T>& A) {
             long long spins = 0;
             while (*gen == g) {
                 __nanosleep(100);
-                if (++spins > (1ll << 24)) {  // a few seconds
+                if (++spins > A.spin_limit) {
                     atomicOr(A.err, ERR_TIMEOUT);
                     ok = 0;
                     break;
@@ -545,6 +548,21 @@ int get_workspace(nwcch_topology* t, int64_t k, UpdateWorkspace** out) {
 
 }  // namespace
 
+// Every per-arc and per-level flag of the workspace back to zero (after a
+// sweep that could not clean up after itself).
+static int reset_workspace(nwcch_topology* t, UpdateWorkspace* ws, cudaStream_t s) {
+    const int64_t mp = t->d.m_plus, L = t->levels;
+    const size_t qbytes = (size_t)((mp + 3) & ~3LL) + 4;
+    NWCCH_CUDA_TRY(cudaMemsetAsync(ws->queued, 0, qbytes, s));
+    NWCCH_CUDA_TRY(cudaMemsetAsync(ws->chg, 0, qbytes, s));
+    NWCCH_CUDA_TRY(cudaMemsetAsync(ws->dq, 0, qbytes, s));
+    NWCCH_CUDA_TRY(cudaMemsetAsync(ws->bcount, 0, L * 4, s));
+    NWCCH_CUDA_TRY(cudaMemsetAsync(ws->pending, 0, ((L + 31) / 32) * 4, s));
+    NWCCH_CUDA_TRY(cudaMemsetAsync(ws->stats, 0, kStatWords * sizeof(unsigned long long), s));
+    NWCCH_CUDA_TRY(cudaStreamSynchronize(s));
+    return NWCCH_OK;
+}
+
 // Time the level sweep may take before the update is finished densely: about
 // half a full customization (which runs near 1e11 triangles/s), at least
 // 0.2 ms. NWCCH_UPDATE_MODE=dense or =incremental forces one form.
@@ -595,12 +613,12 @@ int finish_dense(nwcch_topology* t, UpdateWorkspace* ws, const int32_t* w_dev, T
         ws->ntiles = (int64_t)tl.size();
         ws->tiles_plan = P;
     }
-    const unsigned grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>(ws->ntiles, 152 * 8));
+    const unsigned grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>(ws->ntiles, (int64_t)t->sms * 8));
     k_dense_cols<<<grid, 32 * kMarkWarps, 0, s>>>(t->d, P->dev, ws->tiles, ws->ntiles, ws->chg, ws->acol, bflag);
     k_dense_mark<<<grid, 32 * kMarkWarps, 0, s>>>(t->d, P->dev, ws->tiles, ws->ntiles, ws->chg, ws->dq, ws->acol,
                                                   bflag);
     k_dense_count<<<grid_for(mp, 256), 256, 0, s>>>(t->d, L, ws->queued, ws->dq, ws->stats);
-    k_update_clean<<<152 * 4, 256, 0, s>>>(*ws, t->d_level_arc_off, mp);
+    k_update_clean<<<t->sms * 4, 256, 0, s>>>(*ws, t->d_level_arc_off, mp);
     NWCCH_CUDA_TRY(cudaGetLastError());
     NWCCH_CUDA_TRY(cudaMemsetAsync(ws->dq, 0, (size_t)mp, s));
     return NWCCH_OK;
@@ -649,12 +667,25 @@ int update(nwcch_topology* t, int32_t* w_dev, T* up_dev, T* dn_dev, const int64_
     // large updates touch most of the top separators: finish densely at once
     A.budget_ns = (t->tune.update_dense_min > 0 && kk >= t->tune.update_dense_min) ? 0 : sweep_budget_ns(t);
     A.max_arcs = std::max<int64_t>(4096, t->d.m_plus / 8);
+    A.spin_limit = t->tune.update_spin_limit;
+    A.barrier_extra = t->tune.test_barrier_extra;
     void* args[] = {&A};
     const int blocks = sizeof(T) == 4 ? ws->blocks32 : ws->blocks64;
     NWCCH_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k_update<T>, dim3(blocks), dim3(256), args, 0, s));
     unsigned long long h[kStatWords];
+    int herr = 0;
     NWCCH_CUDA_TRY(cudaMemcpyAsync(h, ws->stats, sizeof(h), cudaMemcpyDeviceToHost, s));
+    NWCCH_CUDA_TRY(cudaMemcpyAsync(&herr, A.err, sizeof(int), cudaMemcpyDeviceToHost, s));
     NWCCH_CUDA_TRY(cudaStreamSynchronize(s));
+    if (herr & ERR_TIMEOUT) {
+        // a barrier wait ran out: the blocks left without the sweep's
+        // cleanup, so the queued flags, bucket counts, pending bits and
+        // change flags are reset here; w holds the new weights and up/dn are
+        // partly updated (the caller customizes again)
+        rc = reset_workspace(t, ws, s);
+        const int rc2 = consume_error(t, s);
+        return rc ? rc : rc2;
+    }
     if (h[7]) {  // the sweep stopped at level h[7] - 1: finish densely
         rc = finish_dense<T>(t, ws, w_dev, up_dev, dn_dev, (int32_t)(h[7] - 1), s);
         if (rc) return rc;

@@ -2,6 +2,12 @@
 
 The library is built in-tree by ``negative-weight-cch_gb300/build.py``. There
 is no fallback: if the library cannot be loaded, every entry point raises.
+
+The weight-independent host preprocessing (``nwcch_undirected_csr``,
+``nwcch_nested_dissection``, ``nwcch_symbolic``, ``nwcch_edge_arcs``, the graph
+generation helpers) is bound from ``libnwcch_host.so``, which holds the same
+host objects without device code: preparing a topology never maps the CUDA
+library.
 """
 from __future__ import annotations
 
@@ -13,6 +19,7 @@ import numpy as np
 
 PKG = Path(__file__).resolve().parent.parent
 LIB_PATH = PKG / "_build" / "libnwcch.so"
+HOST_LIB_PATH = PKG / "_build" / "libnwcch_host.so"
 
 OK = 0
 ERRORS = {
@@ -36,6 +43,7 @@ class NwcchError(RuntimeError):
 
 _lock = threading.Lock()
 _lib = None
+_host = None
 
 P = C.c_void_p
 I64 = C.c_int64
@@ -54,6 +62,8 @@ _SIGNATURES = {
     "nwcch_emst_mask": [I64, I64, P, P, P, P],
 }
 _VOID = {"nwcch_host_free"}
+# bound from the host library (and from the full library too, where present)
+_HOST = frozenset(_SIGNATURES)
 
 
 def register(name: str, argtypes, restype=C.c_int):
@@ -87,6 +97,22 @@ def lib():
     return _lib
 
 
+def host_lib():
+    """The host-only library (no device code): the preprocessing entry points."""
+    global _host
+    if _host is not None:
+        return _host
+    with _lock:
+        if _host is None:
+            if not HOST_LIB_PATH.exists():
+                raise RuntimeError(f"{HOST_LIB_PATH} is missing: build it with negative-weight-cch_gb300/build.py")
+            handle = C.CDLL(str(HOST_LIB_PATH))
+            for name in _HOST:
+                _bind(handle, name)
+            _host = handle
+    return _host
+
+
 def check(code: int, where: str):
     if code != OK:
         raise NwcchError(code, where)
@@ -110,4 +136,4 @@ def take_buffer(p: C.c_void_p, count: int, dtype) -> np.ndarray:
         buf = (C.c_char * (count * dtype.itemsize)).from_address(p.value)
         return np.frombuffer(buf, dtype=dtype, count=count).copy()
     finally:
-        lib().nwcch_host_free(p)
+        host_lib().nwcch_host_free(p)

@@ -85,9 +85,12 @@ class BatteryProfiles:
         if s.numel() != t.numel():
             raise ValueError("s and t differ in length")
         if isinstance(b0, torch.Tensor):
-            b = b0.to(device="cuda", dtype=torch.float64)
+            b = b0.to(device="cuda", dtype=torch.float64).reshape(-1)
         else:
             b = torch.as_tensor(np.broadcast_to(np.asarray(b0, np.float64), (s.numel(),)).copy()).cuda()
+        if b.numel() not in (1, s.numel()):
+            # the kernel reads one start charge per query
+            raise ValueError(f"b0 has {b.numel()} values for {s.numel()} queries (expected 1 or {s.numel()})")
         b = b.expand(s.numel()).contiguous() if b.numel() == 1 else b.contiguous()
         if out is None:
             out = torch.empty(max(s.numel(), 1), dtype=torch.float64, device="cuda")

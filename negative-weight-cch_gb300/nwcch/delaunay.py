@@ -77,7 +77,7 @@ def _edges_from_triangles(tri: np.ndarray, n: int):
     from . import _lib
     tri = np.ascontiguousarray(tri, np.int64)
     eu, ev, ne = C.c_void_p(), C.c_void_p(), C.c_int64()
-    _lib.check(_lib.lib().nwcch_triangle_edges(n, tri.shape[0], _lib.ptr(tri), C.byref(eu), C.byref(ev),
+    _lib.check(_lib.host_lib().nwcch_triangle_edges(n, tri.shape[0], _lib.ptr(tri), C.byref(eu), C.byref(ev),
                                                C.byref(ne)), "triangle_edges")
     return _lib.take_buffer(eu, ne.value, np.int64), _lib.take_buffer(ev, ne.value, np.int64)
 

@@ -113,7 +113,7 @@ def _emst_mask(n, eu, ev, length):
     ev = np.ascontiguousarray(ev, np.int64)
     length = np.ascontiguousarray(length, np.float64)
     mask = np.empty(eu.size, np.uint8)
-    _lib.check(_lib.lib().nwcch_emst_mask(n, eu.size, _lib.ptr(eu), _lib.ptr(ev), _lib.ptr(length),
+    _lib.check(_lib.host_lib().nwcch_emst_mask(n, eu.size, _lib.ptr(eu), _lib.ptr(ev), _lib.ptr(length),
                                           _lib.ptr(mask)), "emst_mask")
     return mask.astype(bool)
 

@@ -1,7 +1,8 @@
 """Weight-independent preprocessing on the host, with the reference's names and
 array layouts (python/cch_nb.py:22-524): undirected_csr, nested_dissection,
 symbolic, edge_arcs, count_triangles. The work is done in C++ inside
-libnwcch.so; these wrappers only convert arrays.
+libnwcch_host.so (the host objects of libnwcch.so without device code);
+these wrappers only convert arrays.
 """
 from __future__ import annotations
 
@@ -12,7 +13,7 @@ import numpy as np
 from . import _lib
 
 __all__ = ["undirected_csr", "nested_dissection", "symbolic", "edge_arcs", "count_triangles",
-           "elimination_depth", "build_topology"]
+           "elimination_depth", "build_topology", "save_cache", "load_cache"]
 
 
 def _i64(a):
@@ -26,7 +27,7 @@ def _i32(a):
 def undirected_csr(n, off, tgt):
     """Returns (noff int64[n+1], nbrs int32[...], rev int64[...]); rev is the
     position of u in v's list, as in the reference (cch_nb.py:22-71)."""
-    lib = _lib.lib()
+    lib = _lib.host_lib()
     off, tgt = _i64(off), _i32(tgt)
     noff = np.empty(n + 1, np.int64)
     nbr_p, slots = C.c_void_p(), C.c_int64()
@@ -44,7 +45,7 @@ def undirected_csr(n, off, tgt):
 def nested_dissection(n, noff, nbrs, rev, x, y, leaf=64, threads=0):
     """rank[v] (int64, 0 = eliminated first); `rev` is accepted for signature
     compatibility with cch_nb.nested_dissection and not needed."""
-    lib = _lib.lib()
+    lib = _lib.host_lib()
     noff, nbrs = _i64(noff), _i32(nbrs)
     x = np.ascontiguousarray(x, dtype=np.float64)
     y = np.ascontiguousarray(y, dtype=np.float64)
@@ -56,7 +57,7 @@ def nested_dissection(n, noff, nbrs, rev, x, y, leaf=64, threads=0):
 
 def symbolic(n, noff, nbrs, rank):
     """(first int64[n+1], head int32[m+] sorted per row, parent int64[n])."""
-    lib = _lib.lib()
+    lib = _lib.host_lib()
     noff, nbrs, rank32 = _i64(noff), _i32(nbrs), _i32(rank)
     first = np.empty(n + 1, np.int64)
     parent = np.empty(n, np.int32)
@@ -69,7 +70,7 @@ def symbolic(n, noff, nbrs, rank):
 
 def edge_arcs(n, off, tgt, rank, first, head):
     """(e_arc int64[m] with -1 for self-loops, e_up int8[m])."""
-    lib = _lib.lib()
+    lib = _lib.host_lib()
     off, tgt, rank32, first, head = _i64(off), _i32(tgt), _i32(rank), _i64(first), _i32(head)
     m = int(off[n])
     e_arc = np.empty(m, np.int64)
@@ -132,3 +133,57 @@ def build_topology(g: dict, leaf: int = 64, rank=None, threads: int = 0) -> dict
     e_arc, e_up = edge_arcs(n, off, tgt, rank, first, head)
     return dict(n=n, rank=np.asarray(rank, np.int64), first=first, head=head, parent=parent,
                 e_arc=e_arc, e_up=e_up)
+
+
+# ------------------------------------------------------------ topology cache
+
+_GRAPH_KEYS = ("off", "tgt", "w", "L", "h", "x", "y")
+_TOPO_KEYS = ("rank", "first", "head", "parent", "e_arc", "e_up")
+
+
+def save_cache(path, key: str, g: dict, top: dict) -> bool:
+    """Writes a graph and its topology as uncompressed .npy files under `path`
+    (the role of the reference's rank_<name>.npy cache, python/run_nb.py:83-93,
+    extended to the contracted topology). `key` names what was built (graph
+    generator, size, seed, code version); a later load_cache with another key
+    misses. Returns False, leaving no partial cache, when the write fails
+    (a full disk is not an error of the caller)."""
+    import json
+    import shutil
+    from pathlib import Path
+    path = Path(path)
+    tmp = path.with_name(path.name + ".tmp")
+    try:
+        shutil.rmtree(tmp, ignore_errors=True)
+        tmp.mkdir(parents=True)
+        for k in _GRAPH_KEYS:
+            np.save(tmp / f"g_{k}.npy", np.asarray(g[k]))
+        for k in _TOPO_KEYS:
+            np.save(tmp / f"t_{k}.npy", np.asarray(top[k]))
+        meta = {"key": key, "n": int(g["n"]), "kind": g.get("kind"), "seed": g.get("seed")}
+        (tmp / "meta.json").write_text(json.dumps(meta))
+        shutil.rmtree(path, ignore_errors=True)
+        tmp.rename(path)
+        return True
+    except OSError:
+        shutil.rmtree(tmp, ignore_errors=True)
+        return False
+
+
+def load_cache(path, key: str):
+    """(g, top) from save_cache, or None when absent, unreadable or built under
+    another key."""
+    import json
+    from pathlib import Path
+    path = Path(path)
+    try:
+        meta = json.loads((path / "meta.json").read_text())
+        if meta.get("key") != key:
+            return None
+        g = {k: np.load(path / f"g_{k}.npy") for k in _GRAPH_KEYS}
+        g.update(n=int(meta["n"]), kind=meta.get("kind"), seed=meta.get("seed"))
+        top = {k: np.load(path / f"t_{k}.npy") for k in _TOPO_KEYS}
+        top["n"] = int(meta["n"])
+        return g, top
+    except (OSError, ValueError, KeyError):
+        return None

@@ -16,19 +16,22 @@ import numpy as np
 
 HERE = Path(__file__).resolve().parent
 LIB = HERE / "_ref" / "libcchref.so"
-REF_DIR = Path(os.environ.get("NWCCH_REFERENCE_DIR", "/root/reference"))
+# the reference checkout: NWCCH_REFERENCE_DIR names it (no default location)
+REF_DIR = Path(os.environ["NWCCH_REFERENCE_DIR"]) if os.environ.get("NWCCH_REFERENCE_DIR") else None
 
 _lib = None
 
 
 def available() -> bool:
-    return LIB.exists() or (REF_DIR / "cpp" / "cch.cpp").exists()
+    return LIB.exists() or (REF_DIR is not None and (REF_DIR / "cpp" / "cch.cpp").exists())
 
 
 def lib():
     global _lib
     if _lib is None:
         if not LIB.exists():
+            if REF_DIR is None:
+                raise RuntimeError("set NWCCH_REFERENCE_DIR to the reference checkout to build _ref/libcchref.so")
             subprocess.run(["make", "-s", "-C", str(HERE), "ref", f"REF_DIR={REF_DIR}"], check=True)
         L = C.CDLL(str(LIB))
         P, I64 = C.c_void_p, C.c_int64

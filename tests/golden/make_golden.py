@@ -1,6 +1,6 @@
 """Generates the golden fixtures in this directory from the REFERENCE's own code.
 
-    python tests/golden/make_golden.py [--reference /root/reference]
+    python tests/golden/make_golden.py --reference <reference checkout>
 
 Runs in a container that has the reference checkout; the fixtures it writes
 travel with the repository, the reference does not. Sources of truth:
@@ -53,6 +53,7 @@ import argparse
 import importlib
 import itertools
 import random
+import os
 import sys
 import types
 from pathlib import Path
@@ -539,9 +540,10 @@ def make_battery_long(R):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--reference", required=True, help="the reference checkout")
     ap.add_argument("--only", default="")
     args = ap.parse_args()
+    os.environ["NWCCH_REFERENCE_DIR"] = str(Path(args.reference).resolve())  # read by oracle/refcpp.py
     R = import_reference(Path(args.reference))
     makers = dict(techniques=make_techniques, family=make_family, grid64=make_grid64,
                   delaunay_negcycle=make_delaunay_negcycle, potential=make_potential, paths=make_paths,
