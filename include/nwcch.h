@@ -169,6 +169,12 @@ int nwcch_check(nwcch_topology* t, void* stream);
  * next update is exact. */
 #define NWCCH_TUNE_UPDATE_SPIN_LIMIT 14
 #define NWCCH_TUNE_TEST_BARRIER_EXTRA 15
+/* Batched queries (more than QUERY_CTA_MAX of them, int32 storage): the
+ * supernodes crossed by about this many chains of the batch or more (the top
+ * of the elimination tree) are swept as (min,+) products over tiles of up to
+ * 32 chains, the rest of each chain per warp; 0 sweeps every chain per warp.
+ * Default 64. */
+#define NWCCH_TUNE_QUERY_TOP_CHAINS 16
 int nwcch_tune_set(nwcch_topology* t, int key, int64_t value);
 int nwcch_tune_get(const nwcch_topology* t, int key, int64_t* value);
 

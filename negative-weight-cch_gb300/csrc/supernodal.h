@@ -127,6 +127,15 @@ template <class T>
 int query_sn_async(nwcch_topology* t, const T* up, const T* dn, const int32_t* s_rank, const int32_t* t_rank,
                    int64_t nq, int64_t* dist, cudaStream_t s, bool allow_alloc, bool* used);
 
+// Enqueues the batched query pipeline of query_top.cu (int32 storage): the
+// lower part of every chain per warp, the top supernodes as (min,+) products
+// over tiles of chains, the meet per query. Its kernels return at once when
+// the metric needs 64-bit labels (maxabs, on the device). *used = false when
+// the batch is not its case (nothing enqueued).
+int query_top_async(nwcch_topology* t, const int32_t* up, const int32_t* dn, const int32_t* s_rank,
+                    const int32_t* t_rank, int64_t nq, int64_t* dist, const unsigned int* maxabs, int* err,
+                    cudaStream_t s, bool* used);
+
 // The same through a CUDA graph captured once per (w, up, dn) binding and
 // error word (the slot of stream s) and replayed afterwards; when s is itself
 // being captured the launches are simply enqueued into the caller's capture.

@@ -33,6 +33,7 @@ int upload(nwcch_topology* t, const T* src, size_t count, T** dst) {
 void release(nwcch_topology* t) {
     if (t->free_plans) t->free_plans(t);
     if (t->free_battery_plan) t->free_battery_plan(t);
+    if (t->free_query_plans) t->free_query_plans(t);
     free_supernodal_plan(static_cast<SnPlan*>(t->sn_plan));
     t->sn_plan = nullptr;
     for (void* p : t->allocations) cudaFree(p);
@@ -261,6 +262,7 @@ int replan(nwcch_topology* t, const SnPlanParams& prm) {
     int rc = NWCCH_OK;
     SnPlan* P = build_supernodal_plan(n, first.data(), head.data(), parent.data(), prm, &rc);
     if (!P) return rc ? rc : NWCCH_ERR_NOMEM;
+    if (t->free_query_plans) t->free_query_plans(t);  // built over the old plan's supernodes
     auto* old = static_cast<SnPlan*>(t->sn_plan);
     if (old) t->device_bytes -= old->bytes;
     free_supernodal_plan(old);
@@ -322,6 +324,10 @@ extern "C" int nwcch_tune_set(nwcch_topology* t, int key, int64_t value) {
             if (value < 1) return NWCCH_ERR_ARG;
             t->tune.update_spin_limit = value;
             return NWCCH_OK;
+        case NWCCH_TUNE_QUERY_TOP_CHAINS:
+            if (value < 0) return NWCCH_ERR_ARG;
+            t->tune.query_top_chains = value;
+            return NWCCH_OK;
         case NWCCH_TUNE_TEST_BARRIER_EXTRA:
             if (value < 0 || value > 1024) return NWCCH_ERR_ARG;
             t->tune.test_barrier_extra = (int32_t)value;
@@ -359,6 +365,7 @@ extern "C" int nwcch_tune_get(const nwcch_topology* t, int key, int64_t* value) 
         case NWCCH_TUNE_UPDATE_DENSE_MIN: *value = t->tune.update_dense_min; return NWCCH_OK;
         case NWCCH_TUNE_UPDATE_SPIN_LIMIT: *value = t->tune.update_spin_limit; return NWCCH_OK;
         case NWCCH_TUNE_TEST_BARRIER_EXTRA: *value = t->tune.test_barrier_extra; return NWCCH_OK;
+        case NWCCH_TUNE_QUERY_TOP_CHAINS: *value = t->tune.query_top_chains; return NWCCH_OK;
         case NWCCH_TUNE_BATTERY_POOL: *value = t->tune.battery_pool; return NWCCH_OK;
         case NWCCH_TUNE_BATTERY_BUFFER: *value = t->tune.battery_buffer; return NWCCH_OK;
         case NWCCH_TUNE_SN_WARP_CAP:

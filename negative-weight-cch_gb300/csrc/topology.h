@@ -44,6 +44,8 @@ struct Tuning {
     int64_t update_dense_min = 0;           // updates of at least this many arcs skip the sweep (0: never)
     int64_t update_spin_limit = 1 << 24;    // spins (about 100 ns each) of one update barrier wait
     int32_t test_barrier_extra = 0;         // test hook: barrier waits for this many extra blocks
+    int64_t query_top_chains = 64;          // batched queries: top supernodes = those crossed by about this
+                                            // many chains of a batch (0: per-query kernels only)
     int64_t battery_pool = 0;               // initial battery piece pool (0: 1.5 pieces a direction)
     int32_t battery_buffer = 512;           // initial per-warp buffer of a long battery profile (pieces)
 };
@@ -82,6 +84,8 @@ struct nwcch_topology {
     std::mutex mu;                            // serialises lazily built plans
     void* plans = nullptr;                    // owned by the modules that build plans
     void (*free_plans)(nwcch_topology*) = nullptr;
+    void* query_plans = nullptr;              // query_top.cu: top-supernode plans of batched queries
+    void (*free_query_plans)(nwcch_topology*) = nullptr;
     void* battery_plan = nullptr;             // battery.cu: arcs in level order
     int64_t battery_pool_hint = 0;            // pieces of the largest battery customization so far (+1/8)
     void (*free_battery_plan)(nwcch_topology*) = nullptr;
