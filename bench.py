@@ -226,7 +226,12 @@ def run_ours(args, W, world):
     dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0")))
     torch.cuda.set_device(dev)
     top = W["top"]
-    T = DeviceTopology.from_dict(top)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    T = DeviceTopology.from_dict(top)  # upload + the derived arrays on the device + supernodal plan
+    torch.cuda.synchronize()
+    topo_s = time.perf_counter() - t0
+    log(f"topology handle: {topo_s:.2f}s")
     stream = torch.cuda.current_stream()
     w_step = W["w_bad"] if W["w_bad"] is not None else W["w"]
     w_host = torch.from_numpy(w_step).pin_memory()
@@ -370,9 +375,34 @@ def run_ours(args, W, world):
     good_host = good.to_numpy()
     bad_host = metric.to_numpy()  # the timed metric, compared with the oracle's in full
     return dict(T=T, tuned=tuned, cust_tuned=cust_tuned, cust_ms=cust_ms, q_ms=q_ms, wall=wall, plain_ms=plain_ms, plain_equal=same,
-                e2e_ms=e2e_ms, graph_q=graph_q, bad_host=bad_host, batch_dist=ref_d.cpu().numpy(),
+                e2e_ms=e2e_ms, graph_q=graph_q, bad_host=bad_host, batch_dist=ref_d.cpu().numpy(), topo_s=topo_s,
                 plain_q_ms=plain_q_ms, lat_dist=lat_dist, pot_ms=pot_ms, pot=pot.cpu().numpy(), good_host=good_host,
                 lat_us=lat, clocks=clocks.summary(), neg=neg_k, saturated=bool(sat))
+
+
+def scanned_arcs(top, qs, qt, sample: int = 1000) -> float:
+    """Mean arcs a query relaxes in the reference's ET sweep
+    (python/cch_nb.py:577-615: every arc out of every ancestor of s, then of
+    t), over the first `sample` pairs of the batch: the (min,+) relaxations
+    per query, walked supernode by supernode (a supernode's rows from the
+    entry row x hold first[last + 1] - first[x] arcs)."""
+    first = np.asarray(top["first"], np.int64)
+    parent = np.asarray(top["parent"], np.int64)
+    n = int(top["n"])
+    rl = np.diff(first)
+    join = np.zeros(n, bool)
+    join[1:] = (parent[:-1] == np.arange(1, n)) & (rl[:-1] == rl[1:] + 1)
+    sid = np.cumsum(~join) - 1
+    s0 = np.nonzero(~join)[0]
+    last = np.append(s0[1:], n) - 1
+    total = 0
+    k = min(sample, len(qs))
+    for x in np.concatenate([qs[:k], qt[:k]]).astype(np.int64):
+        while x >= 0:
+            S = sid[x]
+            total += int(first[last[S] + 1] - first[x])
+            x = int(parent[last[S]])
+    return total / max(1, k)
 
 
 def cpu_potential(W, good_host, pot_dev):
@@ -613,6 +643,45 @@ def run_batch(args, Wd, K):
             "partial_updates": updates, "update_schedule": upd_tuning, "parity": par}
 
 
+def run_batch_headline(args, W, K, single_ms):
+    """K metrics of the headline workload's topology customized in one batched
+    launch sequence (grid y = metric), against the single-metric time of the
+    timed step; metric 0 of the batch equal to its single customization."""
+    import torch
+
+    from nwcch import graphs as G
+    from nwcch.device import DeviceTopology
+    T = DeviceTopology.from_dict(W["top"])
+    stream = torch.cuda.current_stream()
+    Wk = G.scaled_metrics(W["g"], K, seed=11)
+    w_dev = torch.from_numpy(Wk).cuda()
+    del Wk
+    b = T.customize_batch(w_dev)
+    counts = T.negative_cycle_arcs_batch(b)
+    torch.cuda.synchronize()
+    times = []
+    for _ in range(max(3, min(args.steps, 5))):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        T.customize_batch(w_dev, out=b, sync=False)
+        T.negative_cycle_arcs_batch(b, out=counts)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1))
+    assert not T.check()
+    single = T.customize(w_dev[0].contiguous(), "int32")
+    equal = bool(torch.equal(single.up, b.up[0]) and torch.equal(single.dn, b.dn[0]))
+    assert equal, "batched customization differs from single customization"
+    bm = statistics.median(times)
+    out = {"workload": W["name"], "metrics": K, "batch_ms": round(bm, 3), "ms_per_metric": round(bm / K, 3),
+           "single_metric_ms": round(single_ms, 3), "speedup_per_metric": round(single_ms / (bm / K), 2),
+           "metric0_equal_single": equal, "negative_cycle_arcs": [int(c) for c in counts.cpu()],
+           "l2": "inputs larger than L2"}
+    del b, w_dev, single, T
+    torch.cuda.empty_cache()
+    return out
+
+
 def batch_parity(Wd, w0, arcs0, qs, qt, T, m):
     """Metric 0 of the batch as customized by the device equal to the
     oracle's level-parallel customization, and the device's answers on the
@@ -823,6 +892,8 @@ def main():
     ap.add_argument("--batch-metrics", type=int, default=64,
                     help="metrics of the batched customization (0: skip it)")
     ap.add_argument("--batch-workload", default="delaunay264k", choices=list(WORKLOADS))
+    ap.add_argument("--headline-batch-metrics", type=int, default=8,
+                    help="metrics of a batched customization on the headline workload (0: skip it)")
     ap.add_argument("--serve-workload", default="delaunay1m", choices=list(WORKLOADS) + ["none"])
     ap.add_argument("--serve-loads", default="1e4,1e5,1e6", help="offered query loads (queries/s)")
     ap.add_argument("--serve-seconds", type=float, default=1.0)
@@ -877,7 +948,10 @@ def main():
     if rank != 0:
         return
     # rank 0 only, after the timed replicas: the batched and serving sections
-    batch = serving = None
+    batch = serving = head_batch = None
+    if args.headline_batch_metrics > 0:
+        head_batch = run_batch_headline(args, W, args.headline_batch_metrics, statistics.median(R["cust_ms"]))
+        log(f"batched (headline workload): {head_batch}")
     if args.batch_metrics > 0:
         Wd = W if args.batch_workload == args.workload else make_workload(args.batch_workload, seed=0)
         batch = run_batch(args, Wd, args.batch_metrics)
@@ -906,6 +980,7 @@ def main():
     top = W["top"]
     B = algorithmic_bytes(top["n"], top["e_arc"].size, T.m_plus, T.triangles)
     achieved = B / (cust / 1000) / 1e9
+    arcs_q = scanned_arcs(top, W["qs"], W["qt"])
     cb = cpu_baseline(W, args.cpu_budget)
     parity = check_parity(W, cb, R["bad_host"], R["good_host"], R["batch_dist"], W["qs"], W["qt"],
                           args.parity_queries)
@@ -932,6 +1007,11 @@ def main():
         "plain_customize_ms": round(statistics.median(R["plain_ms"]), 3) if R["plain_ms"] else None,
         "plain_equals_supernodal": R["plain_equal"],
         "queries_per_s": round(nq / (qms / 1000) * world, 1), "query_batch_ms": round(qms, 4),
+        "query_work": {"arcs_per_query": round(arcs_q, 1), "sample": min(1000, nq),
+                       "relaxations_per_s": round(arcs_q * nq / (qms / 1000), 1),
+                       "note": "arcs of both ancestor chains (the reference's per-query relaxations); the batched "
+                               "form applies each top-supernode weight to a tile of up to 32 chains"},
+        "topology_handle_s": round(R["topo_s"], 3),
         "query_schedule": R["tuned"],
         "customize_schedule": R["cust_tuned"],
         "plain_queries_per_s": round(nq / (R["plain_q_ms"] / 1000) * world, 1),
@@ -964,6 +1044,7 @@ def main():
                       "cpu_ms": round(cp["ms"], 1), "cpu_cores": 1, "cpu_kind": "port of cpp/cch.cpp:631-655",
                       "equal": cp["equal"], "metric": "conservative (no injected cycle)"},
         "batched_customization": batch,
+        "batched_customization_headline": head_batch,
         "serving": serving,
         "battery": bat,
     }

@@ -103,9 +103,10 @@ int nwcch_emst_mask(int64_t n, int64_t m, const int64_t* eu, const int64_t* ev, 
 
 /* ------------------------------------------------------------------------
  * Device-resident topology. The reference passes first/head/parent/e_arc/
- * e_up to every call (python/cch_nb.py:529, 577); here they are validated,
- * extended (tails, levels, elimination-tree depths, downward lists) and
- * uploaded once.
+ * e_up to every call (python/cch_nb.py:529, 577) and derives what customize
+ * and query need from them in Python (cch_nb.py:431-515); here they are
+ * uploaded once, validated and extended on the device (tails, levels,
+ * elimination-tree depths, downward lists, original arcs per shortcut arc).
  * ---------------------------------------------------------------------- */
 
 typedef struct nwcch_topology nwcch_topology;
@@ -123,6 +124,26 @@ int nwcch_topology_destroy(nwcch_topology* t);
  * supernodal customization (after the two base-value launches), outgoing
  * arc ids stored. */
 int nwcch_topology_info(const nwcch_topology* t, int64_t* info, int64_t len);
+
+/* Copies one derived array of the handle into host memory `dst` of `count`
+ * elements (count must equal the array's length): what the device built
+ * from first/head/parent/e_arc, for inspection and tests (no counterpart in
+ * the reference, whose arrays are Python locals). */
+#define NWCCH_ARRAY_TAIL 0          /* int32[m+]: lower endpoint of every arc */
+#define NWCCH_ARRAY_DEPTH 1         /* int32[n]: elimination-tree depth (root 0) */
+#define NWCCH_ARRAY_HDEP 2          /* int32[m+]: depth of every arc's head */
+#define NWCCH_ARRAY_DOFF 3          /* int64[n+1]: downward lists, arcs grouped by head ... */
+#define NWCCH_ARRAY_DARC 4          /* int32[m+]:  ... ascending in the tail */
+#define NWCCH_ARRAY_LEVEL 5         /* int32[n]: 1 + max level of the lower neighbours (0: none) */
+#define NWCCH_ARRAY_AEOFF 6         /* int64[m+ + 1]: original arcs of every shortcut arc ... */
+#define NWCCH_ARRAY_AEIDX 7         /* int32[aeoff[m+]]: ... ascending arc id */
+#define NWCCH_ARRAY_LEVEL_VERTS 8   /* int32[n]: vertices by (level, rank) */
+#define NWCCH_ARRAY_LOOPS 9         /* int32[self-loops]: original arcs with e_arc = -1 */
+#define NWCCH_ARRAY_LEVEL_OFF 10    /* int64[levels+1]: into LEVEL_VERTS */
+#define NWCCH_ARRAY_LEVEL_ARCS 11   /* int64[levels+1]: arcs whose tail is on each level, prefix sums */
+#define NWCCH_ARRAY_LEVEL_TRI 12    /* int64[levels]: pull triangles landing on each level */
+#define NWCCH_ARRAY_LEVEL_MAXDEG 13 /* int32[levels]: longest row of each level */
+int nwcch_topology_export(const nwcch_topology* t, int which, void* dst, int64_t count);
 
 /* Reads and clears the error word of `stream`'s calls on `t` (synchronizes
  * `stream`). Each stream that enqueues work on a handle gets its own error
@@ -258,7 +279,10 @@ int nwcch_update_i64(nwcch_topology* t, int32_t* w_dev, int64_t* up_dev, int64_t
  * and Query::run (cpp/cch.cpp:549-575), batched: dist_dev[i] = distance from
  * rank s_rank_dev[i] to rank t_rank_dev[i] (NWCCH_INF64 if unreachable).
  * The caller-owned scratch df/dr/mark of the reference is not needed.
- * Synchronous.
+ * Synchronous. Batches of more than NWCCH_TUNE_QUERY_CTA_MAX queries sweep
+ * the top of the elimination tree as (min,+) products over tiles of chains
+ * (stream-ordered scratch of 8 bytes per query and depth level, in passes of
+ * at most 4 GB); smaller batches take a CTA per query.
  * ---------------------------------------------------------------------- */
 int nwcch_query_batch(nwcch_topology* t, const int32_t* up_dev, const int32_t* dn_dev,
                       const int32_t* s_rank_dev, const int32_t* t_rank_dev, int64_t nq,
@@ -268,8 +292,11 @@ int nwcch_query_batch_i64(nwcch_topology* t, const int64_t* up_dev, const int64_
                           const int32_t* s_rank_dev, const int32_t* t_rank_dev, int64_t nq,
                           int64_t* dist_dev, void* stream);
 /* Enqueue-only batch (python/cch_nb.py:577-615), for CUDA-graph capture and
- * pipelines: labels in shared memory, no allocation, no synchronization
- * (argument errors in the rank arrays surface at nwcch_check). Returns
+ * pipelines: no synchronization (argument errors in the rank arrays surface
+ * at nwcch_check); large batches take the (min,+) product form with
+ * stream-ordered scratch (cudaMallocAsync, which a capture records), once a
+ * call outside any capture has built its plan; otherwise labels in shared
+ * memory and no allocation. Returns
  * NWCCH_ERR_CAPACITY when the elimination tree is too deep for shared-memory
  * labels (about 10,000 levels); nwcch_query_batch then falls back to the
  * plain kernel. */

@@ -233,8 +233,9 @@ int query_sn_async(nwcch_topology* t, const T* up, const T* dn, const int32_t* s
                                                    : k_query_sn32<1, false>;
         const size_t cta_smem = (size_t)(((12 * Dp + 16) + 15) & ~15LL);
         bool top_used = false;
-        if (allow_alloc && nq > t->tune.query_cta_max) {
-            // large batch: the top of the tree as (min,+) products over chains
+        if (nq > t->tune.query_cta_max) {
+            // large batch: the top of the tree as (min,+) products over
+            // chains (stream-ordered scratch, also when enqueued only)
             const int rc = query_top_async(t, u32, d32, s_rank, t_rank, nq, dist, maxabs, err, s, &top_used);
             if (rc) return rc;
         }

@@ -51,7 +51,8 @@ namespace {
 
 constexpr int QT_THREADS = 256;           // threads of a top-supernode CTA
 constexpr int QT_MAX_CT = 32;             // chains in one tile
-constexpr int64_t QT_SMEM = 100 * 1024;   // label tile per CTA (two CTAs an SM)
+constexpr int64_t QT_SMEM = 100 * 1024;   // label tile per CTA (two CTAs an SM) ...
+constexpr int64_t QT_SMEM_MAX = 200 * 1024;  // ... or one, for the widest supernodes
 constexpr int64_t QL_SMEM = 200 * 1024;   // lower-sweep labels per block
 constexpr int64_t QT_LABEL_BYTES = (int64_t)4 << 30;  // label rows of one pass over a batch
 
@@ -68,8 +69,8 @@ struct TopDev {
 
 struct TopPlan {
     std::vector<int64_t> lvl_off;     // [levels + 1] into the level order
-    std::vector<int32_t> lvl_ct;      // chains per tile of each level
-    std::vector<int32_t> lvl_stride;  // label row stride: widest k + b of the level, rounded to 4
+    std::vector<int32_t> lvl_ct;      // chains per tile of each level (32, 16 or 8)
+    std::vector<int32_t> lvl_rows;    // most rows (k) of a supernode of the level
     int32_t* d_lvl_dfs = nullptr;     // [ntop] depth-first index of each entry in level order
     int32_t* d_ent_ct = nullptr;      // [ntop] chains per tile of each entry (level order)
     TopDev dev{};
@@ -242,21 +243,28 @@ int build_top_plan(nwcch_topology* t, QueryPlans* Q, int32_t log2_tau, TopPlan**
         const int32_t la = slvl[dfs_sn[a]], lb = slvl[dfs_sn[b]];
         return la != lb ? la < lb : a < b;
     });
+    // chains per tile: the most of 32, 16, 8 whose rows fit the shared
+    // memory budget ((ct + 4) x 4 bytes a row)
     std::vector<int32_t> ent_ct(ntop);
     for (int32_t i = 0; i < ntop;) {
-        int32_t j = i, wide = 0;
+        int32_t j = i, rows = 0;
         const int32_t l = slvl[dfs_sn[ent[i]]];
         while (j < ntop && slvl[dfs_sn[ent[j]]] == l) {
-            wide = std::max(wide, kk[dfs_sn[ent[j]]] + bb[dfs_sn[ent[j]]]);
+            rows = std::max(rows, kk[dfs_sn[ent[j]]]);
             j++;
         }
-        const int32_t stride = (wide + 3) & ~3;
-        const int64_t ct = std::min<int64_t>(QT_MAX_CT, QT_SMEM / (4 * (int64_t)stride));
-        if (ct < 1) T->usable = false;
+        int32_t ct = 0;
+        for (int32_t c : {32, 16, 8})
+            if (ct == 0 && (int64_t)(c + 4) * 4 * rows <= QT_SMEM) ct = c;
+        if (ct == 0 && (int64_t)(8 + 4) * 4 * rows <= QT_SMEM_MAX) ct = 8;
+        if (ct == 0) {
+            T->usable = false;
+            ct = 8;
+        }
         T->lvl_off.push_back(i);
-        T->lvl_ct.push_back((int32_t)std::max<int64_t>(1, ct));
-        T->lvl_stride.push_back(stride);
-        for (int32_t e = i; e < j; e++) ent_ct[e] = (int32_t)std::max<int64_t>(1, ct);
+        T->lvl_ct.push_back(ct);
+        T->lvl_rows.push_back(rows);
+        for (int32_t e = i; e < j; e++) ent_ct[e] = ct;
         i = j;
     }
     T->lvl_off.push_back(ntop);
@@ -474,19 +482,35 @@ __global__ void k_qscatter(DevTopo D, int64_t nq, int32_t nb, const int32_t* __r
     }
 }
 
-// Phase 2: the top supernodes of one level, a tile of chains per CTA.
-__global__ void __launch_bounds__(QT_THREADS) k_qtop(DevTopo D, SnDev S, TopDev T, const int32_t* __restrict__ up,
+// Phase 2: the top supernodes of one level, a tile of up to CT chains per
+// CTA. The tile's labels of S's rows live in shared memory row by row, the
+// tile's chains side by side (Ls[r * CTP + q], CTP = CT + 4 so that 16-byte
+// loads of different rows by the lanes of a warp hit different banks), and
+// one broadcast 16-byte load feeds four chains:
+//  (a) per 32-row block, the diagonal triangle: a warp per chain, four
+//      chains at a time, by shuffles;
+//  (b) the block's rows times the later rows' columns: a thread per column
+//      holding the block's 32 weights and the tile's CT accumulators in
+//      registers;
+//  (c) after the last block, the boundary columns: a thread per column, each
+//      row's weight read once and applied to the whole tile, the
+//      accumulators starting from and returning to the chains' global rows
+//      (boundary labels are outputs only, so they need no shared memory).
+template <int CT>
+__global__ void __launch_bounds__(QT_THREADS, 2) k_qtop(DevTopo D, SnDev S, TopDev T, const int32_t* __restrict__ up,
                                                      const int32_t* __restrict__ dn,
                                                      const int32_t* __restrict__ lvl_dfs, int64_t e_lo, int64_t e_hi,
                                                      const int64_t* __restrict__ tile_off,
                                                      const int32_t* __restrict__ boff,
                                                      const int32_t* __restrict__ order,
                                                      const int32_t* __restrict__ xin, int32_t* __restrict__ Lg,
-                                                     int64_t Dp, int64_t nq, int ct, int stride,
-                                                     const unsigned int* __restrict__ maxabs, int* __restrict__ err) {
+                                                     int64_t Dp, int64_t nq, const unsigned int* __restrict__ maxabs,
+                                                     int* __restrict__ err) {
+    static_assert(CT % 4 == 0 && CT <= QT_MAX_CT, "tile of 4k chains");
+    constexpr int CTP = CT + 4;
     if (!small_labels(D, maxabs)) return;
-    extern __shared__ __align__(16) int32_t Ls[];  // ct x stride labels
-    __shared__ int32_t s_chain[QT_MAX_CT], s_i0[QT_MAX_CT];
+    extern __shared__ __align__(16) int32_t Ls[];  // (k - r_lo) x CTP labels
+    __shared__ int32_t s_chain[CT], s_i0[CT];
     __shared__ int32_t s_imin;
     const int lane = threadIdx.x & 31, wq = threadIdx.x >> 5;
     const int32_t nb1 = T.ntop + 2;
@@ -502,16 +526,16 @@ __global__ void __launch_bounds__(QT_THREADS) k_qtop(DevTopo D, SnDev S, TopDev 
         const int dir = (int)(lo & 1);
         const int32_t d = lvl_dfs[lo >> 1];
         const int32_t sn = T.dfs_sn[d];
-        const int32_t s0 = S.s0[sn], k = S.k[sn], cols = k + S.b[sn];
+        const int32_t s0 = S.s0[sn], k = S.k[sn], b = S.b[sn], cols = k + b;
         const int32_t c_hi = boff[dir * nb1 + T.dfs_end[d]];
-        const int32_t first_c = boff[dir * nb1 + d] + (int32_t)(gt - tile_off[lo]) * ct;
-        const int nct = min(ct, c_hi - first_c);
+        const int32_t first_c = boff[dir * nb1 + d] + (int32_t)(gt - tile_off[lo]) * CT;
+        const int nct = min(CT, c_hi - first_c);
         const int32_t* __restrict__ W = dir ? dn : up;
         const int32_t d0 = D.depth[s0];
-        const int64_t bbase = D.first[s0 + k - 1];
+        const int64_t base0 = D.first[s0];
         if (threadIdx.x == 0) s_imin = k;
         __syncthreads();
-        if (threadIdx.x < QT_MAX_CT) {
+        if (threadIdx.x < CT) {
             int32_t c = -1, i0 = k;
             if (threadIdx.x < nct) {
                 c = order[dir * nq + first_c + threadIdx.x];
@@ -527,37 +551,32 @@ __global__ void __launch_bounds__(QT_THREADS) k_qtop(DevTopo D, SnDev S, TopDev 
             s_i0[threadIdx.x] = i0;
         }
         __syncthreads();
-        // the tile's labels: S's rows (no path below a chain's entry row),
-        // then the boundary
-        for (int idx = threadIdx.x; idx < nct * cols; idx += QT_THREADS) {
-            const int q = idx / cols, j = idx - q * cols;
-            const int32_t* Lc = Lg + (int64_t)s_chain[q] * Dp;
+        const int32_t r_lo = s_imin & ~31, nr = k - r_lo;
+        // rows r_lo.. of the tile's chains (no path below a chain's entry row,
+        // and in the columns of absent chains)
+        for (int idx = threadIdx.x; idx < CT * nr; idx += QT_THREADS) {
+            const int q = idx / nr, rr = idx - q * nr, r = r_lo + rr;
             int32_t v = Q32::CINF;
-            if (j < k) {
-                if (j >= s_i0[q]) v = Lc[d0 - j];
-            } else {
-                v = Lc[D.hdep[bbase + (j - k)]];
-            }
-            Ls[q * stride + j] = v;
+            if (q < nct && r >= s_i0[q]) v = Lg[(int64_t)s_chain[q] * Dp + (d0 - r)];
+            Ls[rr * CTP + q] = v;
         }
         __syncthreads();
-        for (int32_t c0 = s_imin & ~31; c0 < k; c0 += 32) {
+        // row r's arcs start at first[s0 + r] = base0 + r (cols - 1) - r (r - 1) / 2
+        auto rowb = [&](int32_t r) -> int64_t { return base0 + (int64_t)r * (cols - 1) - (int64_t)r * (r - 1) / 2; };
+        for (int32_t c0 = r_lo; c0 < k; c0 += 32) {
             const int n = min(32, k - c0);
-            const int64_t base = D.first[s0 + c0];
-            const int64_t step = cols - c0 - 1;  // length of row c0; rows shrink by one
-            // (a) the 32 x 32 diagonal triangle, a warp per chain (4 at once)
+            const int32_t cr = c0 - r_lo;
+            // (a) the 32 x 32 diagonal triangle
             if (wq < nct) {
                 int32_t u[31];
 #pragma unroll
                 for (int r = 0; r < 31; r++)
-                    u[r] = (r < lane && lane < n)
-                               ? Q32::w(W[base + (int64_t)r * step - (int64_t)r * (r - 1) / 2 + (lane - r - 1)])
-                               : Q32::CINF;
+                    u[r] = (r < lane && lane < n) ? Q32::w(W[rowb(c0 + r) + (lane - r - 1)]) : Q32::CINF;
                 int32_t lab[4];
 #pragma unroll
                 for (int m = 0; m < 4; m++) {
                     const int q = wq + 8 * m;
-                    lab[m] = (q < nct && lane < n) ? Ls[q * stride + c0 + lane] : Q32::CINF;
+                    lab[m] = (q < nct && lane < n) ? Ls[(cr + lane) * CTP + q] : Q32::CINF;
                 }
 #pragma unroll
                 for (int r = 0; r < 31; r++) {
@@ -568,60 +587,86 @@ __global__ void __launch_bounds__(QT_THREADS) k_qtop(DevTopo D, SnDev S, TopDev 
 #pragma unroll
                 for (int m = 0; m < 4; m++) {
                     const int q = wq + 8 * m;
-                    if (q < nct && lane < n) Ls[q * stride + c0 + lane] = Q32::norm(lab[m]);
+                    if (q < nct && lane < n) Ls[(cr + lane) * CTP + q] = Q32::norm(lab[m]);
                 }
             }
             __syncthreads();
-            // (b) the block's rows times every column to their right: each
-            // weight, read once, serves the tile's chains
-            const int32_t* Wb = W + base - c0 - 1;
-            const int32_t st = (int32_t)step - 1;
-            for (int32_t j = c0 + n + threadIdx.x; j < cols; j += QT_THREADS) {
-                int32_t wv[32];
-                int32_t ro = 0;
+            // (b) the block's rows times the later rows' columns
+            for (int32_t j = c0 + n + threadIdx.x; j < k; j += QT_THREADS) {
+                int32_t acc[CT];
+                int4* mine = reinterpret_cast<int4*>(Ls + (j - r_lo) * CTP);
 #pragma unroll
-                for (int r = 0; r < 32; r++) {
-                    wv[r] = r < n ? Q32::w(Wb[ro + j]) : Q32::CINF;
-                    ro += st - r;
+                for (int q4 = 0; q4 < CT / 4; q4++) {
+                    const int4 v = mine[q4];
+                    acc[4 * q4] = v.x;
+                    acc[4 * q4 + 1] = v.y;
+                    acc[4 * q4 + 2] = v.z;
+                    acc[4 * q4 + 3] = v.w;
                 }
-                if (n == 32) {
-                    for (int q = 0; q < nct; q++) {
-                        const int4* L4 = reinterpret_cast<const int4*>(Ls + q * stride + c0);
-                        int32_t acc = Q32::CINF;
+#pragma unroll 1
+                for (int g = 0; g < n; g += 8) {  // 8 rows' weights at a time
+                    int32_t wv[8];
 #pragma unroll
-                        for (int r4 = 0; r4 < 8; r4++) {
-                            const int4 l = L4[r4];
-                            acc = __viaddmin_s32(l.x, wv[4 * r4 + 0], acc);
-                            acc = __viaddmin_s32(l.y, wv[4 * r4 + 1], acc);
-                            acc = __viaddmin_s32(l.z, wv[4 * r4 + 2], acc);
-                            acc = __viaddmin_s32(l.w, wv[4 * r4 + 3], acc);
+                    for (int u = 0; u < 8; u++)
+                        wv[u] = g + u < n ? Q32::w(W[rowb(c0 + g + u) + (j - c0 - g - u - 1)]) : Q32::CINF;
+#pragma unroll
+                    for (int u = 0; u < 8; u++) {
+                        if (g + u < n) {
+                            const int4* row = reinterpret_cast<const int4*>(Ls + (cr + g + u) * CTP);
+#pragma unroll
+                            for (int q4 = 0; q4 < CT / 4; q4++) {
+                                const int4 l = row[q4];
+                                acc[4 * q4] = __viaddmin_s32(l.x, wv[u], acc[4 * q4]);
+                                acc[4 * q4 + 1] = __viaddmin_s32(l.y, wv[u], acc[4 * q4 + 1]);
+                                acc[4 * q4 + 2] = __viaddmin_s32(l.z, wv[u], acc[4 * q4 + 2]);
+                                acc[4 * q4 + 3] = __viaddmin_s32(l.w, wv[u], acc[4 * q4 + 3]);
+                            }
                         }
-                        int32_t* dst = Ls + q * stride + j;
-                        if (acc < *dst) *dst = acc;
-                    }
-                } else {
-                    for (int q = 0; q < nct; q++) {
-                        const int32_t* Lq = Ls + q * stride + c0;
-                        int32_t acc = Q32::CINF;
-#pragma unroll
-                        for (int r = 0; r < 32; r++)
-                            if (r < n) acc = __viaddmin_s32(Lq[r], wv[r], acc);
-                        int32_t* dst = Ls + q * stride + j;
-                        if (acc < *dst) *dst = acc;
                     }
                 }
+#pragma unroll
+                for (int q4 = 0; q4 < CT / 4; q4++)
+                    mine[q4] = make_int4(acc[4 * q4], acc[4 * q4 + 1], acc[4 * q4 + 2], acc[4 * q4 + 3]);
             }
             __syncthreads();
         }
-        for (int idx = threadIdx.x; idx < nct * cols; idx += QT_THREADS) {
-            const int q = idx / cols, j = idx - q * cols;
-            int32_t* Lc = Lg + (int64_t)s_chain[q] * Dp;
-            const int32_t v = Q32::norm(Ls[q * stride + j]);
-            if (j < k) {
-                if (j >= s_i0[q]) Lc[d0 - j] = v;
-            } else {
-                Lc[D.hdep[bbase + (j - k)]] = v;
+        // (c) the boundary columns, from every row of the tile
+        const int64_t bbase = rowb(k - 1);
+        for (int32_t jb = threadIdx.x; jb < b; jb += QT_THREADS) {
+            const int32_t j = k + jb;
+            const int32_t hd = D.hdep[bbase + jb];
+            int32_t acc[CT];
+#pragma unroll
+            for (int q = 0; q < CT; q++) acc[q] = q < nct ? Lg[(int64_t)s_chain[q] * Dp + hd] : Q32::CINF;
+#pragma unroll 1
+            for (int32_t r0 = r_lo; r0 < k; r0 += 8) {
+                int32_t wv[8];
+#pragma unroll
+                for (int u = 0; u < 8; u++)
+                    wv[u] = r0 + u < k ? Q32::w(W[rowb(r0 + u) + (j - r0 - u - 1)]) : Q32::CINF;
+#pragma unroll
+                for (int u = 0; u < 8; u++) {
+                    if (r0 + u < k) {
+                        const int4* row = reinterpret_cast<const int4*>(Ls + (r0 + u - r_lo) * CTP);
+#pragma unroll
+                        for (int q4 = 0; q4 < CT / 4; q4++) {
+                            const int4 l = row[q4];
+                            acc[4 * q4] = __viaddmin_s32(l.x, wv[u], acc[4 * q4]);
+                            acc[4 * q4 + 1] = __viaddmin_s32(l.y, wv[u], acc[4 * q4 + 1]);
+                            acc[4 * q4 + 2] = __viaddmin_s32(l.z, wv[u], acc[4 * q4 + 2]);
+                            acc[4 * q4 + 3] = __viaddmin_s32(l.w, wv[u], acc[4 * q4 + 3]);
+                        }
+                    }
+                }
             }
+#pragma unroll
+            for (int q = 0; q < CT; q++)
+                if (q < nct) Lg[(int64_t)s_chain[q] * Dp + hd] = Q32::norm(acc[q]);
+        }
+        // the rows back to the chains' global rows
+        for (int idx = threadIdx.x; idx < nct * nr; idx += QT_THREADS) {
+            const int q = idx / nr, rr = idx - q * nr, r = r_lo + rr;
+            if (r >= s_i0[q]) Lg[(int64_t)s_chain[q] * Dp + (d0 - r)] = Q32::norm(Ls[rr * CTP + q]);
         }
         __syncthreads();
     }
@@ -658,7 +703,11 @@ __global__ void __launch_bounds__(256) k_qmeet(DevTopo D, SnDev S, TopDev T, int
     }
 }
 
-int get_top_plan(nwcch_topology* t, int32_t log2_tau, TopPlan** out) {
+// The plan of a threshold, built on first use; with lookup_only (a stream
+// being captured, where the build's copies are not allowed) *out stays null
+// when it is not built yet.
+int get_top_plan(nwcch_topology* t, int32_t log2_tau, bool lookup_only, TopPlan** out) {
+    *out = nullptr;
     std::lock_guard<std::mutex> lock(t->mu);
     if (!t->query_plans) {
         t->query_plans = new (std::nothrow) QueryPlans();
@@ -672,6 +721,7 @@ int get_top_plan(nwcch_topology* t, int32_t log2_tau, TopPlan** out) {
         *out = it->second.get();
         return NWCCH_OK;
     }
+    if (lookup_only) return NWCCH_OK;
     return build_top_plan(t, Q, log2_tau, out);
 }
 
@@ -709,10 +759,12 @@ int query_top_async(nwcch_topology* t, const int32_t* up, const int32_t* dn, con
     const int64_t tau = std::max<int64_t>(2, (min_chains * t->d.n) / (2 * chunk));
     int32_t log2_tau = 1;
     while (((int64_t)1 << (log2_tau + 1)) <= tau) log2_tau++;
+    cudaStreamCaptureStatus capture = cudaStreamCaptureStatusNone;
+    NWCCH_CUDA_TRY(cudaStreamIsCapturing(s, &capture));
     TopPlan* T = nullptr;
-    int rc = get_top_plan(t, log2_tau, &T);
+    int rc = get_top_plan(t, log2_tau, capture != cudaStreamCaptureStatusNone, &T);
     if (rc) return rc;
-    if (!T->usable) return NWCCH_OK;
+    if (!T || !T->usable) return NWCCH_OK;
     const auto* P = static_cast<SnPlan*>(t->sn_plan);
     const TopDev& TD = T->dev;
     const int32_t ntop = TD.ntop, nb = ntop + 1;
@@ -754,12 +806,25 @@ int query_top_async(nwcch_topology* t, const int32_t* up, const int32_t* dn, con
         k_qscatter<<<(unsigned)std::max<int64_t>(1, std::min<int64_t>((2 * m + 255) / 256, (int64_t)sms * 8)), 256, 0,
                      s>>>(t->d, m, nb, key, boff, fill, order, maxabs, err);
         for (size_t l = 0; l + 1 < T->lvl_off.size(); l++) {
-            const int ct = T->lvl_ct[l], stride = T->lvl_stride[l];
-            const size_t tsmem = (size_t)ct * stride * 4;
-            if ((rc = occupancy_grid(k_qtop, QT_THREADS, tsmem, (int64_t)sms * 64, sms, &blocks))) break;
-            k_qtop<<<(unsigned)blocks, QT_THREADS, tsmem, s>>>(t->d, P->dev, TD, up, dn, T->d_lvl_dfs,
-                                                               2 * T->lvl_off[l], 2 * T->lvl_off[l + 1], tile_off,
-                                                               boff, order, xin, Lg, Dp, m, ct, stride, maxabs, err);
+            const int ct = T->lvl_ct[l];
+            const size_t tsmem = (size_t)(ct + 4) * 4 * std::max<int32_t>(1, T->lvl_rows[l]);
+            const int64_t e0 = 2 * T->lvl_off[l], e1 = 2 * T->lvl_off[l + 1];
+            if (ct == 32) {
+                if ((rc = occupancy_grid(k_qtop<32>, QT_THREADS, tsmem, (int64_t)sms * 64, sms, &blocks))) break;
+                k_qtop<32><<<(unsigned)blocks, QT_THREADS, tsmem, s>>>(t->d, P->dev, TD, up, dn, T->d_lvl_dfs, e0, e1,
+                                                                       tile_off, boff, order, xin, Lg, Dp, m, maxabs,
+                                                                       err);
+            } else if (ct == 16) {
+                if ((rc = occupancy_grid(k_qtop<16>, QT_THREADS, tsmem, (int64_t)sms * 64, sms, &blocks))) break;
+                k_qtop<16><<<(unsigned)blocks, QT_THREADS, tsmem, s>>>(t->d, P->dev, TD, up, dn, T->d_lvl_dfs, e0, e1,
+                                                                       tile_off, boff, order, xin, Lg, Dp, m, maxabs,
+                                                                       err);
+            } else {
+                if ((rc = occupancy_grid(k_qtop<8>, QT_THREADS, tsmem, (int64_t)sms * 64, sms, &blocks))) break;
+                k_qtop<8><<<(unsigned)blocks, QT_THREADS, tsmem, s>>>(t->d, P->dev, TD, up, dn, T->d_lvl_dfs, e0, e1,
+                                                                      tile_off, boff, order, xin, Lg, Dp, m, maxabs,
+                                                                      err);
+            }
         }
         if (rc) break;
         k_qmeet<<<(unsigned)std::max<int64_t>(1, std::min<int64_t>((m + 7) / 8, (int64_t)sms * 16)), 256, 0, s>>>(

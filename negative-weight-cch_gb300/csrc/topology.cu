@@ -1,7 +1,7 @@
-// Topology handle: validates the upward CSR produced by the host-side
-// preprocessing, derives the structures the kernels need (tails, levels,
-// elimination-tree depths, downward lists, arc -> original-arc index) and
-// uploads everything once. Customization, scans, updates and queries for any
+// Topology handle: uploads the upward CSR produced by the host-side
+// preprocessing once, validates it and derives the structures the kernels
+// need (tails, levels, elimination-tree depths, downward lists, arc ->
+// original-arc index) on the device (topology_build.cu). Customization, scans, updates and queries for any
 // number of metrics then run against this resident copy.
 
 #include <algorithm>
@@ -12,10 +12,22 @@
 #include "common.cuh"
 #include "supernodal.h"
 #include "topology.h"
+#include "topology_build.h"
 
 namespace nwcch {
 
 namespace {
+
+template <class T>
+int alloc(nwcch_topology* t, int64_t count, T** dst) {
+    void* p = nullptr;
+    const size_t bytes = (size_t)std::max<int64_t>(1, count) * sizeof(T);
+    if (cudaMalloc(&p, bytes) != cudaSuccess) return NWCCH_ERR_NOMEM;
+    t->allocations.push_back(p);
+    t->device_bytes += bytes;
+    *dst = static_cast<T*>(p);
+    return NWCCH_OK;
+}
 
 template <class T>
 int upload(nwcch_topology* t, const T* src, size_t count, T** dst) {
@@ -81,19 +93,10 @@ extern "C" int nwcch_topology_create(int64_t n, const int64_t* first, const int3
     const int64_t mp = first[n];
     if (first[0] != 0 || mp < 0 || mp >= INT32_MAX || (mp > 0 && !head) || m >= INT32_MAX)
         return NWCCH_ERR_TOPOLOGY;
-    // rows: strictly increasing heads above the tail; parent = lowest head
-    for (int64_t x = 0; x < n; x++) {
+    // row offsets ascend (the device checks every row: heads strictly
+    // increasing above the tail, parent = lowest head, arc map in range)
+    for (int64_t x = 0; x < n; x++)
         if (first[x + 1] < first[x]) return NWCCH_ERR_TOPOLOGY;
-        int64_t prev = x;
-        for (int64_t a = first[x]; a < first[x + 1]; a++) {
-            if (head[a] <= prev || head[a] >= n) return NWCCH_ERR_TOPOLOGY;
-            prev = head[a];
-        }
-        const int32_t p = first[x + 1] > first[x] ? head[first[x]] : -1;
-        if (parent[x] != p) return NWCCH_ERR_TOPOLOGY;
-    }
-    for (int64_t k = 0; k < m; k++)
-        if (e_arc[k] < -1 || e_arc[k] >= mp) return NWCCH_ERR_TOPOLOGY;
 
     int dev = 0, sms = 0;
     NWCCH_CUDA_TRY(cudaGetDevice(&dev));
@@ -105,119 +108,60 @@ extern "C" int nwcch_topology_create(int64_t n, const int64_t* first, const int3
     t->tune.query_cta_wide_max = t->sms;
     int rc = NWCCH_OK;
     do {
-        std::vector<int32_t> tail(mp), depth(n, 0), hdep(mp), lvl(n, 0);
-        int64_t tri = 0;
-        int32_t maxdeg = 0;
-        for (int64_t x = 0; x < n; x++) {
-            const int64_t d = first[x + 1] - first[x];
-            tri += d * (d - 1) / 2;
-            maxdeg = std::max<int32_t>(maxdeg, (int32_t)d);
-            for (int64_t a = first[x]; a < first[x + 1]; a++) {
-                tail[a] = (int32_t)x;
-                lvl[head[a]] = std::max(lvl[head[a]], lvl[x] + 1);
-            }
-        }
-        int32_t maxd = 0;
-        for (int64_t x = n - 1; x >= 0; x--)
-            if (parent[x] >= 0) {
-                depth[x] = depth[parent[x]] + 1;
-                maxd = std::max(maxd, depth[x]);
-            }
-        for (int64_t a = 0; a < mp; a++) hdep[a] = depth[head[a]];
-        // downward lists, ascending in the tail (arc ids grow with the tail)
-        std::vector<int64_t> doff(n + 1, 0);
-        for (int64_t a = 0; a < mp; a++) doff[head[a] + 1]++;
-        for (int64_t v = 0; v < n; v++) doff[v + 1] += doff[v];
-        std::vector<int32_t> darc(mp);
-        {
-            std::vector<int64_t> fill(doff.begin(), doff.end() - 1);
-            for (int64_t a = 0; a < mp; a++) darc[fill[head[a]]++] = (int32_t)a;
-        }
-        // levels: vertices bucketed by level, stable in rank
-        int32_t L = 0;
-        for (int64_t x = 0; x < n; x++) L = std::max(L, lvl[x] + 1);
-        t->levels = L;
-        t->level_off.assign(L + 1, 0);
-        for (int64_t x = 0; x < n; x++) t->level_off[lvl[x] + 1]++;
-        for (int32_t l = 0; l < L; l++) t->level_off[l + 1] += t->level_off[l];
-        std::vector<int32_t> lverts(n);
-        t->level_maxdeg.assign(L, 0);
-        t->level_tri.assign(L, 0);
-        t->level_arc_off.assign(L + 1, 0);
-        {
-            std::vector<int64_t> fill(t->level_off.begin(), t->level_off.end() - 1);
-            for (int64_t x = 0; x < n; x++) {
-                const int32_t l = lvl[x];
-                lverts[fill[l]++] = (int32_t)x;
-                t->level_maxdeg[l] = std::max<int32_t>(t->level_maxdeg[l], (int32_t)(first[x + 1] - first[x]));
-                t->level_arc_off[l + 1] += first[x + 1] - first[x];
-            }
-        }
-        for (int32_t l = 0; l < L; l++) t->level_arc_off[l + 1] += t->level_arc_off[l];
-        for (int64_t a = 0; a < mp; a++) {
-            const int64_t x = tail[a];
-            t->level_tri[lvl[head[a]]] += first[x + 1] - a - 1;  // pull work lands on the head's level
-        }
-        // original arcs mapped onto each shortcut arc, and the self-loops
-        std::vector<int64_t> aeoff(mp + 1, 0);
-        std::vector<int32_t> loops;
-        for (int64_t k = 0; k < m; k++) {
-            if (e_arc[k] >= 0) aeoff[e_arc[k] + 1]++;
-            else loops.push_back((int32_t)k);
-        }
-        for (int64_t a = 0; a < mp; a++) aeoff[a + 1] += aeoff[a];
-        std::vector<int32_t> aeidx(aeoff[mp]);
-        {
-            std::vector<int64_t> fill(aeoff.begin(), aeoff.end() - 1);
-            for (int64_t k = 0; k < m; k++)
-                if (e_arc[k] >= 0) aeidx[fill[e_arc[k]]++] = (int32_t)k;
-        }
-        t->sn_plan = build_supernodal_plan(n, first, head, parent, SnPlanParams{}, &rc);
-        if (rc) break;
-        t->device_bytes += static_cast<SnPlan*>(t->sn_plan)->bytes;
-        t->triangles = tri;
-        t->max_deg = maxdeg;
-        t->nloops = (int64_t)loops.size();
         DevTopo& d = t->d;
         d.n = n;
         d.m_plus = mp;
         d.m = m;
-        d.max_depth = maxd;
         int64_t* p64;
         int32_t* p32;
         int8_t* p8;
+        // the inputs, then everything derived from them on the device
         if ((rc = upload(t, first, n + 1, &p64))) break;
         d.first = p64;
         if ((rc = upload(t, head, mp, &p32))) break;
         d.head = p32;
         if ((rc = upload(t, parent, n, &p32))) break;
         d.parent = p32;
-        if ((rc = upload(t, depth.data(), n, &p32))) break;
-        d.depth = p32;
-        if ((rc = upload(t, hdep.data(), mp, &p32))) break;
-        d.hdep = p32;
-        if ((rc = upload(t, tail.data(), mp, &p32))) break;
-        d.tail = p32;
-        if ((rc = upload(t, doff.data(), n + 1, &p64))) break;
-        d.doff = p64;
-        if ((rc = upload(t, darc.data(), mp, &p32))) break;
-        d.darc = p32;
-        if ((rc = upload(t, lvl.data(), n, &p32))) break;
-        d.vlevel = p32;
         if ((rc = upload(t, e_arc, m, &p64))) break;
         d.e_arc = p64;
         if ((rc = upload(t, e_up, m, &p8))) break;
         d.e_up = p8;
-        if ((rc = upload(t, aeoff.data(), mp + 1, &p64))) break;
-        d.aeoff = p64;
-        if ((rc = upload(t, aeidx.data(), aeidx.size(), &p32))) break;
-        d.aeidx = p32;
-        if ((rc = upload(t, loops.data(), loops.size(), &p32))) break;
-        t->loops = p32;
-        if ((rc = upload(t, lverts.data(), n, &p32))) break;
-        t->level_verts = p32;
+        DerivedTopology D;
+        if ((rc = alloc(t, mp, &D.tail)) || (rc = alloc(t, n, &D.depth)) || (rc = alloc(t, mp, &D.hdep)) ||
+            (rc = alloc(t, n + 1, &D.doff)) || (rc = alloc(t, mp, &D.darc)) || (rc = alloc(t, n, &D.vlevel)) ||
+            (rc = alloc(t, mp + 1, &D.aeoff)) || (rc = alloc(t, n, &D.level_verts)))
+            break;
+        rc = derive_topology(n, mp, m, d.first, d.head, d.parent, d.e_arc, &D);
+        if (D.aeidx_sorted) {
+            t->allocations.push_back(D.aeidx_sorted);
+            t->device_bytes += (size_t)std::max<int64_t>(1, m) * sizeof(int32_t);
+        }
+        if (rc) break;
+        d.tail = D.tail;
+        d.depth = D.depth;
+        d.hdep = D.hdep;
+        d.doff = D.doff;
+        d.darc = D.darc;
+        d.vlevel = D.vlevel;
+        d.aeoff = D.aeoff;
+        d.aeidx = D.aeidx_sorted;
+        d.max_depth = D.max_depth;
+        t->loops = D.aeidx_sorted + (m - D.nloops);
+        t->nloops = D.nloops;
+        t->level_verts = D.level_verts;
+        t->triangles = D.triangles;
+        t->max_deg = D.max_deg;
+        t->levels = D.levels;
+        t->level_off = std::move(D.level_off);
+        t->level_arc_off = std::move(D.level_arc_off);
+        t->level_tri = std::move(D.level_tri);
+        t->level_maxdeg = std::move(D.level_maxdeg);
         if ((rc = upload(t, t->level_arc_off.data(), t->level_arc_off.size(), &p64))) break;
         t->d_level_arc_off = p64;
+        // the supernodal plan, from the caller's host arrays (validated above)
+        t->sn_plan = build_supernodal_plan(n, first, head, parent, SnPlanParams{}, &rc);
+        if (rc) break;
+        t->device_bytes += static_cast<SnPlan*>(t->sn_plan)->bytes;
         // per-stream slots: 256 bytes each, the error word first and the
         // 16 counters from byte 128
         const std::vector<int64_t> zeros((size_t)kStreamSlots * 32, 0);
@@ -396,5 +340,41 @@ extern "C" int nwcch_topology_info(const nwcch_topology* t, int64_t* info, int64
         info[10] = p ? (int64_t)p->launches.size() : 0;
         info[11] = p ? p->rel_entries : 0;
     }
+    return NWCCH_OK;
+}
+
+extern "C" int nwcch_topology_export(const nwcch_topology* t, int which, void* dst, int64_t count) {
+    if (!t || !dst || count < 0) return NWCCH_ERR_ARG;
+    const DevTopo& d = t->d;
+    const int64_t mp = d.m_plus, n = d.n;
+    const void* src = nullptr;
+    int64_t len = 0;
+    size_t elem = 4;
+    const void* host = nullptr;
+    switch (which) {
+        case NWCCH_ARRAY_TAIL: src = d.tail; len = mp; break;
+        case NWCCH_ARRAY_DEPTH: src = d.depth; len = n; break;
+        case NWCCH_ARRAY_HDEP: src = d.hdep; len = mp; break;
+        case NWCCH_ARRAY_DOFF: src = d.doff; len = n + 1; elem = 8; break;
+        case NWCCH_ARRAY_DARC: src = d.darc; len = mp; break;
+        case NWCCH_ARRAY_LEVEL: src = d.vlevel; len = n; break;
+        case NWCCH_ARRAY_AEOFF: src = d.aeoff; len = mp + 1; elem = 8; break;
+        case NWCCH_ARRAY_AEIDX: src = d.aeidx; len = d.m - t->nloops; break;
+        case NWCCH_ARRAY_LEVEL_VERTS: src = t->level_verts; len = n; break;
+        case NWCCH_ARRAY_LOOPS: src = t->loops; len = t->nloops; break;
+        case NWCCH_ARRAY_LEVEL_OFF: host = t->level_off.data(); len = (int64_t)t->level_off.size(); elem = 8; break;
+        case NWCCH_ARRAY_LEVEL_ARCS:
+            host = t->level_arc_off.data(); len = (int64_t)t->level_arc_off.size(); elem = 8; break;
+        case NWCCH_ARRAY_LEVEL_TRI: host = t->level_tri.data(); len = (int64_t)t->level_tri.size(); elem = 8; break;
+        case NWCCH_ARRAY_LEVEL_MAXDEG: host = t->level_maxdeg.data(); len = (int64_t)t->level_maxdeg.size(); break;
+        default: return NWCCH_ERR_ARG;
+    }
+    if (count != len) return NWCCH_ERR_ARG;
+    if (len == 0) return NWCCH_OK;
+    if (host) {
+        std::memcpy(dst, host, (size_t)len * elem);
+        return NWCCH_OK;
+    }
+    NWCCH_CUDA_TRY(cudaMemcpy(dst, src, (size_t)len * elem, cudaMemcpyDeviceToHost));
     return NWCCH_OK;
 }

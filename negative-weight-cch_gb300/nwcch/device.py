@@ -22,6 +22,7 @@ for _name, _args in {
     "nwcch_topology_create": [I64, P, P, P, I64, P, P, PP],
     "nwcch_topology_destroy": [P],
     "nwcch_topology_info": [P, P, I64],
+    "nwcch_topology_export": [P, C.c_int, P, I64],
     "nwcch_check": [P, P],
     "nwcch_customize": [P, P, P, P, P],
     "nwcch_customize_async": [P, P, P, P, P],
@@ -165,6 +166,28 @@ class DeviceTopology:
         (self.n, self.m_plus, self.m, self.triangles, self.levels, self.depth, self.max_row,
          self.device_bytes, self.supernodes, self.sn_levels, self.sn_launches,
          self.rel_entries) = (int(v) for v in info)
+
+    # name -> (key, dtype, length from the handle's figures)
+    _ARRAYS = {"tail": (0, np.int32), "depth": (1, np.int32), "hdep": (2, np.int32), "doff": (3, np.int64),
+               "darc": (4, np.int32), "level": (5, np.int32), "aeoff": (6, np.int64), "aeidx": (7, np.int32),
+               "level_verts": (8, np.int32), "loops": (9, np.int32), "level_off": (10, np.int64),
+               "level_arcs": (11, np.int64), "level_tri": (12, np.int64), "level_maxdeg": (13, np.int32)}
+
+    def export(self, name: str) -> np.ndarray:
+        """A derived array of the handle (built on the device from first,
+        head, parent and e_arc), copied to host memory."""
+        key, dt = self._ARRAYS[name]
+        if name in ("aeidx", "loops"):
+            aeoff = self.export("aeoff")
+            length = int(aeoff[-1]) if name == "aeidx" else self.m - int(aeoff[-1])
+        else:
+            length = {"tail": self.m_plus, "depth": self.n, "hdep": self.m_plus, "doff": self.n + 1,
+                      "darc": self.m_plus, "level": self.n, "aeoff": self.m_plus + 1, "level_verts": self.n,
+                      "level_off": self.levels + 1, "level_arcs": self.levels + 1, "level_tri": self.levels,
+                      "level_maxdeg": self.levels}[name]
+        out = np.empty(max(length, 1), dt)
+        _lib.check(_lib.lib().nwcch_topology_export(self.handle, key, _lib.ptr(out), length), "topology_export")
+        return out[:length]
 
     @classmethod
     def from_dict(cls, t: dict) -> "DeviceTopology":

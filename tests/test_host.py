@@ -330,13 +330,14 @@ def test_ev_energies_are_conservative(oracle):
 
 
 def test_topology_create_rejects_bad_input_without_gpu(built_lib):
-    """Validation happens on the host before any device allocation."""
+    """The row offsets are checked on the host before any device work (the
+    rows themselves on the device: tests/test_gpu_topology_build.py)."""
     import ctypes as C
 
     from nwcch import _lib
-    first = np.array([0, 1, 1], np.int64)
-    head = np.array([0], np.int32)      # head must lie above its tail
-    parent = np.array([0, -1], np.int32)
+    first = np.array([0, 1, 0], np.int64)  # row offsets must not decrease
+    head = np.array([1], np.int32)
+    parent = np.array([1, -1], np.int32)
     e_arc = np.zeros(0, np.int64)
     e_up = np.zeros(0, np.int8)
     h = C.c_void_p()
