@@ -1014,7 +1014,7 @@ int run_levels(nwcch_topology* t, nwcch_battery* b, const BatPlan* P, const doub
     BatArgs A{w,    K,     P->arcs, P->dtail,    b->cnt,    b->pos,   b->pool,
               b->pool_cap, gbuf, tri, P->max_down, gcap, b->status, next};
     const size_t smem = sizeof(WarpStage) * LEVEL_WARPS;
-    NWCCH_CUDA_TRY(cudaFuncSetAttribute(k_bat_level, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    NWCCH_CUDA_TRY(allow_dynamic_smem((const void*)k_bat_level, smem));
     for (int32_t l = 0; l < t->levels; l++) {
         const int64_t a0 = t->level_arc_off[l], a1 = t->level_arc_off[l + 1];
         if (a1 == a0) continue;

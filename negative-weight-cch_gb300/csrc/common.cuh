@@ -4,6 +4,10 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <map>
+#include <mutex>
+#include <utility>
+
 #include "nwcch.h"
 
 namespace nwcch {
@@ -128,6 +132,34 @@ inline int device_sms() {
     if (dev >= 0 && dev < 64) cache[dev] = sms;
     return sms;
 }
+
+// Raises the dynamic shared memory limit of `kernel` on the current device to
+// at least `bytes`; never lowers it. The limit is a property of the function,
+// shared by every host thread: if one thread could lower it between another
+// thread's setting and launch, that launch would be refused. Growing it only
+// keeps every concurrent launch valid (a launch's occupancy follows the
+// shared memory it requests, not this limit).
+inline cudaError_t allow_dynamic_smem(const void* kernel, size_t bytes) {
+    static std::mutex mu;
+    static std::map<std::pair<const void*, int>, size_t> granted;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> lock(mu);
+    size_t& g = granted[{kernel, dev}];
+    if (bytes <= g) return cudaSuccess;
+    e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (e == cudaSuccess) g = bytes;
+    return e;
+}
+
+// Set-up copies and fills issued with the host-synchronous calls (cudaMemcpy
+// from pageable memory, cudaMemset) run on the legacy default stream and may
+// still be in flight when the call returns: a pageable upload returns once its
+// data is staged, a fill returns at once. Work that a caller enqueues on a
+// non-blocking stream is not ordered after them, so every builder of device
+// arrays waits for them before the arrays can be used on any stream.
+inline cudaError_t setup_copies_done() { return cudaStreamSynchronize(cudaStreamLegacy); }
 
 #define NWCCH_CUDA_TRY(expr)                            \
     do {                                                \

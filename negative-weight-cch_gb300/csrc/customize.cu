@@ -167,7 +167,7 @@ int customize_plain(nwcch_topology* t, const int32_t* w, T* up, T* dn, cudaStrea
     int rc = base_init<T>(t, w, up, dn, s, err);
     if (rc) return rc;
     const int max_smem = 227 * 1024;
-    NWCCH_CUDA_TRY(cudaFuncSetAttribute(k_pull_rows<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
+    NWCCH_CUDA_TRY(allow_dynamic_smem((const void*)k_pull_rows<T>, (size_t)max_smem));
     for (int32_t l = 1; l < t->levels; l++) {
         if (t->level_tri[l] == 0) continue;
         const int64_t v0 = t->level_off[l], nv = t->level_off[l + 1] - v0;

@@ -192,7 +192,7 @@ static bool sn_query_shape(const nwcch_topology* t, int64_t bytes_per_pos, int* 
 
 template <class K>
 static int launch_shape(K kernel, int warps, size_t smem, int64_t nq, int64_t* blocks) {
-    NWCCH_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    NWCCH_CUDA_TRY(allow_dynamic_smem((const void*)kernel, smem));
     int dev = 0, sms = 0, per_sm = 0;
     NWCCH_CUDA_TRY(cudaGetDevice(&dev));
     NWCCH_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));

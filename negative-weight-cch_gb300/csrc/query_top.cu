@@ -280,6 +280,10 @@ int build_top_plan(nwcch_topology* t, QueryPlans* Q, int32_t log2_tau, TopPlan**
         return rc;
     }
     T->dev = TopDev{d_top_dfs, d_dfs_sn, d_dfs_end, d_lift, Q->tin, Q->tout, ntop, J};
+    if (setup_copies_done() != cudaSuccess) {  // the uploads above, before any stream reads them
+        free_top_plan(T);
+        return NWCCH_ERR_CUDA;
+    }
     *out = T;
     Q->top[log2_tau] = std::move(plan);
     return NWCCH_OK;
@@ -478,7 +482,12 @@ __global__ void k_qscatter(DevTopo D, int64_t nq, int32_t nb, const int32_t* __r
             continue;
         }
         const int32_t pos = atomicAdd(&fill[dir * nb + b], 1);
-        order[dir * nq + boff[dir * (nb + 1) + b] + pos] = (int32_t)c;
+        const int64_t o = (int64_t)boff[dir * (nb + 1) + b] + pos;
+        if (o < 0 || o >= nq) {  // more chains than the histogram counted: cannot happen
+            atomicOr(err, ERR_TOPOLOGY);
+            continue;
+        }
+        order[dir * nq + o] = (int32_t)c;
     }
 }
 
@@ -535,22 +544,31 @@ __global__ void __launch_bounds__(QT_THREADS, 2) k_qtop(DevTopo D, SnDev S, TopD
         const int64_t base0 = D.first[s0];
         if (threadIdx.x == 0) s_imin = k;
         __syncthreads();
+        // the tile's chains, checked before any label row is addressed
+        // through them (a tile with an inconsistent entry is skipped and
+        // reported; this cannot happen)
+        bool bad = nct < 1 || first_c < 0 || (int64_t)first_c + nct > nq || d0 < k - 1 || d0 >= Dp;
         if (threadIdx.x < CT) {
             int32_t c = -1, i0 = k;
-            if (threadIdx.x < nct) {
+            if (threadIdx.x < nct && !bad) {
                 c = order[dir * nq + first_c + threadIdx.x];
-                const int32_t tx = T.tin[xin[c]];
-                i0 = lowest_anc_row(T, s0, k, tx);
-                if (!is_anc(T, s0 + i0, tx)) {  // the chain does not cross S: cannot happen
-                    e_bits |= ERR_TOPOLOGY;
-                    i0 = k;
+                const int32_t x = (c >= 0 && c < 2 * nq) ? xin[c] : -1;
+                if (x < 0 || x >= D.n) {
+                    bad = true;
+                } else {
+                    const int32_t tx = T.tin[x];
+                    i0 = lowest_anc_row(T, s0, k, tx);
+                    if (!is_anc(T, s0 + i0, tx)) bad = true;  // the chain does not cross S
                 }
                 atomicMin(&s_imin, i0);
             }
             s_chain[threadIdx.x] = c;
             s_i0[threadIdx.x] = i0;
         }
-        __syncthreads();
+        if (__syncthreads_or(bad)) {
+            e_bits |= ERR_TOPOLOGY;
+            continue;
+        }
         const int32_t r_lo = s_imin & ~31, nr = k - r_lo;
         // rows r_lo.. of the tile's chains (no path below a chain's entry row,
         // and in the columns of absent chains)
@@ -635,6 +653,10 @@ __global__ void __launch_bounds__(QT_THREADS, 2) k_qtop(DevTopo D, SnDev S, TopD
         for (int32_t jb = threadIdx.x; jb < b; jb += QT_THREADS) {
             const int32_t j = k + jb;
             const int32_t hd = D.hdep[bbase + jb];
+            if (hd < 0 || hd >= Dp) {  // a head deeper than the tree: cannot happen
+                e_bits |= ERR_TOPOLOGY;
+                continue;
+            }
             int32_t acc[CT];
 #pragma unroll
             for (int q = 0; q < CT; q++) acc[q] = q < nct ? Lg[(int64_t)s_chain[q] * Dp + hd] : Q32::CINF;
@@ -687,10 +709,10 @@ __global__ void __launch_bounds__(256) k_qmeet(DevTopo D, SnDev S, TopDev T, int
             dl = lca[q];
             if (dl == -1) {
                 const int32_t xs = xin[q], xt = xin[nq + q];
-                if (xs >= 0 && xt >= 0) dl = top_lca_depth(D, S, T, xs, xt);
+                if (xs >= 0 && xt >= 0 && xs < D.n && xt < D.n) dl = top_lca_depth(D, S, T, xs, xt);
             }
         }
-        dl = __shfl_sync(FULL, dl, 0);
+        dl = min(__shfl_sync(FULL, dl, 0), (int32_t)(Dp - 1));
         const int32_t* F = Lg + q * Dp;
         const int32_t* R = Lg + (nq + q) * Dp;
         int32_t best = Q32::CINF;
@@ -728,7 +750,7 @@ int get_top_plan(nwcch_topology* t, int32_t log2_tau, bool lookup_only, TopPlan*
 template <class K>
 int occupancy_grid(K kernel, int threads, size_t smem, int64_t want, int sms, int64_t* blocks) {
     int per_sm = 0;
-    NWCCH_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    NWCCH_CUDA_TRY(allow_dynamic_smem((const void*)kernel, smem));
     NWCCH_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem));
     if (per_sm < 1) return NWCCH_ERR_CAPACITY;
     *blocks = std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)sms * per_sm));
@@ -769,27 +791,36 @@ int query_top_async(nwcch_topology* t, const int32_t* up, const int32_t* dn, con
     const TopDev& TD = T->dev;
     const int32_t ntop = TD.ntop, nb = ntop + 1;
     const int sms = t->sms;
-    // scratch of one pass
-    const size_t lab_bytes = (size_t)(2 * chunk * Dp) * 4;
-    const size_t small_bytes = (size_t)(2 * chunk) * 4 * 3 + (size_t)chunk * 4 + (size_t)(2 * nb + 2 * (nb + 1)) * 4 +
-                               (size_t)(2 * (int64_t)ntop + 1) * 8 + 256;
+    // scratch of one pass: the regions in carving order, each rounded up to
+    // 16 bytes; the allocation is the sum of exactly these sizes
+    enum { R_LG, R_TILE_OFF, R_XIN, R_KEY, R_ORDER, R_LCA, R_HIST, R_FILL, R_BOFF, R_COUNT };
+    size_t region[R_COUNT];
+    region[R_LG] = (size_t)(2 * chunk * Dp) * 4;
+    region[R_TILE_OFF] = (size_t)(2 * (int64_t)ntop + 1) * 8;
+    region[R_XIN] = region[R_KEY] = region[R_ORDER] = (size_t)(2 * chunk) * 4;
+    region[R_LCA] = (size_t)chunk * 4;
+    region[R_HIST] = region[R_FILL] = (size_t)(2 * nb) * 4;
+    region[R_BOFF] = (size_t)(2 * (nb + 1)) * 4;
+    auto round16 = [](size_t bytes) { return (bytes + 15) & ~(size_t)15; };
+    size_t total = 0;
+    for (size_t r : region) total += round16(r);
     void* scratch = nullptr;
-    NWCCH_CUDA_TRY(cudaMallocAsync(&scratch, lab_bytes + small_bytes, s));
+    NWCCH_CUDA_TRY(cudaMallocAsync(&scratch, total, s));
     char* p = static_cast<char*>(scratch);
-    auto take = [&](size_t bytes) {
-        char* r = p;
-        p += (bytes + 15) & ~(size_t)15;
-        return r;
+    auto take = [&](int r) {
+        char* at = p;
+        p += round16(region[r]);
+        return at;
     };
-    int32_t* Lg = reinterpret_cast<int32_t*>(take(lab_bytes));
-    int64_t* tile_off = reinterpret_cast<int64_t*>(take((size_t)(2 * (int64_t)ntop + 1) * 8));
-    int32_t* xin = reinterpret_cast<int32_t*>(take((size_t)(2 * chunk) * 4));
-    int32_t* key = reinterpret_cast<int32_t*>(take((size_t)(2 * chunk) * 4));
-    int32_t* order = reinterpret_cast<int32_t*>(take((size_t)(2 * chunk) * 4));
-    int32_t* lca = reinterpret_cast<int32_t*>(take((size_t)chunk * 4));
-    int32_t* hist = reinterpret_cast<int32_t*>(take((size_t)(2 * nb) * 4));
-    int32_t* fill = reinterpret_cast<int32_t*>(take((size_t)(2 * nb) * 4));
-    int32_t* boff = reinterpret_cast<int32_t*>(take((size_t)(2 * (nb + 1)) * 4));
+    int32_t* Lg = reinterpret_cast<int32_t*>(take(R_LG));
+    int64_t* tile_off = reinterpret_cast<int64_t*>(take(R_TILE_OFF));
+    int32_t* xin = reinterpret_cast<int32_t*>(take(R_XIN));
+    int32_t* key = reinterpret_cast<int32_t*>(take(R_KEY));
+    int32_t* order = reinterpret_cast<int32_t*>(take(R_ORDER));
+    int32_t* lca = reinterpret_cast<int32_t*>(take(R_LCA));
+    int32_t* hist = reinterpret_cast<int32_t*>(take(R_HIST));
+    int32_t* fill = reinterpret_cast<int32_t*>(take(R_FILL));
+    int32_t* boff = reinterpret_cast<int32_t*>(take(R_BOFF));
     const int dense_rows = t->tune.query_dense_rows;
     for (int64_t q0 = 0; q0 < nq && rc == NWCCH_OK; q0 += chunk) {
         const int64_t m = std::min(chunk, nq - q0);

@@ -172,6 +172,7 @@ extern "C" int nwcch_topology_create(int64_t n, const int64_t* first, const int3
             slot.counters = reinterpret_cast<unsigned long long*>(p64 + 32 * i + 16);
             t->slots.push_back(slot);
         }
+        if (setup_copies_done() != cudaSuccess) rc = NWCCH_ERR_CUDA;
     } while (false);
     if (rc != NWCCH_OK) {
         release(t);

@@ -106,6 +106,10 @@ static __device__ __forceinline__ void enqueue(const UpdateArgs<T>& A, int32_t c
     if (atomicOr(word, bit) & bit) return;
     const int32_t L = A.D.vlevel[A.D.tail[c]];
     const int32_t pos = atomicAdd(&A.ws.bcount[L], 1);
+    if (pos >= A.level_arc_off[L + 1] - A.level_arc_off[L]) {  // more arcs than the level has: cannot happen
+        atomicOr(A.err, ERR_TOPOLOGY);
+        return;
+    }
     A.ws.bucket[A.level_arc_off[L] + pos] = c;
     atomicOr(&A.ws.pending[L >> 5], 1u << (L & 31));
 }
@@ -208,7 +212,7 @@ __global__ void __launch_bounds__(256) k_update(UpdateArgs<T> A) {
                 for (int32_t wi = L >> 5; wi < ((A.levels + 31) >> 5); wi++) {
                     uint32_t bits = __ldcg(A.ws.pending + wi);
                     if (wi == (L >> 5)) bits &= ~((1u << (L & 31)) - 1u);
-                    while (bits) {
+                    while (bits && d < (unsigned long long)A.levels) {
                         A.ws.done_levels[d++] = wi * 32 + __ffs(bits) - 1;
                         bits &= bits - 1;
                     }
@@ -218,10 +222,10 @@ __global__ void __launch_bounds__(256) k_update(UpdateArgs<T> A) {
             break;
         }
         const int64_t base = A.level_arc_off[L];
-        const int32_t cnt = __ldcg(A.ws.bcount + L);
+        const int32_t cnt = (int32_t)min((int64_t)__ldcg(A.ws.bcount + L), A.level_arc_off[L + 1] - base);
         if (gtid == 0) {
             const unsigned long long d = atomicAdd(A.ws.stats + 3, 1ull);
-            A.ws.done_levels[d] = L;
+            if (d < (unsigned long long)A.levels) A.ws.done_levels[d] = L;  // (a level is done once)
             atomicAdd(A.ws.stats + 0, (unsigned long long)cnt);
         }
         for (int64_t i = gwarp; i < cnt; i += gwarps) {
@@ -255,7 +259,7 @@ __global__ void __launch_bounds__(256) k_update(UpdateArgs<T> A) {
                 A.dn[c] = nd;
                 A.ws.chg[c] = 1;
                 const unsigned long long p = atomicAdd(A.ws.stats + 1, 1ull);
-                A.ws.changed[p] = c;
+                if (p < (unsigned long long)D.m_plus) A.ws.changed[p] = c;  // (an arc changes once)
                 if (negative_pair(nu, nd)) atomicAdd(A.ws.stats + 2, 1ull);
             }
             // every triangle (y; v, z) or (y; z, v) of row y has c as a lower side
@@ -282,13 +286,13 @@ __global__ void __launch_bounds__(256) k_update(UpdateArgs<T> A) {
         return;
     }
     // 4. clean the workspace for the next call
-    const int64_t nchanged = (int64_t)__ldcg(A.ws.stats + 1);
+    const int64_t nchanged = min((int64_t)__ldcg(A.ws.stats + 1), D.m_plus);
     for (int64_t j = gtid; j < nchanged; j += gthreads) A.ws.chg[__ldcg(A.ws.changed + j)] = 0;
-    const int32_t nd_levels = (int32_t)__ldcg(A.ws.stats + 3);
+    const int32_t nd_levels = (int32_t)min((int64_t)__ldcg(A.ws.stats + 3), (int64_t)A.levels);
     for (int32_t li = 0; li < nd_levels; li++) {
         const int32_t l = __ldcg(A.ws.done_levels + li);
         const int64_t base = A.level_arc_off[l];
-        const int32_t cnt = __ldcg(A.ws.bcount + l);
+        const int32_t cnt = (int32_t)min((int64_t)__ldcg(A.ws.bcount + l), A.level_arc_off[l + 1] - base);
         for (int64_t i = gtid; i < cnt; i += gthreads) A.ws.queued[__ldcg(A.ws.bucket + base + i)] = 0;
     }
     if (!grid_sync(A)) return;
@@ -432,16 +436,16 @@ __global__ void __launch_bounds__(256) k_dense_count(DevTopo D, int32_t L, const
 
 // The workspace cleanup of the sweep, for a stopped sweep.
 __global__ void __launch_bounds__(256) k_update_clean(UpdateWorkspace ws, const int64_t* __restrict__ level_arc_off,
-                                                      int64_t m_plus) {
+                                                      int64_t m_plus, int32_t levels) {
     const int64_t nchanged = min((int64_t)ws.stats[1], m_plus);
-    const int32_t nd_levels = (int32_t)ws.stats[3];
+    const int32_t nd_levels = (int32_t)min((int64_t)ws.stats[3], (int64_t)levels);
     for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < nchanged;
          j += (int64_t)gridDim.x * blockDim.x)
         ws.chg[ws.changed[j]] = 0;
     for (int32_t li = blockIdx.x; li < nd_levels; li += gridDim.x) {
         const int32_t l = ws.done_levels[li];
         const int64_t base = level_arc_off[l];
-        const int32_t cnt = ws.bcount[l];
+        const int32_t cnt = (int32_t)min((int64_t)ws.bcount[l], level_arc_off[l + 1] - base);
         for (int32_t i = threadIdx.x; i < cnt; i += blockDim.x) ws.queued[ws.bucket[base + i]] = 0;
         __syncthreads();
         if (threadIdx.x == 0) {
@@ -520,7 +524,8 @@ int get_workspace(nwcch_topology* t, int64_t k, UpdateWorkspace** out) {
             ok = cudaMemset(ws->queued, 0, qbytes) == cudaSuccess && cudaMemset(ws->bcount, 0, L * 4) == cudaSuccess &&
                  cudaMemset(ws->pending, 0, ((L + 31) / 32) * 4) == cudaSuccess &&
                  cudaMemset(ws->chg, 0, qbytes) == cudaSuccess && cudaMemset(ws->dq, 0, qbytes) == cudaSuccess &&
-                 cudaMemset(ws->stats, 0, kStatWords * sizeof(unsigned long long)) == cudaSuccess;
+                 cudaMemset(ws->stats, 0, kStatWords * sizeof(unsigned long long)) == cudaSuccess &&
+                 setup_copies_done() == cudaSuccess;
         if (ok) ok = cooperative_blocks((const void*)k_update<int32_t>, &ws->blocks32) == NWCCH_OK &&
                      cooperative_blocks((const void*)k_update<int64_t>, &ws->blocks64) == NWCCH_OK;
         if (!ok) {
@@ -610,6 +615,7 @@ int finish_dense(nwcch_topology* t, UpdateWorkspace* ws, const int32_t* w_dev, T
             return NWCCH_ERR_NOMEM;
         if (!tl.empty())
             NWCCH_CUDA_TRY(cudaMemcpy(ws->tiles, tl.data(), sizeof(int2) * tl.size(), cudaMemcpyHostToDevice));
+        NWCCH_CUDA_TRY(setup_copies_done());
         ws->ntiles = (int64_t)tl.size();
         ws->tiles_plan = P;
     }
@@ -618,7 +624,7 @@ int finish_dense(nwcch_topology* t, UpdateWorkspace* ws, const int32_t* w_dev, T
     k_dense_mark<<<grid, 32 * kMarkWarps, 0, s>>>(t->d, P->dev, ws->tiles, ws->ntiles, ws->chg, ws->dq, ws->acol,
                                                   bflag);
     k_dense_count<<<grid_for(mp, 256), 256, 0, s>>>(t->d, L, ws->queued, ws->dq, ws->stats);
-    k_update_clean<<<t->sms * 4, 256, 0, s>>>(*ws, t->d_level_arc_off, mp);
+    k_update_clean<<<t->sms * 4, 256, 0, s>>>(*ws, t->d_level_arc_off, mp, t->levels);
     NWCCH_CUDA_TRY(cudaGetLastError());
     NWCCH_CUDA_TRY(cudaMemsetAsync(ws->dq, 0, (size_t)mp, s));
     return NWCCH_OK;

@@ -95,3 +95,46 @@ def test_top_pipeline_leaves_wide_values_to_the_64_bit_kernel(gpu, oracle):
     m = T.customize(w, "int32")
     tune.set(T, "query_top_chains", 4)
     assert np.array_equal(T.query_batch(m, s, t).cpu().numpy(), want)
+
+
+def test_top_pipeline_concurrent_streams(gpu):
+    """Batches of several metrics enqueued at once from threads on their own
+    streams (as the serving loop does): each call carves its scratch from its
+    own stream-ordered allocation, so every answer equals the same batch run
+    alone."""
+    import threading
+
+    import torch
+
+    from nwcch import graphs as G
+    from nwcch import tune
+    from nwcch.device import DeviceTopology
+    g, top = _graph("delaunay", 60_000, seed=9)
+    T = DeviceTopology.from_dict(top)
+    tune.set(T, "query_top_chains", 64)
+    W = G.scaled_metrics(g, 4, seed=3)
+    ms = [T.customize(w, "int32") for w in W]
+    rng = np.random.default_rng(4)
+    batches = [(top["rank"][rng.integers(0, g["n"], nq)], top["rank"][rng.integers(0, g["n"], nq)])
+               for nq in (1300, 2100, 3500, 5000, 8000, 1800)]
+    want = {(j, b): T.query_batch(ms[j], *batches[b]).cpu().numpy() for j in range(4) for b in range(len(batches))}
+    errors, got = [], {}
+
+    def worker(j):
+        stream = torch.cuda.Stream()
+        try:
+            with torch.cuda.stream(stream):
+                for rep in range(3):
+                    for b in range(len(batches)):
+                        got[j, b, rep] = T.query_batch(ms[j], *batches[b]).cpu().numpy()
+        except Exception as exc:  # reported below
+            errors.append(f"{type(exc).__name__}: {exc}")
+
+    threads = [threading.Thread(target=worker, args=(j,)) for j in range(4)]
+    for th in threads:
+        th.start()
+    for th in threads:
+        th.join()
+    assert not errors, errors[:3]
+    for (j, b, rep), d in got.items():
+        assert np.array_equal(d, want[j, b]), (j, b, rep)
