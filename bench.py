@@ -290,6 +290,7 @@ def run_ours(args, W, world):
             e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
             step(e0, e1)
             T.query_batch(good, qs, qt)  # synchronizes
+            q_launches = T.last_query_launches()
             e2.record(stream)
             torch.cuda.synchronize()
             cust_ms.append(e0.elapsed_time(e1))
@@ -377,7 +378,7 @@ def run_ours(args, W, world):
     return dict(T=T, tuned=tuned, cust_tuned=cust_tuned, cust_ms=cust_ms, q_ms=q_ms, wall=wall, plain_ms=plain_ms, plain_equal=same,
                 e2e_ms=e2e_ms, graph_q=graph_q, bad_host=bad_host, batch_dist=ref_d.cpu().numpy(), topo_s=topo_s,
                 plain_q_ms=plain_q_ms, lat_dist=lat_dist, pot_ms=pot_ms, pot=pot.cpu().numpy(), good_host=good_host,
-                lat_us=lat, clocks=clocks.summary(), neg=neg_k, saturated=bool(sat))
+                lat_us=lat, clocks=clocks.summary(), neg=neg_k, saturated=bool(sat), query_launches=q_launches)
 
 
 def scanned_arcs(top, qs, qt, sample: int = 1000) -> float:
@@ -779,6 +780,8 @@ def profile_part(args):
         tune.set(T, "sn_warp_cap", args.sn_warp_cap)
     if args.sn_warp_min_count is not None:
         tune.set(T, "sn_warp_min_count", args.sn_warp_min_count)
+    if args.sn_chain_max_items is not None:
+        tune.set(T, "sn_chain_max_items", args.sn_chain_max_items)
     w = torch.from_numpy(W["w"]).cuda()
     m = T.customize(w, "int32")
     qs, qt = torch.from_numpy(W["qs"]).cuda(), torch.from_numpy(W["qt"]).cuda()
@@ -815,7 +818,8 @@ def profile_part(args):
         torch.cuda.synchronize()
         times.append(e0.elapsed_time(e1))
     print(json.dumps({"profile": args.profile, "workload": args.workload, "ms": [round(x, 4) for x in times],
-                      "sn_launches": T.sn_launches, "sn_warp_cap": tune.get(T, "sn_warp_cap"),
+                      "sn_launches": T.sn_launches, "chain_level": T.chain_level, "chain_phases": T.chain_phases,
+                      "sn_warp_cap": tune.get(T, "sn_warp_cap"),
                       "sn_warp_min_count": tune.get(T, "sn_warp_min_count")}), flush=True)
 
 
@@ -906,6 +910,9 @@ def main():
                     help="run only this part, --steps times after --warmup (for ncu captures); no bench line")
     ap.add_argument("--sn-warp-cap", type=int, default=None, help="customization plan: warp-kernel trapezoid cap")
     ap.add_argument("--sn-warp-min-count", type=int, default=None, help="customization plan: level threshold")
+    ap.add_argument("--sn-chain-max-items", type=int, default=None,
+                    help="customization plan: persistent launch of the levels whose launches hold at most this many "
+                         "items (0: none)")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -1022,9 +1029,11 @@ def main():
                              "cpu_note": "the oracle's ET query, 1 thread, same graph, metric and pairs"},
         "e2e": {"value": round(statistics.median(R["e2e_ms"]), 4), "unit": "ms",
                 "h2d_bytes_per_step": int(W["w"].size * 4), "d2h_bytes_per_step": 8},
-        # per timed step: k_fill2 + k_base + the supernodal launches, the
-        # scan, and the query batch's k_maxabs + k_query_sn32 + k_query_sn
-        "gpu_launches": (2 + T.sn_launches + 1 + 3) * args.steps,
+        # per timed step: k_fill2 + k_base + the supernodal launches (those
+        # below the persistent top, plus k_sn_chain), the scan, and the query
+        # batch's kernels
+        "gpu_launches": (2 + (T.chain_from + 1 if T.chain_phases else T.sn_launches) + 1 + R["query_launches"])
+                        * args.steps,
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "peak_source": peak_src,
                      "unit": "GB/s", "frac": round(achieved / peak, 4),
                      "traffic": (int(MEASURED_TRAFFIC[args.workload][0]) if args.workload in MEASURED_TRAFFIC

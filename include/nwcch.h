@@ -196,6 +196,19 @@ int nwcch_check(nwcch_topology* t, void* stream);
  * 32 chains, the rest of each chain per warp; 0 sweeps every chain per warp.
  * Default 64. */
 #define NWCCH_TUNE_QUERY_TOP_CHAINS 16
+/* Customization schedule near the root (int32 storage): the levels from
+ * which every level has no warp-kernel launch and no launch of more than
+ * this many items run as one persistent cooperative launch, one phase per
+ * former launch with a bounded grid barrier between phases (a wait past the
+ * NWCCH_TUNE_UPDATE_SPIN_LIMIT reports NWCCH_ERR_TIMEOUT); 0: every level
+ * launches its own kernels. Default 0. Setting it rebuilds the plan, as
+ * NWCCH_TUNE_SN_WARP_CAP does. */
+#define NWCCH_TUNE_SN_CHAIN_MAX_ITEMS 17
+/* Customization schedule at the bottom: in the levels where supernodes take
+ * the warp kernel, those whose trapezoid holds at most this many arcs
+ * (<= 32) take a kernel with one thread per supernode instead (0: none).
+ * Default 16. Setting it rebuilds the plan. */
+#define NWCCH_TUNE_SN_THREAD_CAP 18
 int nwcch_tune_set(nwcch_topology* t, int key, int64_t value);
 int nwcch_tune_get(const nwcch_topology* t, int key, int64_t* value);
 

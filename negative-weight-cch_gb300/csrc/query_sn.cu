@@ -213,10 +213,12 @@ int query_sn_async(nwcch_topology* t, const T* up, const T* dn, const int32_t* s
     const StreamSlot slot = stream_slot(t, s);
     unsigned int* maxabs = reinterpret_cast<unsigned int*>(slot.counters + 3);
     int* err = slot.err;
+    int64_t launches = 0;
     if (sizeof(T) == 4) {
         // 32-bit labels when the metric's values allow them (decided on the
         // device: each kernel returns at once when the batch is not its own)
         NWCCH_CUDA_TRY(cudaMemsetAsync(maxabs, 0, sizeof(unsigned int), s));
+        launches++;
         k_maxabs<<<grid_for_queries(t->d.m_plus), 256, 0, s>>>(reinterpret_cast<const int32_t*>(up),
                                                                reinterpret_cast<const int32_t*>(dn), t->d.m_plus,
                                                                maxabs);
@@ -236,8 +238,11 @@ int query_sn_async(nwcch_topology* t, const T* up, const T* dn, const int32_t* s
         if (nq > t->tune.query_cta_max) {
             // large batch: the top of the tree as (min,+) products over
             // chains (stream-ordered scratch, also when enqueued only)
-            const int rc = query_top_async(t, u32, d32, s_rank, t_rank, nq, dist, maxabs, err, s, &top_used);
+            int64_t top_launches = 0;
+            const int rc = query_top_async(t, u32, d32, s_rank, t_rank, nq, dist, maxabs, err, s, &top_used,
+                                           &top_launches);
             if (rc) return rc;
+            launches += top_launches;
         }
         if (top_used) {
             // answered (or left to the 64-bit kernel below)
@@ -249,11 +254,13 @@ int query_sn_async(nwcch_topology* t, const T* up, const T* dn, const int32_t* s
             if (nq <= t->tune.query_cta_wide_max) {
                 int rc = launch_shape(k_query_sn32_cta<16>, 16, cta_smem, nq * 16, &blocks);
                 if (rc) return rc;
+                launches++;
                 k_query_sn32_cta<16><<<(unsigned)blocks, 512, cta_smem, s>>>(t->d, S, u32, d32, s_rank, t_rank, nq,
                                                                             dist, maxabs, err, rows);
             } else {
                 int rc = launch_shape(k_query_sn32_cta<8>, 8, cta_smem, nq * 8, &blocks);  // one query per CTA
                 if (rc) return rc;
+                launches++;
                 k_query_sn32_cta<8><<<(unsigned)blocks, 256, cta_smem, s>>>(t->d, S, u32, d32, s_rank, t_rank, nq,
                                                                            dist, maxabs, err, rows);
             }
@@ -264,6 +271,7 @@ int query_sn_async(nwcch_topology* t, const T* up, const T* dn, const int32_t* s
             if (rc) return rc;
             void* scratch = nullptr;
             NWCCH_CUDA_TRY(cudaMallocAsync(&scratch, (size_t)(blocks * 4 * per_warp), s));
+            launches++;
             kern<<<(unsigned)blocks, 128, 0, s>>>(t->d, S, u32, d32, s_rank, t_rank, nq, dist, maxabs,
                                                           static_cast<unsigned char*>(scratch), err,
                                                           t->tune.query_dense_rows);
@@ -277,6 +285,7 @@ int query_sn_async(nwcch_topology* t, const T* up, const T* dn, const int32_t* s
                 int64_t blocks = 0;
                 int rc = launch_shape(kern, w32, smem32, nq, &blocks);
                 if (rc) return rc;
+                launches++;
                 kern<<<(unsigned)blocks, 32 * w32, smem32, s>>>(t->d, S, u32, d32, s_rank, t_rank, nq, dist,
                                                                         maxabs, nullptr, err,
                                                                         t->tune.query_dense_rows);
@@ -289,6 +298,7 @@ int query_sn_async(nwcch_topology* t, const T* up, const T* dn, const int32_t* s
     k_query_sn<T><<<(unsigned)blocks, 32 * w64, smem64, s>>>(t->d, S, up, dn, s_rank, t_rank, nq, dist, maxabs,
                                                              err, t->tune.query_dense_rows);
     NWCCH_CUDA_TRY(cudaGetLastError());
+    t->last_query_launches = launches + 1;
     *used = true;
     return NWCCH_OK;
 }

@@ -765,8 +765,9 @@ int occupancy_grid(K kernel, int threads, size_t smem, int64_t want, int sms, in
 // shared-memory labels, or a top supernode is too wide for a label tile.
 int query_top_async(nwcch_topology* t, const int32_t* up, const int32_t* dn, const int32_t* s_rank,
                     const int32_t* t_rank, int64_t nq, int64_t* dist, const unsigned int* maxabs, int* err,
-                    cudaStream_t s, bool* used) {
+                    cudaStream_t s, bool* used, int64_t* launches) {
     *used = false;
+    *launches = 0;
     const int64_t min_chains = t->tune.query_top_chains;
     if (min_chains <= 0 || !t->sn_plan || nq < 1) return NWCCH_OK;
     const int64_t Dp = t->d.max_depth + 1;
@@ -858,6 +859,7 @@ int query_top_async(nwcch_topology* t, const int32_t* up, const int32_t* dn, con
             }
         }
         if (rc) break;
+        *launches += 4 + (int64_t)(T->lvl_off.size() - 1);  // k_qlow, k_qscan, k_qscatter, k_qtop per level, k_qmeet
         k_qmeet<<<(unsigned)std::max<int64_t>(1, std::min<int64_t>((m + 7) / 8, (int64_t)sms * 16)), 256, 0, s>>>(
             t->d, P->dev, TD, m, xin, lca, Lg, Dp, dist + q0, maxabs);
         if (cudaGetLastError() != cudaSuccess) rc = NWCCH_ERR_CUDA;

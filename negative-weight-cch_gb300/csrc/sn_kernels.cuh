@@ -48,6 +48,22 @@ struct Exact {
     __device__ static T to(V x) { return x; }
 };
 
+// Loads of customized values. LdPlain: the arcs a kernel reads were written
+// by earlier launches. LdL2: they may have been written by other CTAs of the
+// same (persistent) launch before a grid barrier, so the load bypasses L1
+// (which is not kept coherent between SMs) and reads L2.
+struct LdPlain {
+    template <class T>
+    __device__ static T ld(const T* p) { return *p; }
+};
+struct LdL2 {
+    template <class T>
+    __device__ static T ld(const T* p) {
+        if constexpr (sizeof(T) == 4) return (T)__ldcg(reinterpret_cast<const int*>(p));
+        else return (T)__ldcg(reinterpret_cast<const long long*>(p));
+    }
+};
+
 __device__ __forceinline__ void atomic_min_t(int32_t* p, int32_t v) { atomicMin(p, v); }
 __device__ __forceinline__ void atomic_min_t(int64_t* p, int64_t v) {
     atomicMin(reinterpret_cast<long long*>(p), (long long)v);
@@ -147,7 +163,7 @@ __device__ void panel_compute(PanelSmem<V, CT>& sm, int pn, bool hasj, int& e) {
 
 // Loads the diagonal triangle and the thread's column (converted by P).
 // Returns true if some value is outside the fast range (FastI32 only).
-template <class P, class T, class V, int CT>
+template <class P, class T, class V, int CT, class LD = LdPlain>
 __device__ bool panel_load(PanelSmem<V, CT>& sm, const T* __restrict__ up, const T* __restrict__ dn, int pn,
                            int i0, int j, bool hasj) {
     // every load of a group is issued before its values are used, so the
@@ -163,8 +179,8 @@ __device__ bool panel_load(PanelSmem<V, CT>& sm, const T* __restrict__ up, const
             du[q] = Lim<T>::INF;
             dd[q] = Lim<T>::INF;
             if (a < c && c < pn) {
-                du[q] = up[sm.rowb[a] + c - a - 1];
-                dd[q] = dn[sm.rowb[a] + c - a - 1];
+                du[q] = LD::ld(up + sm.rowb[a] + c - a - 1);
+                dd[q] = LD::ld(dn + sm.rowb[a] + c - a - 1);
             }
         }
 #pragma unroll
@@ -189,8 +205,8 @@ __device__ bool panel_load(PanelSmem<V, CT>& sm, const T* __restrict__ up, const
                 cd[q] = Lim<T>::INF;
                 if (a < pn) {
                     const int64_t idx = sm.rowb[a] + (j - (i0 + a)) - 1;
-                    cu[q] = up[idx];
-                    cd[q] = dn[idx];
+                    cu[q] = LD::ld(up + idx);
+                    cd[q] = LD::ld(dn + idx);
                 }
             }
 #pragma unroll
@@ -305,11 +321,12 @@ struct TileCtx {
     int ibeg, iend, abase, bbase, alim;
 };
 
+// The tile of work item `it` (a triple: supernode, row tile, column tile).
 template <class T, int TILE, int MT, bool OUT>
-__device__ __forceinline__ TileCtx<T, TILE, MT, OUT> tile_ctx(const SnDev& S, const int32_t* items, int panel) {
+__device__ __forceinline__ TileCtx<T, TILE, MT, OUT> tile_ctx(const SnDev& S, const int32_t* it, int panel) {
     TileCtx<T, TILE, MT, OUT> c;
-    c.s = items[3 * blockIdx.x];
-    const int tr = items[3 * blockIdx.x + 1], tc = items[3 * blockIdx.x + 2];
+    c.s = it[0];
+    const int tr = it[1], tc = it[2];
     c.s0 = S.s0[c.s];
     c.k = S.k[c.s];
     c.b = S.b[c.s];
@@ -338,7 +355,7 @@ struct TileSmem {
 
 // Runs the product with policy P; returns false (fast policy only) as soon as
 // an operand leaves the fast range, leaving the accumulators meaningless.
-template <class P, class T, int TILE, int MT, int CH, bool OUT>
+template <class P, class T, int TILE, int MT, int CH, bool OUT, class LD = LdPlain>
 __device__ bool tile_product(const DevTopo& D, const TileCtx<T, TILE, MT, OUT>& c,
                              TileSmem<typename P::V, TILE, CH>& sm, const T* __restrict__ up,
                              const T* __restrict__ dn, typename P::V (&accU)[MT][MT], typename P::V (&accD)[MT][MT],
@@ -372,10 +389,10 @@ __device__ bool tile_product(const DevTopo& D, const TileCtx<T, TILE, MT, OUT>& 
             const int ac = c.abase + cc, bc = c.bbase + cc;
             const bool okr = a < nch;
             const int64_t rb = sm.rowb[a] - (i0 + a) - 1;
-            ad[q] = (okr && ac < c.alim) ? dn[rb + ac] : Lim<T>::INF;
-            au[q] = (okr && ac < c.alim) ? up[rb + ac] : Lim<T>::INF;
-            bu[q] = (okr && bc < c.cols) ? up[rb + bc] : Lim<T>::INF;
-            bd[q] = (okr && bc < c.cols) ? dn[rb + bc] : Lim<T>::INF;
+            ad[q] = (okr && ac < c.alim) ? LD::ld(dn + rb + ac) : Lim<T>::INF;
+            au[q] = (okr && ac < c.alim) ? LD::ld(up + rb + ac) : Lim<T>::INF;
+            bu[q] = (okr && bc < c.cols) ? LD::ld(up + rb + bc) : Lim<T>::INF;
+            bd[q] = (okr && bc < c.cols) ? LD::ld(dn + rb + bc) : Lim<T>::INF;
         }
 #pragma unroll
         for (int q = 0; q < NL; q++) {
@@ -413,7 +430,7 @@ __device__ bool tile_product(const DevTopo& D, const TileCtx<T, TILE, MT, OUT>& 
     return true;
 }
 
-template <class P, class T, int TILE, int MT, bool OUT>
+template <class P, class T, int TILE, int MT, bool OUT, class LD = LdPlain>
 __device__ void tile_store(const DevTopo& D, const SnDev& S, const TileCtx<T, TILE, MT, OUT>& c, T* __restrict__ up,
                            T* __restrict__ dn, const typename P::V (&accU)[MT][MT],
                            const typename P::V (&accD)[MT][MT]) {
@@ -435,8 +452,8 @@ __device__ void tile_store(const DevTopo& D, const SnDev& S, const TileCtx<T, TI
                 if (fd) atomic_min_t(&dn[a], (T)P::to(accD[ii][jj]));
             } else {
                 a = D.first[c.s0 + rr] + (cc - rr - 1);
-                if (fu) up[a] = min(up[a], (T)P::to(accU[ii][jj]));
-                if (fd) dn[a] = min(dn[a], (T)P::to(accD[ii][jj]));
+                if (fu) up[a] = min(LD::ld(up + a), (T)P::to(accU[ii][jj]));
+                if (fd) dn[a] = min(LD::ld(dn + a), (T)P::to(accD[ii][jj]));
             }
         }
 }
@@ -452,7 +469,7 @@ __global__ void __launch_bounds__((TILE / MT) * (TILE / MT))
     pdl_launch_dependents();
     up += blockIdx.y * D.m_plus;  // metric blockIdx.y of a metric-major batch
     dn += blockIdx.y * D.m_plus;
-    const auto c = tile_ctx<T, TILE, MT, OUT>(S, items, panel);
+    const auto c = tile_ctx<T, TILE, MT, OUT>(S, items + 3 * blockIdx.x, panel);
     int e = 0;
     bool done = false;
     if constexpr (sizeof(T) == 4) {
@@ -558,6 +575,211 @@ __global__ void __launch_bounds__(32 * WARPS) k_sn_warp(DevTopo D, SnDev S, cons
             dn[base + x] = Dn[x];
         }
         __syncwarp();
+    }
+    if (e) atomicOr(err, e);
+}
+
+
+// ------------------------------------------------------------------ tiny supernodes
+
+// One thread customizes a whole tiny supernode (trapezoid of at most
+// SN_THREAD_CAP arcs): the same steps as k_sn_warp (stage the trapezoid,
+// pivots in order, every boundary pair's minimum scattered into the
+// ancestors' arcs, write back), with the thread's arcs interleaved in shared
+// memory (arc x of thread t at [x][t], so that the threads of a warp never
+// hit the same bank). The bottom levels of a road-like graph hold millions of
+// supernodes of 2 to 20 arcs, where a warp per supernode leaves most lanes
+// idle.
+template <class T, int TT>
+__global__ void __launch_bounds__(TT) k_sn_thread(DevTopo D, SnDev S, const int32_t* __restrict__ items,
+                                                  int64_t count, T* __restrict__ up, T* __restrict__ dn,
+                                                  int* __restrict__ err) {
+    __shared__ T su[SN_THREAD_CAP][TT];
+    __shared__ T sd[SN_THREAD_CAP][TT];
+    pdl_wait();
+    pdl_launch_dependents();
+    const int tid = threadIdx.x;
+    up += blockIdx.y * D.m_plus;
+    dn += blockIdx.y * D.m_plus;
+    int e = 0;
+    for (int64_t it = (int64_t)blockIdx.x * TT + tid; it < count; it += (int64_t)gridDim.x * TT) {
+        const int32_t sn = items[3 * it];
+        const int32_t s0 = S.s0[sn], k = S.k[sn], b = S.b[sn];
+        const int32_t width = k + b;
+        const int64_t base = D.first[s0];
+        const int32_t total = (int32_t)sn_trapezoid(k, b);
+        if (total > SN_THREAD_CAP) {  // the plan never hands out such a supernode
+            e |= ERR_CAPACITY;
+            continue;
+        }
+        for (int x = 0; x < total; x++) {
+            su[x][tid] = up[base + x];
+            sd[x][tid] = dn[base + x];
+        }
+        auto ro = [&](int i) { return i * (width - 1) - i * (i - 1) / 2; };  // row i's first arc
+        for (int i = 0; i + 1 < k; i++) {
+            const int ri = ro(i);
+            for (int j = i + 1; j < k; j++) {
+                const T dij = sd[ri + (j - i - 1)][tid], uij = su[ri + (j - i - 1)][tid];
+                const int rj = ro(j);
+                for (int l = j + 1; l < width; l++) {
+                    const T uil = su[ri + (l - i - 1)][tid], dil = sd[ri + (l - i - 1)][tid];
+                    const int ejl = rj + (l - j - 1);
+                    T v;
+                    if (splus(dij, uil, v, e) && v < su[ejl][tid]) su[ejl][tid] = v;
+                    if (splus(dil, uij, v, e) && v < sd[ejl][tid]) sd[ejl][tid] = v;
+                }
+            }
+        }
+        const int32_t* rel = S.rel + S.rel_off[sn];
+        for (int p = 0; p + 1 < b; p++) {
+            const int prow = p * (2 * b - p - 1) / 2 - p - 1;  // + q: pair (p, q)
+            for (int q = p + 1; q < b; q++) {
+                T cu = Lim<T>::INF, cd = Lim<T>::INF;
+                for (int i = 0; i < k; i++) {
+                    const int ri = ro(i) - i - 1 + k;
+                    T v;
+                    if (splus(sd[ri + p][tid], su[ri + q][tid], v, e) && v < cu) cu = v;
+                    if (splus(sd[ri + q][tid], su[ri + p][tid], v, e) && v < cd) cd = v;
+                }
+                const int32_t a = rel[prow + q];
+                if (cu != Lim<T>::INF) atomic_min_t(&up[a], cu);
+                if (cd != Lim<T>::INF) atomic_min_t(&dn[a], cd);
+            }
+        }
+        for (int x = 0; x < total; x++) {
+            up[base + x] = su[x][tid];
+            dn[base + x] = sd[x][tid];
+        }
+    }
+    if (e) atomicOr(err, e);
+}
+
+// ------------------------------------------------------------------ top chain
+
+// Near the root of the supernode tree a level holds one or a few supernodes,
+// and one launch per panel, trailing update and outgoing product leaves most
+// of the GPU idle while each launch waits for the previous one. k_sn_chain
+// runs all of those levels in one cooperative launch: every phase (the items
+// of one former launch) is spread over the CTAs, and a grid barrier separates
+// consecutive phases. Values written before a barrier are read back through
+// L2 (LdL2). int32 storage; the phases and items come from the plan.
+
+// Barrier of all CTAs of the chain launch (co-resident: cooperative launch).
+// bar[0] counts arrivals, bar[1] is the generation. A wait that runs past
+// spin_limit iterations records ERR_TIMEOUT and returns false; the kernel then
+// stops. `extra` (a test hook, normally 0) makes the barrier wait for that
+// many arrivals more than the grid has, so that its wait runs out.
+__device__ __forceinline__ bool chain_barrier(unsigned int* bar, long long spin_limit, int extra, int* err) {
+    __shared__ int ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile unsigned int* gen = bar + 1;
+        const unsigned int g = *gen;
+        __threadfence();
+        ok = 1;
+        if (atomicAdd(bar, 1u) == gridDim.x + extra - 1) {
+            atomicExch(bar, 0u);
+            __threadfence();
+            atomicAdd(bar + 1, 1u);
+        } else {
+            long long spins = 0;
+            while (*gen == g) {
+                __nanosleep(32);
+                if (++spins > spin_limit) {
+                    atomicOr(err, ERR_TIMEOUT);
+                    ok = 0;
+                    break;
+                }
+            }
+        }
+        __threadfence();
+    }
+    __syncthreads();
+    return ok;
+}
+
+// One panel item of the chain: rows [i0, i0 + pn) of supernode it[0], the
+// CT columns of column tile it[1].
+template <int CT>
+__device__ void chain_panel(const DevTopo& D, const SnDev& S, const int32_t* it, int panel, int32_t* up,
+                            int32_t* dn, int& e, PanelSmem<int32_t, CT>& sm) {
+    const int32_t s = it[0], ct = it[1];
+    const int32_t s0 = S.s0[s], k = S.k[s], cols = k + S.b[s];
+    const int i0 = panel * SN_P;
+    const int pn = min(SN_P, k - i0);
+    const int tid = threadIdx.x;
+    if (tid < pn) sm.rowb[tid] = D.first[s0 + i0 + tid];
+    __syncthreads();
+    const int j = i0 + pn + ct * CT + tid;
+    const bool hasj = j < cols;
+    const bool diag = ct == 0;
+    bool done = false;
+    const bool bad = panel_load<FastI32, int32_t, int32_t, CT, LdL2>(sm, up, dn, pn, i0, j, hasj);
+    if (!__syncthreads_or(bad)) {
+        panel_compute<FastI32, int32_t, CT>(sm, pn, hasj, e);
+        const bool ok = panel_outputs_ok<FastI32, int32_t, CT>(sm, pn, hasj);
+        if (!__syncthreads_or(!ok)) {
+            panel_store<FastI32, int32_t, int32_t, CT>(sm, up, dn, pn, i0, j, hasj, diag);
+            done = true;
+        }
+    }
+    if (!done) {
+        using E = Exact<int32_t>;
+        __syncthreads();
+        panel_load<E, int32_t, int32_t, CT, LdL2>(sm, up, dn, pn, i0, j, hasj);
+        __syncthreads();
+        panel_compute<E, int32_t, CT>(sm, pn, hasj, e);
+        panel_store<E, int32_t, int32_t, CT>(sm, up, dn, pn, i0, j, hasj, diag);
+    }
+    __syncthreads();
+}
+
+// One 64 x 64 tile item of the chain (trailing update, or outgoing product).
+template <bool OUT>
+__device__ void chain_tile(const DevTopo& D, const SnDev& S, const int32_t* it, int panel, int32_t* up,
+                           int32_t* dn, int& e, TileSmem<int32_t, 64, 32>& sm) {
+    const auto c = tile_ctx<int32_t, 64, 4, OUT>(S, it, panel);
+    int32_t accU[4][4], accD[4][4];
+    if (tile_product<FastI32, int32_t, 64, 4, 32, OUT, LdL2>(D, c, sm, up, dn, accU, accD, e)) {
+        tile_store<FastI32, int32_t, 64, 4, OUT, LdL2>(D, S, c, up, dn, accU, accD);
+    } else {
+        using E = Exact<int32_t>;
+        tile_product<E, int32_t, 64, 4, 32, OUT, LdL2>(D, c, sm, up, dn, accU, accD, e);
+        tile_store<E, int32_t, 64, 4, OUT, LdL2>(D, S, c, up, dn, accU, accD);
+    }
+}
+
+// Shared memory of a chain CTA: the larger of a panel's and a tile's.
+constexpr size_t chain_smem_bytes() {
+    return sizeof(PanelSmem<int32_t, CHAIN_THREADS>) > sizeof(TileSmem<int32_t, 64, 32>)
+               ? sizeof(PanelSmem<int32_t, CHAIN_THREADS>)
+               : sizeof(TileSmem<int32_t, 64, 32>);
+}
+
+// The chain's phases in order; metric m of a metric-major batch is item
+// (w / count) of phase-wide index w. Grid: one CTA per SM, co-resident.
+__global__ void __launch_bounds__(CHAIN_THREADS, 1)
+    k_sn_chain(DevTopo D, SnDev S, const int32_t* __restrict__ items, const ChainPhase* __restrict__ phases,
+               int32_t nphases, int32_t* up, int32_t* dn, int* __restrict__ err, unsigned int* bar,
+               long long spin_limit, int32_t barrier_extra, int32_t metrics) {
+    extern __shared__ __align__(16) unsigned char chain_smem[];
+    auto& psm = *reinterpret_cast<PanelSmem<int32_t, CHAIN_THREADS>*>(chain_smem);
+    auto& tsm = *reinterpret_cast<TileSmem<int32_t, 64, 32>*>(chain_smem);
+    int e = 0;
+    for (int32_t p = 0; p < nphases; p++) {
+        const ChainPhase ph = phases[p];
+        const int64_t total = ph.count * metrics;
+        for (int64_t w = blockIdx.x; w < total; w += gridDim.x) {
+            const int64_t m = w / ph.count, i = w - m * ph.count;
+            int32_t* upm = up + m * D.m_plus;
+            int32_t* dnm = dn + m * D.m_plus;
+            const int32_t* it = items + 3 * (ph.off + i);
+            if (ph.kind == SN_PANEL) chain_panel<CHAIN_THREADS>(D, S, it, ph.panel, upm, dnm, e, psm);
+            else if (ph.kind == SN_TRAIL) chain_tile<false>(D, S, it, ph.panel, upm, dnm, e, tsm);
+            else chain_tile<true>(D, S, it, 0, upm, dnm, e, tsm);
+        }
+        if (p + 1 < nphases && !chain_barrier(bar, spin_limit, barrier_extra, err)) break;
     }
     if (e) atomicOr(err, e);
 }

@@ -154,12 +154,14 @@ SnPlan* build_supernodal_plan(int64_t n, const int64_t* first, const int32_t* he
     std::vector<int64_t> warp_count(L, 0);
     for (int64_t s = 0; s < ns; s++)
         if (warp_ok(s)) warp_count[lvl[s]]++;
-    std::vector<std::vector<int32_t>> small(L), big(L), out_small(L), out_big(L), warp(L);
+    const int64_t tcap = std::min<int64_t>(prm.thread_cap, SN_THREAD_CAP);
+    std::vector<std::vector<int32_t>> small(L), big(L), out_small(L), out_big(L), warp(L), thread(L);
     for (int64_t s = 0; s < ns; s++) {
         const int32_t l = lvl[s];
         if (kv[s] == 1 && bv[s] < 2) continue;  // no triangle has its lowest vertex here
         if (warp_ok(s) && warp_count[l] >= prm.warp_min_count) {
-            warp[l].insert(warp[l].end(), {(int32_t)s, 0, 0});
+            if (sn_trapezoid(kv[s], bv[s]) <= tcap) thread[l].insert(thread[l].end(), {(int32_t)s, 0, 0});
+            else warp[l].insert(warp[l].end(), {(int32_t)s, 0, 0});
             continue;
         }
         if (kv[s] >= 2 && kv[s] <= SN_SMALL_K) small[l].push_back((int32_t)s);
@@ -193,6 +195,7 @@ SnPlan* build_supernodal_plan(int64_t n, const int64_t* first, const int32_t* he
         P->launches.push_back(la);
     };
     for (int32_t l = 0; l < L; l++) {
+        add(SN_THREAD, l, 0, thread[l]);
         add(SN_WARP, l, 0, warp[l]);
         std::vector<int32_t> v;
         for (int32_t s : small[l]) v.insert(v.end(), {s, 0, 0});
@@ -223,6 +226,72 @@ SnPlan* build_supernodal_plan(int64_t n, const int64_t* first, const int32_t* he
         add(SN_OUT_BIG, l, 0, out_big[l]);
     }
     P->items = (int64_t)items.size() / 3;
+    // the persistent top: from the lowest level such that it and every level
+    // above it have no warp-kernel launch and no launch of more than
+    // chain_max_items items, the levels run as phases of k_sn_chain (int32
+    // storage): panels in CHAIN_THREADS-column items, trailing and outgoing
+    // products in 64 x 64 tiles
+    P->chain_level = L;
+    if (prm.chain_max_items > 0) {
+        std::vector<char> level_ok(L, 1);
+        for (const SnLaunch& la : P->launches)
+            if (la.kind == SN_WARP || la.kind == SN_THREAD || la.kind == SN_INT_SMALL || la.count > prm.chain_max_items)
+                level_ok[la.level] = 0;
+        while (P->chain_level > 0 && level_ok[P->chain_level - 1]) P->chain_level--;
+    }
+    P->chain_from = P->launches.size();
+    for (size_t i = 0; i < P->launches.size(); i++)
+        if (P->launches[i].level >= P->chain_level) {
+            P->chain_from = i;
+            break;
+        }
+    std::vector<int32_t> citems;
+    std::vector<ChainPhase> phases;
+    if (P->chain_from < P->launches.size()) {
+        std::vector<std::vector<int32_t>> at(L - P->chain_level);  // supernodes of each chain level
+        for (int64_t s = 0; s < ns; s++)
+            if (lvl[s] >= P->chain_level) at[lvl[s] - P->chain_level].push_back((int32_t)s);
+        auto phase = [&](int kind, int panel, const std::vector<int32_t>& v) {
+            if (v.empty()) return;
+            phases.push_back(ChainPhase{kind, panel, (int64_t)citems.size() / 3, (int64_t)v.size() / 3});
+            citems.insert(citems.end(), v.begin(), v.end());
+        };
+        for (int32_t l = P->chain_level; l < L; l++) {
+            const auto& ss = at[l - P->chain_level];
+            int32_t maxp = 0;
+            for (int32_t s : ss)
+                if (kv[s] > SN_SMALL_K) maxp = std::max<int32_t>(maxp, (int32_t)ceil_div(kv[s], SN_P));
+            for (int32_t pi = 0; pi < maxp; pi++) {
+                std::vector<int32_t> pv, tv;
+                for (int32_t s : ss) {
+                    const int64_t k = kv[s], b = bv[s];
+                    const int64_t i0 = (int64_t)pi * SN_P;
+                    if (k <= SN_SMALL_K || i0 >= k) continue;
+                    const int64_t pn = std::min<int64_t>(SN_P, k - i0);
+                    const int64_t ncols = (k + b) - (i0 + pn);
+                    const int64_t ct = std::max<int64_t>(1, ceil_div(ncols, CHAIN_THREADS));
+                    for (int64_t c = 0; c < ct; c++) pv.insert(pv.end(), {s, (int32_t)c, 0});
+                    const int64_t nrows = k - i0 - pn;
+                    if (nrows > 0) {
+                        const int64_t tr_n = ceil_div(nrows, 64), tc_n = ceil_div(ncols, 64);
+                        for (int64_t tr = 0; tr < tr_n; tr++)
+                            for (int64_t tc = tr; tc < tc_n; tc++) tv.insert(tv.end(), {s, (int32_t)tr, (int32_t)tc});
+                    }
+                }
+                phase(SN_PANEL, pi, pv);
+                phase(SN_TRAIL, pi, tv);
+            }
+            std::vector<int32_t> ov;
+            for (int32_t s : ss) {
+                if (bv[s] < 2) continue;
+                const int64_t nt = ceil_div(bv[s], 64);
+                for (int64_t tp = 0; tp < nt; tp++)
+                    for (int64_t tq = tp; tq < nt; tq++) ov.insert(ov.end(), {s, (int32_t)tp, (int32_t)tq});
+            }
+            phase(SN_OUT_BIG, 0, ov);
+        }
+        P->nchain_phases = (int32_t)phases.size();
+    }
     // supernodes by level: whole-CTA ones, then warp ones, then single
     // vertices (k = 1), which a thread each sweeps
     std::vector<int32_t> order;
@@ -266,7 +335,8 @@ SnPlan* build_supernodal_plan(int64_t n, const int64_t* first, const int32_t* he
         (*rc = upload_vec(P, rel_off, &d_rel_off)) || (*rc = upload_vec(P, rel, &d_rel)) ||
         (*rc = upload_vec(P, items, &P->d_items)) || (*rc = upload_vec(P, sid, &d_sid)) ||
         (*rc = upload_vec(P, order, &P->d_sn_order)) || (*rc = upload_vec(P, pot_bu, &P->d_pot_bu)) ||
-        (*rc = upload_vec(P, pot_bd, &P->d_pot_bd))) {
+        (*rc = upload_vec(P, pot_bd, &P->d_pot_bd)) || (*rc = upload_vec(P, citems, &P->d_chain_items)) ||
+        (*rc = upload_vec(P, phases, &P->d_chain_phases))) {
         free_supernodal_plan(P);
         return nullptr;
     }
@@ -286,6 +356,25 @@ SnPlan* build_supernodal_plan(int64_t n, const int64_t* first, const int32_t* he
 
 namespace nwcch {
 
+// CTAs of the plan's persistent launch: one per SM if one fits (0: it cannot
+// run, and its levels are launched one kernel at a time). Sized once per plan.
+static int chain_grid(SnPlan* P) {
+    std::lock_guard<std::mutex> lock(P->chain_mu);
+    if (P->chain_grid >= 0) return P->chain_grid;
+    P->chain_grid = 0;
+    int dev = 0, coop = 0, per_sm = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) != cudaSuccess || !coop ||
+        allow_dynamic_smem((const void*)k_sn_chain, chain_smem_bytes()) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sn_chain, CHAIN_THREADS, chain_smem_bytes()) !=
+            cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    if (per_sm >= 1) P->chain_grid = device_sms();
+    return P->chain_grid;
+}
+
 template <class T>
 int run_supernodal(nwcch_topology* t, SnPlan* P, const int32_t* w, T* up, T* dn, cudaStream_t s, int* err,
                    int metrics) {
@@ -294,7 +383,10 @@ int run_supernodal(nwcch_topology* t, SnPlan* P, const int32_t* w, T* up, T* dn,
     const DevTopo& D = t->d;
     constexpr int CT = sizeof(T) == 4 ? 128 : 32;
     const bool pdl = t->tune.pdl != 0;
-    for (const SnLaunch& la : P->launches) {
+    const bool chain = sizeof(T) == 4 && P->nchain_phases > 0 && chain_grid(P) > 0;
+    const size_t end = chain ? P->chain_from : P->launches.size();
+    for (size_t li = 0; li < end; li++) {
+        const SnLaunch& la = P->launches[li];
         const int32_t* it = P->d_items + 3 * la.off;
         const dim3 grid((unsigned)la.count, metrics);
         cudaError_t e = cudaSuccess;
@@ -312,6 +404,13 @@ int run_supernodal(nwcch_topology* t, SnPlan* P, const int32_t* w, T* up, T* dn,
             case SN_OUT_SMALL:
                 e = launch_pdl(pdl, k_sn_tile<T, 16, 2, true>, grid, dim3(64), 0, s, D, P->dev, it, 0, up, dn, err);
                 break;
+            case SN_THREAD: {
+                constexpr int TT = sizeof(T) == 4 ? 128 : 64;  // 32 KB of staged arcs a block
+                const int64_t blocks = std::min<int64_t>((la.count + TT - 1) / TT, (int64_t)device_sms() * 16);
+                e = launch_pdl(pdl, k_sn_thread<T, TT>, dim3((unsigned)blocks, metrics), dim3(TT), 0, s, D, P->dev,
+                               it, la.count, up, dn, err);
+                break;
+            }
             case SN_WARP: {
                 constexpr int WARPS = sizeof(T) == 4 ? 8 : 4;
                 const int64_t blocks = std::min<int64_t>((la.count + WARPS - 1) / WARPS, (int64_t)device_sms() * 64);
@@ -323,6 +422,29 @@ int run_supernodal(nwcch_topology* t, SnPlan* P, const int32_t* w, T* up, T* dn,
                 return NWCCH_ERR_TOPOLOGY;
         }
         if (e != cudaSuccess) return NWCCH_ERR_CUDA;
+    }
+    if constexpr (sizeof(T) == 4) {
+        if (chain) {
+            // the barrier words start at zero; the launch is cooperative, so
+            // its CTAs are co-resident and the barrier can complete
+            unsigned int* bar = reinterpret_cast<unsigned int*>(slot_counters_of(err) + 8);
+            NWCCH_CUDA_TRY(cudaMemsetAsync(bar, 0, 2 * sizeof(unsigned int), s));
+            cudaLaunchConfig_t cfg = {};
+            cfg.gridDim = dim3((unsigned)P->chain_grid);
+            cfg.blockDim = dim3(CHAIN_THREADS);
+            cfg.dynamicSmemBytes = chain_smem_bytes();
+            cfg.stream = s;
+            cudaLaunchAttribute attr[1];
+            attr[0].id = cudaLaunchAttributeCooperative;
+            attr[0].val.cooperative = 1;
+            cfg.attrs = attr;
+            cfg.numAttrs = 1;
+            NWCCH_CUDA_TRY(cudaLaunchKernelEx(&cfg, k_sn_chain, D, P->dev, (const int32_t*)P->d_chain_items,
+                                              (const ChainPhase*)P->d_chain_phases, P->nchain_phases,
+                                              reinterpret_cast<int32_t*>(up), reinterpret_cast<int32_t*>(dn), err,
+                                              bar, (long long)t->tune.update_spin_limit,
+                                              (int32_t)t->tune.test_barrier_extra, (int32_t)metrics));
+        }
     }
     return cudaGetLastError() == cudaSuccess ? NWCCH_OK : NWCCH_ERR_CUDA;
 }
@@ -336,7 +458,7 @@ int launch_cached(SnPlan* P, const SnGraph& key, cudaStream_t s, const std::func
     SnGraph* hit = nullptr;
     for (auto& g : P->graphs)
         if (g.kind == key.kind && g.storage == key.storage && g.metrics == key.metrics && g.err == key.err &&
-            g.w == key.w && g.up == key.up && g.dn == key.dn)
+            g.w == key.w && g.up == key.up && g.dn == key.dn && g.spin == key.spin && g.extra == key.extra)
             hit = &g;
     if (!hit) {
         cudaStream_t cs;
@@ -370,8 +492,11 @@ int launch_cached(SnPlan* P, const SnGraph& key, cudaStream_t s, const std::func
 template <class T>
 int launch_supernodal(nwcch_topology* t, SnPlan* P, const int32_t* w, T* up, T* dn, cudaStream_t s, int metrics) {
     int* err = stream_slot(t, s).err;
+    if (sizeof(T) == 4 && P->nchain_phases > 0) chain_grid(P);  // sized before any capture starts
     // the launch form (programmatic dependent launches or not) is part of the key
     SnGraph key{SN_GRAPH_CUSTOMIZE, (int)sizeof(T), metrics * 2 + (t->tune.pdl != 0), err, w, up, dn, nullptr, 0};
+    key.spin = t->tune.update_spin_limit;  // the persistent launch's wait bound and test hook are baked in
+    key.extra = t->tune.test_barrier_extra;
     return launch_cached(P, key, s, [&](cudaStream_t cs) { return run_supernodal<T>(t, P, w, up, dn, cs, err, metrics); });
 }
 

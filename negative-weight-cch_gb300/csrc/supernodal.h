@@ -33,12 +33,16 @@ enum SnKind : int {
     SN_OUT_BIG = 3,    // CTA per 64x64 tile of the outgoing boundary x boundary block
     SN_OUT_SMALL = 4,  // CTA per 16x16 tile of the same
     SN_WARP = 5,       // warp per small supernode: the whole supernode in shared memory
+    SN_THREAD = 6,     // thread per tiny supernode: the whole supernode in shared memory
 };
 
 // A supernode whose trapezoid holds at most this many arcs (and k <= 32,
 // b <= 64) is customized by one warp from shared memory in one launch.
 constexpr int SN_WARP_CAP = 512;
-inline int64_t sn_trapezoid(int64_t k, int64_t b) { return k * (k + b - 1) - k * (k - 1) / 2; }
+// A supernode whose trapezoid holds at most this many arcs may be customized
+// by one thread (levels with many of them: most of a road-like graph).
+constexpr int SN_THREAD_CAP = 32;
+__host__ __device__ inline int64_t sn_trapezoid(int64_t k, int64_t b) { return k * (k + b - 1) - k * (k - 1) / 2; }
 
 struct SnLaunch {
     int kind;
@@ -62,6 +66,8 @@ struct SnGraph {
     const void* dn;
     cudaGraphExec_t exec;
     uint64_t last_use;
+    long long spin = 0;  // device wait bound and test hook of the persistent launch
+    int extra = 0;
 };
 
 // Schedule choices of a plan (measured per topology; results never depend
@@ -72,7 +78,28 @@ struct SnGraph {
 struct SnPlanParams {
     int32_t warp_cap = SN_WARP_CAP;
     int64_t warp_min_count = 1024;
+    // supernodes of such levels whose trapezoid holds at most thread_cap
+    // (<= SN_THREAD_CAP) arcs take the thread kernel instead (0: none)
+    int32_t thread_cap = 16;
+    // levels near the root whose launches each hold at most this many items
+    // (and no warp-kernel launch) run as one persistent launch, k_sn_chain
+    // (int32 storage); 0: every level launches its kernels. Off by default:
+    // on the 24M road-like graph the launches are faster (one CTA per SM runs
+    // a phase's items in rounds, where separate launches keep several tiles
+    // per SM in flight); the autotuner tries both.
+    int64_t chain_max_items = 0;
 };
+
+// One phase of the persistent top-of-tree launch (the items of one former
+// launch; consecutive phases are separated by a grid barrier).
+struct ChainPhase {
+    int32_t kind;   // SN_PANEL, SN_TRAIL or SN_OUT_BIG
+    int32_t panel;  // panel index (SN_PANEL, SN_TRAIL)
+    int64_t off;    // first item (int32 triples) in the chain's item array
+    int64_t count;  // items
+};
+
+constexpr int CHAIN_THREADS = 256;  // threads of a chain CTA = panel columns of a chain panel item
 
 struct SnPlan {
     SnPlanParams params;
@@ -99,6 +126,16 @@ struct SnPlan {
     int32_t* d_pot_bd = nullptr;
     int32_t* d_sn_order = nullptr;
     std::vector<SnLaunch> launches;
+    // the persistent top of the plan: launches[chain_from..] (levels >=
+    // chain_level) as phases of k_sn_chain for int32 storage; the other
+    // storage runs them as launches
+    size_t chain_from = 0;
+    int32_t chain_level = 0;
+    int32_t nchain_phases = 0;
+    int32_t* d_chain_items = nullptr;
+    ChainPhase* d_chain_phases = nullptr;
+    int chain_grid = -1;  // CTAs of the chain launch (-1: not sized yet, 0: cannot run)
+    std::mutex chain_mu;
     SnDev dev{};
     int32_t* d_items = nullptr;
     std::vector<void*> allocations;
@@ -127,14 +164,15 @@ template <class T>
 int query_sn_async(nwcch_topology* t, const T* up, const T* dn, const int32_t* s_rank, const int32_t* t_rank,
                    int64_t nq, int64_t* dist, cudaStream_t s, bool allow_alloc, bool* used);
 
-// Enqueues the batched query pipeline of query_top.cu (int32 storage): the
+// Enqueues the batched query pipeline of query_top.cu (int32 storage; counts
+// its kernel launches in *launches): the
 // lower part of every chain per warp, the top supernodes as (min,+) products
 // over tiles of chains, the meet per query. Its kernels return at once when
 // the metric needs 64-bit labels (maxabs, on the device). *used = false when
 // the batch is not its case (nothing enqueued).
 int query_top_async(nwcch_topology* t, const int32_t* up, const int32_t* dn, const int32_t* s_rank,
                     const int32_t* t_rank, int64_t nq, int64_t* dist, const unsigned int* maxabs, int* err,
-                    cudaStream_t s, bool* used);
+                    cudaStream_t s, bool* used, int64_t* launches);
 
 // The same through a CUDA graph captured once per (w, up, dn) binding and
 // error word (the slot of stream s) and replayed afterwards; when s is itself

@@ -54,12 +54,34 @@ void release(nwcch_topology* t) {
 
 }  // namespace
 
+// Allocates and zeroes one more block of kStreamSlots slots (caller holds
+// t->slot_mu).
+static int add_slot_block(nwcch_topology* t) {
+    void* p = nullptr;
+    const size_t bytes = (size_t)kStreamSlots * kSlotBytes;
+    if (cudaMalloc(&p, bytes) != cudaSuccess) return NWCCH_ERR_NOMEM;
+    if (cudaMemset(p, 0, bytes) != cudaSuccess || setup_copies_done() != cudaSuccess) {
+        cudaFree(p);
+        return NWCCH_ERR_CUDA;
+    }
+    t->allocations.push_back(p);
+    t->device_bytes += bytes;
+    char* base = static_cast<char*>(p);
+    for (int i = 0; i < kStreamSlots; i++) {
+        StreamSlot slot;
+        slot.err = reinterpret_cast<int*>(base + (size_t)i * kSlotBytes);
+        slot.counters = slot_counters_of(slot.err);
+        t->slots.push_back(slot);
+    }
+    return NWCCH_OK;
+}
+
 StreamSlot stream_slot(nwcch_topology* t, cudaStream_t stream) {
     std::lock_guard<std::mutex> lock(t->slot_mu);
     const size_t used = t->slot_stream.size();
     for (size_t i = 0; i < used; i++)
         if (t->slot_stream[i] == stream) return t->slots[i];
-    if (used < t->slots.size()) {
+    if (used < t->slots.size() || add_slot_block(t) == NWCCH_OK) {
         t->slot_stream.push_back(stream);
         return t->slots[used];
     }
@@ -162,16 +184,8 @@ extern "C" int nwcch_topology_create(int64_t n, const int64_t* first, const int3
         t->sn_plan = build_supernodal_plan(n, first, head, parent, SnPlanParams{}, &rc);
         if (rc) break;
         t->device_bytes += static_cast<SnPlan*>(t->sn_plan)->bytes;
-        // per-stream slots: 256 bytes each, the error word first and the
-        // 16 counters from byte 128
-        const std::vector<int64_t> zeros((size_t)kStreamSlots * 32, 0);
-        if ((rc = upload(t, zeros.data(), zeros.size(), &p64))) break;
-        for (int i = 0; i < kStreamSlots; i++) {
-            StreamSlot slot;
-            slot.err = reinterpret_cast<int*>(p64 + 32 * i);
-            slot.counters = reinterpret_cast<unsigned long long*>(p64 + 32 * i + 16);
-            t->slots.push_back(slot);
-        }
+        // per-stream slots (layout in topology.h)
+        if ((rc = add_slot_block(t))) break;
         if (setup_copies_done() != cudaSuccess) rc = NWCCH_ERR_CUDA;
     } while (false);
     if (rc != NWCCH_OK) {
@@ -222,11 +236,15 @@ extern "C" int nwcch_tune_set(nwcch_topology* t, int key, int64_t value) {
     if (!t) return NWCCH_ERR_ARG;
     switch (key) {
         case NWCCH_TUNE_SN_WARP_CAP:
-        case NWCCH_TUNE_SN_WARP_MIN_COUNT: {
+        case NWCCH_TUNE_SN_WARP_MIN_COUNT:
+        case NWCCH_TUNE_SN_CHAIN_MAX_ITEMS:
+        case NWCCH_TUNE_SN_THREAD_CAP: {
             if (value < 0 || !t->sn_plan) return NWCCH_ERR_ARG;
             SnPlanParams prm = static_cast<SnPlan*>(t->sn_plan)->params;
             if (key == NWCCH_TUNE_SN_WARP_CAP) prm.warp_cap = (int32_t)std::min<int64_t>(value, SN_WARP_CAP);
-            else prm.warp_min_count = value;
+            else if (key == NWCCH_TUNE_SN_WARP_MIN_COUNT) prm.warp_min_count = value;
+            else if (key == NWCCH_TUNE_SN_THREAD_CAP) prm.thread_cap = (int32_t)std::min<int64_t>(value, SN_THREAD_CAP);
+            else prm.chain_max_items = value;
             return replan(t, prm);
         }
         case NWCCH_TUNE_QUERY_DENSE_ROWS:
@@ -314,10 +332,15 @@ extern "C" int nwcch_tune_get(const nwcch_topology* t, int key, int64_t* value) 
         case NWCCH_TUNE_BATTERY_POOL: *value = t->tune.battery_pool; return NWCCH_OK;
         case NWCCH_TUNE_BATTERY_BUFFER: *value = t->tune.battery_buffer; return NWCCH_OK;
         case NWCCH_TUNE_SN_WARP_CAP:
-        case NWCCH_TUNE_SN_WARP_MIN_COUNT: {
+        case NWCCH_TUNE_SN_WARP_MIN_COUNT:
+        case NWCCH_TUNE_SN_CHAIN_MAX_ITEMS:
+        case NWCCH_TUNE_SN_THREAD_CAP: {
             if (!t->sn_plan) return NWCCH_ERR_ARG;
             const SnPlanParams& prm = static_cast<const SnPlan*>(t->sn_plan)->params;
-            *value = key == NWCCH_TUNE_SN_WARP_CAP ? prm.warp_cap : prm.warp_min_count;
+            *value = key == NWCCH_TUNE_SN_WARP_CAP          ? prm.warp_cap
+                     : key == NWCCH_TUNE_SN_WARP_MIN_COUNT ? prm.warp_min_count
+                     : key == NWCCH_TUNE_SN_THREAD_CAP     ? prm.thread_cap
+                                                           : prm.chain_max_items;
             return NWCCH_OK;
         }
         default: return NWCCH_ERR_ARG;
@@ -341,6 +364,13 @@ extern "C" int nwcch_topology_info(const nwcch_topology* t, int64_t* info, int64
         info[10] = p ? (int64_t)p->launches.size() : 0;
         info[11] = p ? p->rel_entries : 0;
     }
+    if (len >= 15) {
+        const auto* p = static_cast<const SnPlan*>(t->sn_plan);
+        info[12] = p ? p->chain_level : 0;      // lowest level of the persistent launch (= levels: none)
+        info[13] = p ? p->nchain_phases : 0;    // its phases
+        info[14] = p ? (int64_t)p->chain_from : 0;  // launches before it (int32 storage)
+    }
+    if (len >= 16) info[15] = t->last_query_launches.load();  // kernels of the latest batched-query call
     return NWCCH_OK;
 }
 

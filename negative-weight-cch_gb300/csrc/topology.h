@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
 #include <mutex>
 #include <vector>
 
@@ -58,6 +59,16 @@ struct StreamSlot {
     unsigned long long* counters = nullptr;
 };
 
+// Layout of a slot (256 bytes): the error word at byte 0, the counters from
+// byte 128. Counters: [0] and [1] scan results, [3] the query range flag,
+// [8] the two 32-bit words (arrivals, generation) of the persistent
+// customization launch's grid barrier.
+constexpr int kSlotBytes = 256;
+constexpr int kSlotCounterOffset = 128;
+inline unsigned long long* slot_counters_of(int* err) {
+    return reinterpret_cast<unsigned long long*>(reinterpret_cast<char*>(err) + kSlotCounterOffset);
+}
+
 }  // namespace nwcch
 
 struct nwcch_topology {
@@ -82,6 +93,7 @@ struct nwcch_topology {
     size_t device_bytes = 0;
     void* sn_plan = nullptr;                  // nwcch::SnPlan (supernodal customization)
     std::mutex mu;                            // serialises lazily built plans
+    std::atomic<int64_t> last_query_launches{0};  // kernels the latest batched-query call enqueued
     void* plans = nullptr;                    // owned by the modules that build plans
     void (*free_plans)(nwcch_topology*) = nullptr;
     void* query_plans = nullptr;              // query_top.cu: top-supernode plans of batched queries
@@ -96,9 +108,10 @@ namespace nwcch {
 // Slots preallocated per handle (one per stream that enqueues work on it).
 constexpr int kStreamSlots = 64;
 
-// The slot of `stream` (bound on first use); error words of the calls on a
-// stream beyond the first kStreamSlots streams fall back to the last slot,
-// shared, which only merges their status reports.
+// The slot of `stream` (bound on first use). Slots come in blocks of
+// kStreamSlots; when every slot is bound, another block is allocated, so no
+// two streams ever share one (their counters are scratch of in-flight work).
+// Only if that allocation fails do the further streams share the last slot.
 StreamSlot stream_slot(nwcch_topology* t, cudaStream_t stream);
 
 // Reads and clears the error word of `stream`'s slot (synchronizes `stream`).

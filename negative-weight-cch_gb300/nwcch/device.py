@@ -161,11 +161,17 @@ class DeviceTopology:
 
     def refresh_info(self):
         """Re-reads the handle's figures (the plan's change when re-planned)."""
-        info = np.zeros(12, np.int64)
-        _lib.check(_lib.lib().nwcch_topology_info(self.handle, _lib.ptr(info), 12), "topology_info")
+        info = np.zeros(16, np.int64)
+        _lib.check(_lib.lib().nwcch_topology_info(self.handle, _lib.ptr(info), 16), "topology_info")
         (self.n, self.m_plus, self.m, self.triangles, self.levels, self.depth, self.max_row,
          self.device_bytes, self.supernodes, self.sn_levels, self.sn_launches,
-         self.rel_entries) = (int(v) for v in info)
+         self.rel_entries, self.chain_level, self.chain_phases, self.chain_from, _) = (int(v) for v in info)
+
+    def last_query_launches(self) -> int:
+        """Kernels the latest batched-query call on this handle enqueued."""
+        info = np.zeros(16, np.int64)
+        _lib.check(_lib.lib().nwcch_topology_info(self.handle, _lib.ptr(info), 16), "topology_info")
+        return int(info[15])
 
     # name -> (key, dtype, length from the handle's figures)
     _ARRAYS = {"tail": (0, np.int32), "depth": (1, np.int32), "hdep": (2, np.int32), "doff": (3, np.int64),

@@ -30,8 +30,9 @@ from .device import DeviceTopology, Metric
 KEYS = {"query_dense_rows": 1, "query_smem_labels_max": 2, "update_budget_ns": 3, "query_occupancy": 4,
         "query_cta_max": 5, "sn_warp_cap": 6, "sn_warp_min_count": 7, "pdl": 8, "query_cta_wide_max": 9,
         "query_cta_dense_rows": 10, "battery_pool": 11, "battery_buffer": 12, "update_dense_min": 13,
-        "update_spin_limit": 14, "test_barrier_extra": 15, "query_top_chains": 16}
-PLAN_KEYS = {"sn_warp_cap", "sn_warp_min_count"}
+        "update_spin_limit": 14, "test_barrier_extra": 15, "query_top_chains": 16, "sn_chain_max_items": 17,
+        "sn_thread_cap": 18}
+PLAN_KEYS = {"sn_warp_cap", "sn_warp_min_count", "sn_chain_max_items", "sn_thread_cap"}
 
 _lib.register("nwcch_tune_set", [C.c_void_p, C.c_int, C.c_int64])
 _lib.register("nwcch_tune_get", [C.c_void_p, C.c_int, C.POINTER(C.c_int64)])
@@ -50,7 +51,7 @@ def set(topo: DeviceTopology, key: str, value: int) -> None:  # noqa: A001 - mir
 
 
 def tune_customize(topo: DeviceTopology, w, caps=(0, 128, 256, 512), min_counts=(0, 1024, 16384),
-                   reps: int = 3) -> dict:
+                   reps: int = 3, chains=(0, 1536), threads=(0, 32)) -> dict:
     """Re-plans the customization with each small-supernode schedule (which
     supernodes one warp customizes: trapezoid of at most `cap` arcs, in
     levels with at least `min_count` of them; cap 0 = none), times the
@@ -79,6 +80,38 @@ def tune_customize(topo: DeviceTopology, w, caps=(0, 128, 256, 512), min_counts=
     best = min(trials, key=lambda r: r["ms"])
     set(topo, "sn_warp_cap", best["sn_warp_cap"])
     set(topo, "sn_warp_min_count", best["sn_warp_min_count"])
+    # then the tiny supernodes of the warp levels: a thread each, or a warp
+    thread_before = get(topo, "sn_thread_cap")
+    thread_ms = {}
+    for c in threads:
+        set(topo, "sn_thread_cap", c)
+        thread_ms[c] = _time(torch, lambda: topo.customize(wt, "int32", out=m, sync=False), reps)
+        if not (torch.equal(ref[0], m.up) and torch.equal(ref[1], m.dn)):
+            set(topo, "sn_thread_cap", thread_before)
+            raise AssertionError(f"thread kernel cap {c} changed the values")
+        trials.append({"sn_warp_cap": best["sn_warp_cap"], "sn_warp_min_count": best["sn_warp_min_count"],
+                       "sn_thread_cap": c, "ms": round(thread_ms[c], 4), "launches": topo.sn_launches})
+    if thread_ms:
+        tc = min(thread_ms, key=thread_ms.get)
+        set(topo, "sn_thread_cap", tc)
+        best = {**best, "sn_thread_cap": tc, "ms": round(thread_ms[tc], 4)}
+    # then the persistent launch of the levels near the root (0: none)
+    chain_before = get(topo, "sn_chain_max_items")
+    chain_ms = {}
+    for c in chains:
+        set(topo, "sn_chain_max_items", c)
+        chain_ms[c] = _time(torch, lambda: topo.customize(wt, "int32", out=m, sync=False), reps)
+        if not (torch.equal(ref[0], m.up) and torch.equal(ref[1], m.dn)):
+            set(topo, "sn_chain_max_items", chain_before)
+            raise AssertionError(f"persistent top launch {c} changed the values")
+        trials.append({"sn_warp_cap": best["sn_warp_cap"], "sn_warp_min_count": best["sn_warp_min_count"],
+                       "sn_chain_max_items": c, "ms": round(chain_ms[c], 4), "launches": topo.sn_launches,
+                       "chain_level": topo.chain_level, "chain_phases": topo.chain_phases})
+    if chain_ms:
+        chain = min(chain_ms, key=chain_ms.get)
+        set(topo, "sn_chain_max_items", chain)
+        best = {**best, "sn_chain_max_items": chain, "ms": round(chain_ms[chain], 4),
+                "chain_level": topo.chain_level, "chain_phases": topo.chain_phases}
     # then the launch form on the chosen plan: programmatic dependent launches
     pdl_before = get(topo, "pdl")
     forms = {}
@@ -89,7 +122,8 @@ def tune_customize(topo: DeviceTopology, w, caps=(0, 128, 256, 512), min_counts=
             set(topo, "pdl", pdl_before)
             raise AssertionError(f"launch form pdl={pdl} changed the values")
         trials.append({"sn_warp_cap": best["sn_warp_cap"], "sn_warp_min_count": best["sn_warp_min_count"],
-                       "pdl": pdl, "ms": round(forms[pdl], 4), "launches": topo.sn_launches})
+                       "sn_chain_max_items": get(topo, "sn_chain_max_items"), "pdl": pdl, "ms": round(forms[pdl], 4),
+                       "launches": topo.sn_launches})
     pdl = min(forms, key=forms.get)
     set(topo, "pdl", pdl)
     best = {**best, "pdl": pdl, "ms": round(forms[pdl], 4)}

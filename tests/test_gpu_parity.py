@@ -476,7 +476,7 @@ def test_customize_schedules_keep_values(gpu, oracle):
     T = DeviceTopology.from_dict(top)
     oup, odn = oracle.customize(oracle.Topo.from_dict(top), g["w"])
     r = tune.tune_customize(T, g["w"], caps=(0, 512), min_counts=(0, 4096), reps=1)
-    assert len(r["trials"]) == 3 + 2  # plans, then the two launch forms
+    assert len(r["trials"]) == 3 + 2 + 2 + 2  # plans, thread kernel off/on, persistent top off/on, launch forms
     assert tune.get(T, "sn_warp_cap") == r["best"]["sn_warp_cap"]
     for cap, cnt, pdl in ((512, 0, 0), (0, 0, 1), (128, 64, 1), (512, 0, 1)):
         tune.set(T, "sn_warp_cap", cap)
