@@ -209,6 +209,12 @@ int nwcch_check(nwcch_topology* t, void* stream);
  * (<= 32) take a kernel with one thread per supernode instead (0: none).
  * Default 16. Setting it rebuilds the plan. */
 #define NWCCH_TUNE_SN_THREAD_CAP 18
+/* Batches of at most this many queries (int32 storage) run the streaming
+ * query kernel: a CTA per chain, the chain's rows streamed into shared
+ * memory by bulk asynchronous copies, both chains of a query at once. Used
+ * when the topology fits its shared memory (labels, boundary positions and
+ * the copy ring; rows of at most 12,280 arcs). 0: off. Default 64. */
+#define NWCCH_TUNE_QUERY_STREAM_MAX 19
 int nwcch_tune_set(nwcch_topology* t, int key, int64_t value);
 int nwcch_tune_get(const nwcch_topology* t, int key, int64_t* value);
 

@@ -1066,9 +1066,9 @@ extern "C" int nwcch_battery_customize(nwcch_topology* t, const double* w_dev, d
     void* tri = nullptr;
     BatStatus host{};
     rc = NWCCH_OK;
-    if (cudaMallocAsync(&next, sizeof(unsigned long long) * std::max<int32_t>(1, t->levels), s) != cudaSuccess ||
-        cudaMallocAsync(&tri, (size_t)slots * std::max<int64_t>(1, P->max_down) * sizeof(int2), s) != cudaSuccess ||
-        cudaMallocAsync(&gbuf, (size_t)slots * gcap * sizeof(Rich), s) != cudaSuccess)
+    if (scratch_alloc(&next, sizeof(unsigned long long) * std::max<int32_t>(1, t->levels), s) != cudaSuccess ||
+        scratch_alloc(&tri, (size_t)slots * std::max<int64_t>(1, P->max_down) * sizeof(int2), s) != cudaSuccess ||
+        scratch_alloc(&gbuf, (size_t)slots * gcap * sizeof(Rich), s) != cudaSuccess)
         rc = NWCCH_ERR_NOMEM;
     for (int attempt = 0; rc == NWCCH_OK; attempt++) {
         rc = run_levels(t, b, P, w_dev, static_cast<Rich*>(gbuf), gcap, static_cast<int2*>(tri),
@@ -1093,7 +1093,7 @@ extern "C" int nwcch_battery_customize(nwcch_topology* t, const double* w_dev, d
             gcap *= 4;
             cudaFreeAsync(gbuf, s);
             gbuf = nullptr;
-            if (cudaMallocAsync(&gbuf, (size_t)slots * gcap * sizeof(Rich), s) != cudaSuccess)
+            if (scratch_alloc(&gbuf, (size_t)slots * gcap * sizeof(Rich), s) != cudaSuccess)
                 rc = NWCCH_ERR_NOMEM;
         }
     }
@@ -1167,13 +1167,13 @@ extern "C" int nwcch_battery_query(nwcch_topology* t, const nwcch_battery* b, co
     int* err = stream_slot(t, s).err;
     void* scratch = nullptr;
     if (nq <= QUERY_CTA_MAX) {
-        NWCCH_CUDA_TRY(cudaMallocAsync(&scratch, (size_t)(nq * per_query), s));
+        NWCCH_CUDA_TRY(scratch_alloc(&scratch, (size_t)(nq * per_query), s));
         k_bat_query_cta<<<(unsigned)nq, 32 * QUERY_CTA_WARPS, 0, s>>>(
             t->d, B, s_rank_dev, t_rank_dev, b0_dev, nq, out_dev, static_cast<unsigned char*>(scratch), per_query, err);
     } else {
         const int64_t warps = std::min<int64_t>(nq, (int64_t)t->sms * 16);
         const int64_t blocks = (warps + QUERY_WARPS - 1) / QUERY_WARPS;
-        NWCCH_CUDA_TRY(cudaMallocAsync(&scratch, (size_t)(blocks * QUERY_WARPS * per_query), s));
+        NWCCH_CUDA_TRY(scratch_alloc(&scratch, (size_t)(blocks * QUERY_WARPS * per_query), s));
         k_bat_query<<<(unsigned)blocks, 32 * QUERY_WARPS, 0, s>>>(
             t->d, B, s_rank_dev, t_rank_dev, b0_dev, nq, out_dev, static_cast<unsigned char*>(scratch), per_query, err);
     }

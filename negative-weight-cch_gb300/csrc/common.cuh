@@ -6,6 +6,7 @@
 
 #include <map>
 #include <mutex>
+#include <tuple>
 #include <utility>
 
 #include "nwcch.h"
@@ -150,6 +151,66 @@ inline cudaError_t allow_dynamic_smem(const void* kernel, size_t bytes) {
     if (bytes <= g) return cudaSuccess;
     e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
     if (e == cudaSuccess) g = bytes;
+    return e;
+}
+
+// Blocks per SM of `kernel` at `threads` threads and `smem` bytes of dynamic
+// shared memory, asked once per (kernel, shape, device) and kept: the query
+// paths size every launch by it, and a call of a latency-bound path should
+// not wait on the occupancy calculator.
+inline cudaError_t blocks_per_sm(const void* kernel, int threads, size_t smem, int* out) {
+    static std::mutex mu;
+    static std::map<std::tuple<const void*, int, size_t, int>, int> known;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> lock(mu);
+    const auto key = std::make_tuple(kernel, threads, smem, dev);
+    auto it = known.find(key);
+    if (it != known.end()) {
+        *out = it->second;
+        return cudaSuccess;
+    }
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(out, kernel, threads, smem);
+    if (e == cudaSuccess) known[key] = *out;
+    return e;
+}
+
+// Stream-ordered scratch of the query paths, from a memory pool of this
+// library (one per device) that keeps up to kScratchKeep bytes of freed
+// memory for the next calls instead of returning it to the driver at every
+// synchronization: a small query batch then allocates without mapping pages.
+constexpr uint64_t kScratchKeep = (uint64_t)512 << 20;
+inline cudaError_t scratch_alloc(void** p, size_t bytes, cudaStream_t s) {
+    static std::mutex mu;
+    static std::map<int, cudaMemPool_t> pools;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    cudaMemPool_t pool = nullptr;
+    {
+        std::lock_guard<std::mutex> lock(mu);
+        auto it = pools.find(dev);
+        if (it != pools.end()) {
+            pool = it->second;
+        } else {
+            cudaMemPoolProps props = {};
+            props.allocType = cudaMemAllocationTypePinned;
+            props.location.type = cudaMemLocationTypeDevice;
+            props.location.id = dev;
+            if ((e = cudaMemPoolCreate(&pool, &props)) != cudaSuccess) return e;
+            uint64_t keep = kScratchKeep;
+            cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+            pools[dev] = pool;
+        }
+    }
+    return cudaMallocFromPoolAsync(p, bytes, pool, s);
+}
+template <class T>
+inline cudaError_t scratch_alloc(T** p, size_t bytes, cudaStream_t s) {
+    void* v = nullptr;
+    const cudaError_t e = scratch_alloc(&v, bytes, s);
+    *p = static_cast<T*>(v);
     return e;
 }
 

@@ -64,7 +64,7 @@ extern "C" int nwcch_edge_arcs_device(int64_t n, const int64_t* off_dev, const i
     if (n == 0) return NWCCH_OK;
     cudaStream_t s = (cudaStream_t)stream;
     int* bad = nullptr;
-    NWCCH_CUDA_TRY(cudaMallocAsync(&bad, sizeof(int), s));
+    NWCCH_CUDA_TRY(scratch_alloc(&bad, sizeof(int), s));
     NWCCH_CUDA_TRY(cudaMemsetAsync(bad, 0, sizeof(int), s));
     const unsigned blocks = (unsigned)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, (int64_t)device_sms() * 32));
     k_edge_arcs<<<blocks, 256, 0, s>>>(n, off_dev, tgt_dev, rank_dev, first_dev, head_dev, e_arc_dev, e_up_dev, bad);

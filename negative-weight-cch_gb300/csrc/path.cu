@@ -281,7 +281,7 @@ int query_paths(nwcch_topology* t, const T* up, const T* dn, const int32_t* s_ra
     const int64_t warps = std::max<int64_t>(1, std::min<int64_t>(nq, (int64_t)t->sms * 16));
     const int64_t blocks = (warps + 3) / 4;
     void* scratch = nullptr;
-    NWCCH_CUDA_TRY(cudaMallocAsync(&scratch, (size_t)(blocks * 4 * per_warp), s));
+    NWCCH_CUDA_TRY(scratch_alloc(&scratch, (size_t)(blocks * 4 * per_warp), s));
     int* err = stream_slot(t, s).err;
     auto* sc = static_cast<unsigned char*>(scratch);
     NWCCH_CUDA_TRY(cudaMemsetAsync(off, 0, sizeof(int64_t), s));

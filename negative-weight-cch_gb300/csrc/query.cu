@@ -98,7 +98,7 @@ int query_plain(nwcch_topology* t, const T* up, const T* dn, const int32_t* s_ra
     const int block = 128;
     const int64_t blocks = (warps * 32 + block - 1) / block;
     void* scratch = nullptr;
-    NWCCH_CUDA_TRY(cudaMallocAsync(&scratch, (size_t)(blocks * (block / 32)) * per_warp * sizeof(int64_t), s));
+    NWCCH_CUDA_TRY(scratch_alloc(&scratch, (size_t)(blocks * (block / 32)) * per_warp * sizeof(int64_t), s));
     k_query_plain<T><<<(unsigned)blocks, block, 0, s>>>(t->d, up, dn, s_rank, t_rank, nq, dist, (int64_t*)scratch,
                                                        stream_slot(t, s).err);
     const cudaError_t launch = cudaGetLastError();
@@ -164,7 +164,7 @@ extern "C" int nwcch_query_batch_i64(nwcch_topology* t, const int64_t* up_dev, c
 // ---------------------------------------------------------------------------
 // Allocation-free query entry point.
 //
-// nwcch_query_batch takes its per-warp label scratch from cudaMallocAsync.
+// nwcch_query_batch takes its per-warp label scratch from a stream-ordered allocation.
 // Some callers cannot allocate at all: a serving loop whose admission control
 // has already handed every byte of device memory to resident metrics, an
 // embedding application whose own allocator owns the device and forbids

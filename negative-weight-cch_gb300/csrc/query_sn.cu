@@ -129,12 +129,14 @@ __global__ void __launch_bounds__(32 * WARPS) k_query_sn32_cta(DevTopo D, SnDev 
     if (e) atomicOr(err, e);
 }
 
+// wide != nullptr: only the queries flagged there (the rest is answered);
+// otherwise every query, unless int32 values fit 32-bit labels.
 template <class T>
 __global__ void k_query_sn(DevTopo D, SnDev S, const T* __restrict__ up, const T* __restrict__ dn,
                            const int32_t* __restrict__ s_rank, const int32_t* __restrict__ t_rank, int64_t nq,
                            int64_t* __restrict__ dist, const unsigned int* __restrict__ maxabs,
-                           int* __restrict__ err, int dense_rows) {
-    if (sizeof(T) == 4 && small_labels(D, maxabs)) return;  // answered by k_query_sn32
+                           int* __restrict__ err, int dense_rows, const int32_t* __restrict__ wide) {
+    if (sizeof(T) == 4 && !wide && small_labels(D, maxabs)) return;  // answered by k_query_sn32
     extern __shared__ __align__(16) unsigned char smraw[];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const int64_t Dp = D.max_depth + 1;
@@ -147,6 +149,7 @@ __global__ void k_query_sn(DevTopo D, SnDev S, const T* __restrict__ up, const T
     const int64_t nwarps = (int64_t)gridDim.x * (blockDim.x >> 5);
     int e = 0;
     for (int64_t q = warp; q < nq; q += nwarps) {
+        if (wide && !wide[q]) continue;
         const int32_t s = s_rank[q], t = t_rank[q];
         if (s < 0 || s >= D.n || t < 0 || t >= D.n) {
             if (lane == 0) dist[q] = INF64;
@@ -193,10 +196,9 @@ static bool sn_query_shape(const nwcch_topology* t, int64_t bytes_per_pos, int* 
 template <class K>
 static int launch_shape(K kernel, int warps, size_t smem, int64_t nq, int64_t* blocks) {
     NWCCH_CUDA_TRY(allow_dynamic_smem((const void*)kernel, smem));
-    int dev = 0, sms = 0, per_sm = 0;
-    NWCCH_CUDA_TRY(cudaGetDevice(&dev));
-    NWCCH_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    NWCCH_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, 32 * warps, smem));
+    int per_sm = 0;
+    const int sms = device_sms();
+    NWCCH_CUDA_TRY(blocks_per_sm((const void*)kernel, 32 * warps, smem, &per_sm));
     const int64_t want = (nq + warps - 1) / warps;
     *blocks = std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)sms * std::max(1, per_sm)));
     return NWCCH_OK;
@@ -214,6 +216,19 @@ int query_sn_async(nwcch_topology* t, const T* up, const T* dn, const int32_t* s
     unsigned int* maxabs = reinterpret_cast<unsigned int*>(slot.counters + 3);
     int* err = slot.err;
     int64_t launches = 0;
+    if (sizeof(T) == 4 && nq <= t->tune.query_stream_max) {
+        // few queries: a CTA per chain, the chains streamed by bulk copies
+        // (its 64-bit fallback flagged per query, no pass over the metric)
+        bool stream_used = false;
+        const int rc = query_stream_async(t, reinterpret_cast<const int32_t*>(up), reinterpret_cast<const int32_t*>(dn),
+                                          s_rank, t_rank, nq, dist, err, s, &stream_used, &launches);
+        if (rc) return rc;
+        if (stream_used) {
+            t->last_query_launches = launches;
+            *used = true;
+            return NWCCH_OK;
+        }
+    }
     if (sizeof(T) == 4) {
         // 32-bit labels when the metric's values allow them (decided on the
         // device: each kernel returns at once when the batch is not its own)
@@ -270,7 +285,7 @@ int query_sn_async(nwcch_topology* t, const T* up, const T* dn, const int32_t* s
             int rc = launch_shape(kern, 4, 0, nq, &blocks);
             if (rc) return rc;
             void* scratch = nullptr;
-            NWCCH_CUDA_TRY(cudaMallocAsync(&scratch, (size_t)(blocks * 4 * per_warp), s));
+            NWCCH_CUDA_TRY(scratch_alloc(&scratch, (size_t)(blocks * 4 * per_warp), s));
             launches++;
             kern<<<(unsigned)blocks, 128, 0, s>>>(t->d, S, u32, d32, s_rank, t_rank, nq, dist, maxabs,
                                                           static_cast<unsigned char*>(scratch), err,
@@ -296,10 +311,26 @@ int query_sn_async(nwcch_topology* t, const T* up, const T* dn, const int32_t* s
     int rc = launch_shape(k_query_sn<T>, w64, smem64, nq, &blocks);
     if (rc) return rc;
     k_query_sn<T><<<(unsigned)blocks, 32 * w64, smem64, s>>>(t->d, S, up, dn, s_rank, t_rank, nq, dist, maxabs,
-                                                             err, t->tune.query_dense_rows);
+                                                             err, t->tune.query_dense_rows, nullptr);
     NWCCH_CUDA_TRY(cudaGetLastError());
     t->last_query_launches = launches + 1;
     *used = true;
+    return NWCCH_OK;
+}
+
+int query_sn64_flagged(nwcch_topology* t, const int32_t* up, const int32_t* dn, const int32_t* s_rank,
+                       const int32_t* t_rank, int64_t nq, int64_t* dist, const int32_t* wide, int* err,
+                       cudaStream_t s) {
+    int w64 = 0;
+    size_t smem64 = 0;
+    if (!t->sn_plan || !sn_query_shape(t, 20, &w64, &smem64)) return NWCCH_ERR_CAPACITY;
+    const SnDev& S = static_cast<SnPlan*>(t->sn_plan)->dev;
+    int64_t blocks = 0;
+    int rc = launch_shape(k_query_sn<int32_t>, w64, smem64, nq, &blocks);
+    if (rc) return rc;
+    k_query_sn<int32_t><<<(unsigned)blocks, 32 * w64, smem64, s>>>(t->d, S, up, dn, s_rank, t_rank, nq, dist,
+                                                                   nullptr, err, t->tune.query_dense_rows, wide);
+    NWCCH_CUDA_TRY(cudaGetLastError());
     return NWCCH_OK;
 }
 

@@ -751,7 +751,7 @@ template <class K>
 int occupancy_grid(K kernel, int threads, size_t smem, int64_t want, int sms, int64_t* blocks) {
     int per_sm = 0;
     NWCCH_CUDA_TRY(allow_dynamic_smem((const void*)kernel, smem));
-    NWCCH_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem));
+    NWCCH_CUDA_TRY(blocks_per_sm((const void*)kernel, threads, smem, &per_sm));
     if (per_sm < 1) return NWCCH_ERR_CAPACITY;
     *blocks = std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)sms * per_sm));
     return NWCCH_OK;
@@ -806,7 +806,7 @@ int query_top_async(nwcch_topology* t, const int32_t* up, const int32_t* dn, con
     size_t total = 0;
     for (size_t r : region) total += round16(r);
     void* scratch = nullptr;
-    NWCCH_CUDA_TRY(cudaMallocAsync(&scratch, total, s));
+    NWCCH_CUDA_TRY(scratch_alloc(&scratch, total, s));
     char* p = static_cast<char*>(scratch);
     auto take = [&](int r) {
         char* at = p;

@@ -147,6 +147,13 @@ SnPlan* build_supernodal_plan(int64_t n, const int64_t* first, const int32_t* he
         }
     }
     P->rel_entries = rel_off[ns];
+    // the chain walk of the streaming query kernel
+    std::vector<QsNode> qnodes(ns);
+    for (int64_t s = 0; s < ns; s++) {
+        const int32_t pv = parent[s0v[s] + kv[s] - 1];
+        const int32_t nx = pv >= 0 ? sid[pv] : -1;
+        qnodes[s] = QsNode{s0v[s], kv[s], bv[s], nx, nx >= 0 ? pv - s0v[nx] : 0, 0, first[s0v[s]]};
+    }
     // work items per level
     P->params = prm;
     const int64_t cap = std::min<int64_t>(prm.warp_cap, SN_WARP_CAP);
@@ -336,7 +343,7 @@ SnPlan* build_supernodal_plan(int64_t n, const int64_t* first, const int32_t* he
         (*rc = upload_vec(P, items, &P->d_items)) || (*rc = upload_vec(P, sid, &d_sid)) ||
         (*rc = upload_vec(P, order, &P->d_sn_order)) || (*rc = upload_vec(P, pot_bu, &P->d_pot_bu)) ||
         (*rc = upload_vec(P, pot_bd, &P->d_pot_bd)) || (*rc = upload_vec(P, citems, &P->d_chain_items)) ||
-        (*rc = upload_vec(P, phases, &P->d_chain_phases))) {
+        (*rc = upload_vec(P, phases, &P->d_chain_phases)) || (*rc = upload_vec(P, qnodes, &P->d_qnodes))) {
         free_supernodal_plan(P);
         return nullptr;
     }

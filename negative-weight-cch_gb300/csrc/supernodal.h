@@ -90,6 +90,15 @@ struct SnPlanParams {
     int64_t chain_max_items = 0;
 };
 
+// A supernode as the streaming query kernel walks it: first vertex, rows,
+// boundary size, next supernode on the chain (-1 at a root) and the entry
+// row there, first arc of its trapezoid. One 32-byte load a step.
+struct QsNode {
+    int32_t s0, k, b, next;
+    int32_t next_row, pad;
+    int64_t base;
+};
+
 // One phase of the persistent top-of-tree launch (the items of one former
 // launch; consecutive phases are separated by a grid barrier).
 struct ChainPhase {
@@ -135,6 +144,8 @@ struct SnPlan {
     int32_t* d_chain_items = nullptr;
     ChainPhase* d_chain_phases = nullptr;
     int chain_grid = -1;  // CTAs of the chain launch (-1: not sized yet, 0: cannot run)
+    // chain walk of the streaming query kernel (one descriptor a supernode)
+    struct QsNode* d_qnodes = nullptr;
     std::mutex chain_mu;
     SnDev dev{};
     int32_t* d_items = nullptr;
@@ -173,6 +184,21 @@ int query_sn_async(nwcch_topology* t, const T* up, const T* dn, const int32_t* s
 int query_top_async(nwcch_topology* t, const int32_t* up, const int32_t* dn, const int32_t* s_rank,
                     const int32_t* t_rank, int64_t nq, int64_t* dist, const unsigned int* maxabs, int* err,
                     cudaStream_t s, bool* used, int64_t* launches);
+
+// Enqueues the streaming query kernel of query_stream.cu for a batch of at
+// most tune.query_stream_max int32-stored queries (a CTA per chain; counts
+// its launches in *launches). *used = false when the batch or the topology is
+// not its case (nothing enqueued).
+int query_stream_async(nwcch_topology* t, const int32_t* up, const int32_t* dn, const int32_t* s_rank,
+                       const int32_t* t_rank, int64_t nq, int64_t* dist, int* err, cudaStream_t s, bool* used,
+                       int64_t* launches);
+
+// Enqueues the 64-bit supernodal query kernel for the queries of a batch
+// flagged in `wide` (int32 storage): the answers of the streaming kernel's
+// queries that met a weight beyond the 32-bit label bound.
+int query_sn64_flagged(nwcch_topology* t, const int32_t* up, const int32_t* dn, const int32_t* s_rank,
+                       const int32_t* t_rank, int64_t nq, int64_t* dist, const int32_t* wide, int* err,
+                       cudaStream_t s);
 
 // The same through a CUDA graph captured once per (w, up, dn) binding and
 // error word (the slot of stream s) and replayed afterwards; when s is itself

@@ -291,6 +291,10 @@ extern "C" int nwcch_tune_set(nwcch_topology* t, int key, int64_t value) {
             if (value < 0) return NWCCH_ERR_ARG;
             t->tune.query_top_chains = value;
             return NWCCH_OK;
+        case NWCCH_TUNE_QUERY_STREAM_MAX:
+            if (value < 0) return NWCCH_ERR_ARG;
+            t->tune.query_stream_max = value;
+            return NWCCH_OK;
         case NWCCH_TUNE_TEST_BARRIER_EXTRA:
             if (value < 0 || value > 1024) return NWCCH_ERR_ARG;
             t->tune.test_barrier_extra = (int32_t)value;
@@ -329,6 +333,7 @@ extern "C" int nwcch_tune_get(const nwcch_topology* t, int key, int64_t* value) 
         case NWCCH_TUNE_UPDATE_SPIN_LIMIT: *value = t->tune.update_spin_limit; return NWCCH_OK;
         case NWCCH_TUNE_TEST_BARRIER_EXTRA: *value = t->tune.test_barrier_extra; return NWCCH_OK;
         case NWCCH_TUNE_QUERY_TOP_CHAINS: *value = t->tune.query_top_chains; return NWCCH_OK;
+        case NWCCH_TUNE_QUERY_STREAM_MAX: *value = t->tune.query_stream_max; return NWCCH_OK;
         case NWCCH_TUNE_BATTERY_POOL: *value = t->tune.battery_pool; return NWCCH_OK;
         case NWCCH_TUNE_BATTERY_BUFFER: *value = t->tune.battery_buffer; return NWCCH_OK;
         case NWCCH_TUNE_SN_WARP_CAP:
