@@ -1018,6 +1018,14 @@ def main():
                        "relaxations_per_s": round(arcs_q * nq / (qms / 1000), 1),
                        "note": "arcs of both ancestor chains (the reference's per-query relaxations); the batched "
                                "form applies each top-supernode weight to a tile of up to 32 chains"},
+        # the batched query as a roofline: algorithmic bytes = one 32-bit
+        # weight read per relaxation of the reference's sweep
+        "query_roofline": {"bound": "hbm", "unit": "GB/s",
+                           "achieved": round(4 * arcs_q * nq / (qms / 1000) / 1e9, 1),
+                           "peak": peak, "frac": round(4 * arcs_q * nq / (qms / 1000) / 1e9 / peak, 4),
+                           "bytes_per_query": round(4 * arcs_q, 1),
+                           "note": "above 1: the tiles of the top supernodes serve each weight read to up to 32 "
+                                   "chains from shared memory (L2 reads, not the reference's per-query reads)"},
         "topology_handle_s": round(R["topo_s"], 3),
         "query_schedule": R["tuned"],
         "customize_schedule": R["cust_tuned"],
@@ -1043,7 +1051,8 @@ def main():
                      "dram_gbs_at_traffic": (round(MEASURED_TRAFFIC[args.workload][0] / (cust / 1000) / 1e9, 1)
                                              if args.workload in MEASURED_TRAFFIC else None),
                      "algorithmic_bytes_per_launch": int(B),
-                     "launch": "one customization: CUDA graph of k_fill2, k_base, k_sn_warp, k_sn_panel, k_sn_tile"},
+                     "launch": "one customization: CUDA graph of k_fill2, k_base, k_sn_thread, k_sn_warp, k_sn_panel, "
+                               "k_sn_tile"},
         "cpu_baseline": {"value": round(cb["value"], 3), "unit": "ms", "cores": cb["cores"], "kind": "port",
                          "sample": f"{cb['runs']} level-parallel customizations (cpp/cch.cpp:468-529) + scans "
                                    f"of the same metric"},

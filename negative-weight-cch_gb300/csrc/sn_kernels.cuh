@@ -69,6 +69,12 @@ __device__ __forceinline__ void atomic_min_t(int64_t* p, int64_t v) {
     atomicMin(reinterpret_cast<long long*>(p), (long long)v);
 }
 
+// First arc of row r of a supernode's trapezoid (rows shrink by one entry a
+// vertex): the closed form of first[s0 + r].
+__device__ __forceinline__ int64_t sn_row_base(int64_t base, int32_t cols, int32_t r) {
+    return base + (int64_t)r * (cols - 1) - (int64_t)r * (r - 1) / 2;
+}
+
 // ------------------------------------------------------------------ panel
 
 // Shared state of one panel block: the panel's diagonal triangle (arcs among
@@ -171,18 +177,20 @@ __device__ bool panel_load(PanelSmem<V, CT>& sm, const T* __restrict__ up, const
     const int tid = threadIdx.x;
     bool bad = false;
     constexpr int DI = SN_P * SN_P / CT;  // diagonal entries per thread
-    {
-        T du[DI], dd[DI];
+    T du[DI], dd[DI];
 #pragma unroll
-        for (int q = 0; q < DI; q++) {
-            const int t = tid + q * CT, a = t >> 5, c = t & 31;
-            du[q] = Lim<T>::INF;
-            dd[q] = Lim<T>::INF;
-            if (a < c && c < pn) {
-                du[q] = LD::ld(up + sm.rowb[a] + c - a - 1);
-                dd[q] = LD::ld(dn + sm.rowb[a] + c - a - 1);
-            }
+    for (int q = 0; q < DI; q++) {
+        const int t = tid + q * CT, a = t >> 5, c = t & 31;
+        du[q] = Lim<T>::INF;
+        dd[q] = Lim<T>::INF;
+        if (a < c && c < pn) {
+            du[q] = LD::ld(up + sm.rowb[a] + c - a - 1);
+            dd[q] = LD::ld(dn + sm.rowb[a] + c - a - 1);
         }
+    }
+    // the diagonal's loads and (for 32-bit values) all of the column's are
+    // in flight together: one round trip to memory for the whole panel
+    auto put_diag = [&]() {
 #pragma unroll
         for (int q = 0; q < DI; q++) {
             const int t = tid + q * CT, a = t >> 5, c = t & 31;
@@ -192,9 +200,10 @@ __device__ bool panel_load(PanelSmem<V, CT>& sm, const T* __restrict__ up, const
                 sm.Dd[a][c] = P::from(dd[q]);
             }
         }
-    }
+    };
+    if (!hasj) put_diag();
     if (hasj) {
-        constexpr int G = 8;  // column loads in flight per group
+        constexpr int G = sizeof(T) == 4 ? SN_P : 8;  // column loads in flight per group
 #pragma unroll
         for (int a0 = 0; a0 < SN_P; a0 += G) {
             T cu[G], cd[G];
@@ -209,6 +218,7 @@ __device__ bool panel_load(PanelSmem<V, CT>& sm, const T* __restrict__ up, const
                     cd[q] = LD::ld(dn + idx);
                 }
             }
+            if (a0 == 0) put_diag();
 #pragma unroll
             for (int q = 0; q < G; q++) {
                 const int a = a0 + q;
@@ -269,12 +279,13 @@ __global__ void __launch_bounds__(CT) k_sn_panel(DevTopo D, SnDev S, const int32
     up += blockIdx.y * D.m_plus;  // metric blockIdx.y of a metric-major batch
     dn += blockIdx.y * D.m_plus;
     const int32_t s = items[3 * blockIdx.x], ct = items[3 * blockIdx.x + 1];
-    const int32_t s0 = S.s0[s], k = S.k[s], cols = k + S.b[s];
+    const QsNode nd = S.node[s];
+    const int32_t k = nd.k, cols = k + nd.b;
     const int i0 = panel * SN_P;
     const int pn = min(SN_P, k - i0);
     const int tid = threadIdx.x;
     int e = 0;
-    if (tid < pn) sm.rowb[tid] = D.first[s0 + i0 + tid];
+    if (tid < pn) sm.rowb[tid] = sn_row_base(nd.base, cols, i0 + tid);
     __syncthreads();
     for (int pass = 0; pass < 128 / CT; pass++) {
         const int j = i0 + pn + ct * 128 + pass * CT + tid;
@@ -319,6 +330,7 @@ template <class T, int TILE, int MT, bool OUT>
 struct TileCtx {
     int32_t s, s0, k, b, cols;
     int ibeg, iend, abase, bbase, alim;
+    int64_t base;  // first arc of the trapezoid
 };
 
 // The tile of work item `it` (a triple: supernode, row tile, column tile).
@@ -327,9 +339,11 @@ __device__ __forceinline__ TileCtx<T, TILE, MT, OUT> tile_ctx(const SnDev& S, co
     TileCtx<T, TILE, MT, OUT> c;
     c.s = it[0];
     const int tr = it[1], tc = it[2];
-    c.s0 = S.s0[c.s];
-    c.k = S.k[c.s];
-    c.b = S.b[c.s];
+    const QsNode nd = S.node[c.s];
+    c.s0 = nd.s0;
+    c.k = nd.k;
+    c.b = nd.b;
+    c.base = nd.base;
     c.cols = c.k + c.b;
     if (OUT) {
         c.ibeg = 0;
@@ -375,7 +389,7 @@ __device__ bool tile_product(const DevTopo& D, const TileCtx<T, TILE, MT, OUT>& 
     for (int i0 = c.ibeg; i0 < c.iend; i0 += CH) {
         const int nch = min(CH, c.iend - i0);
         __syncthreads();
-        if (tid < CH) sm.rowb[tid] = tid < nch ? D.first[c.s0 + i0 + tid] : 0;
+        if (tid < CH) sm.rowb[tid] = tid < nch ? sn_row_base(c.base, c.cols, i0 + tid) : 0;
         __syncthreads();
         bool bad = false;
         // all of a thread's loads are issued before any is used (their
@@ -451,7 +465,7 @@ __device__ void tile_store(const DevTopo& D, const SnDev& S, const TileCtx<T, TI
                 if (fu) atomic_min_t(&up[a], (T)P::to(accU[ii][jj]));
                 if (fd) atomic_min_t(&dn[a], (T)P::to(accD[ii][jj]));
             } else {
-                a = D.first[c.s0 + rr] + (cc - rr - 1);
+                a = sn_row_base(c.base, c.cols, rr) + (cc - rr - 1);
                 if (fu) up[a] = min(LD::ld(up + a), (T)P::to(accU[ii][jj]));
                 if (fd) dn[a] = min(LD::ld(dn + a), (T)P::to(accD[ii][jj]));
             }
@@ -515,10 +529,11 @@ __global__ void __launch_bounds__(32 * WARPS) k_sn_warp(DevTopo D, SnDev S, cons
     int e = 0;
     for (int64_t it = (int64_t)blockIdx.x * WARPS + wib; it < count; it += (int64_t)gridDim.x * WARPS) {
         const int32_t sn = items[3 * it];
-        const int32_t s0 = S.s0[sn], k = S.k[sn], b = S.b[sn];
+        const QsNode nd = S.node[sn];
+        const int32_t k = nd.k, b = nd.b;
         const int32_t width = k + b;
-        const int64_t base = D.first[s0];
-        const int32_t total = (int32_t)(D.first[s0 + k] - base);
+        const int64_t base = nd.base;
+        const int32_t total = (int32_t)sn_trapezoid(k, b);
         // staged 4 loads deep per array, so their latencies overlap
         for (int x0 = 0; x0 < total; x0 += 128) {
             T vu[4], vd[4];
@@ -604,9 +619,10 @@ __global__ void __launch_bounds__(TT) k_sn_thread(DevTopo D, SnDev S, const int3
     int e = 0;
     for (int64_t it = (int64_t)blockIdx.x * TT + tid; it < count; it += (int64_t)gridDim.x * TT) {
         const int32_t sn = items[3 * it];
-        const int32_t s0 = S.s0[sn], k = S.k[sn], b = S.b[sn];
+        const QsNode nd = S.node[sn];
+        const int32_t k = nd.k, b = nd.b;
         const int32_t width = k + b;
-        const int64_t base = D.first[s0];
+        const int64_t base = nd.base;
         const int32_t total = (int32_t)sn_trapezoid(k, b);
         if (total > SN_THREAD_CAP) {  // the plan never hands out such a supernode
             e |= ERR_CAPACITY;
@@ -705,11 +721,12 @@ template <int CT>
 __device__ void chain_panel(const DevTopo& D, const SnDev& S, const int32_t* it, int panel, int32_t* up,
                             int32_t* dn, int& e, PanelSmem<int32_t, CT>& sm) {
     const int32_t s = it[0], ct = it[1];
-    const int32_t s0 = S.s0[s], k = S.k[s], cols = k + S.b[s];
+    const QsNode nd = S.node[s];
+    const int32_t k = nd.k, cols = k + nd.b;
     const int i0 = panel * SN_P;
     const int pn = min(SN_P, k - i0);
     const int tid = threadIdx.x;
-    if (tid < pn) sm.rowb[tid] = D.first[s0 + i0 + tid];
+    if (tid < pn) sm.rowb[tid] = sn_row_base(nd.base, cols, i0 + tid);
     __syncthreads();
     const int j = i0 + pn + ct * CT + tid;
     const bool hasj = j < cols;

@@ -347,7 +347,7 @@ SnPlan* build_supernodal_plan(int64_t n, const int64_t* first, const int32_t* he
         free_supernodal_plan(P);
         return nullptr;
     }
-    P->dev = SnDev{d_s0, d_k, d_b, d_rel_off, d_rel, d_sid};
+    P->dev = SnDev{P->d_qnodes, d_s0, d_k, d_b, d_rel_off, d_rel, d_sid};
     if (setup_copies_done() != cudaSuccess) {
         *rc = NWCCH_ERR_CUDA;
         free_supernodal_plan(P);

@@ -17,7 +17,18 @@ namespace nwcch {
 // Its arcs form a dense trapezoid: row i (vertex s0+i) holds the columns
 // j in (i, k + b): ranks s0+i+1..s0+k-1 and then the boundary B (the row of
 // the last vertex, b entries), at index first[s0+i] + (j - i - 1).
+// A supernode in one 32-byte load: first vertex, rows, boundary size, next
+// supernode on its elimination-tree path (-1 at a root) and the entry row
+// there, first arc of its trapezoid (the customization kernels and the
+// streaming query kernel read it instead of chasing s0/k/b and first[]).
+struct QsNode {
+    int32_t s0, k, b, next;
+    int32_t next_row, pad;
+    int64_t base;
+};
+
 struct SnDev {
+    const QsNode* node;      // [nsn]
     const int32_t* s0;       // [nsn]
     const int32_t* k;        // [nsn]
     const int32_t* b;        // [nsn]
@@ -88,15 +99,6 @@ struct SnPlanParams {
     // a phase's items in rounds, where separate launches keep several tiles
     // per SM in flight); the autotuner tries both.
     int64_t chain_max_items = 0;
-};
-
-// A supernode as the streaming query kernel walks it: first vertex, rows,
-// boundary size, next supernode on the chain (-1 at a root) and the entry
-// row there, first arc of its trapezoid. One 32-byte load a step.
-struct QsNode {
-    int32_t s0, k, b, next;
-    int32_t next_row, pad;
-    int64_t base;
 };
 
 // One phase of the persistent top-of-tree launch (the items of one former

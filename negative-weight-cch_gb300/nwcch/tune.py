@@ -51,7 +51,7 @@ def set(topo: DeviceTopology, key: str, value: int) -> None:  # noqa: A001 - mir
 
 
 def tune_customize(topo: DeviceTopology, w, caps=(0, 128, 256, 512), min_counts=(0, 1024, 16384),
-                   reps: int = 3, chains=(0, 1536), threads=(0, 32)) -> dict:
+                   reps: int = 3, chains=(0, 1536), threads=(0, 16)) -> dict:
     """Re-plans the customization with each small-supernode schedule (which
     supernodes one warp customizes: trapezoid of at most `cap` arcs, in
     levels with at least `min_count` of them; cap 0 = none), times the
