@@ -89,6 +89,39 @@ struct PanelSmem {
 // Factor the diagonal triangle, then run the panel recurrence down this
 // thread's column. Rows a < r of the panel: for every column c beyond r,
 //   U(r, c) <- Dn(a, r) + U(a, c),   Dn(r, c) <- Dn(a, c) + U(a, r).
+// The panel recurrence down one column (this thread's) in registers, for a
+// panel of at most NP rows: rows at or past pn are neither read nor relaxed.
+template <class P, class V, int CT, int NP>
+__device__ __forceinline__ void panel_column(PanelSmem<V, CT>& sm, int pn, int& e) {
+    const int tid = threadIdx.x;
+    V cu[NP], cd[NP];
+#pragma unroll
+    for (int r = 0; r < NP; r++) {
+        cu[r] = r < pn ? sm.cU[r][tid] : P::inf();
+        cd[r] = r < pn ? sm.cD[r][tid] : P::inf();
+    }
+#pragma unroll
+    for (int a = 0; a + 1 < NP; a++) {
+        if (a + 1 < pn) {
+            const V ua = P::clean(cu[a]), da = P::clean(cd[a]);
+#pragma unroll
+            for (int r = a + 1; r < NP; r++) {
+                if (r < pn) {
+                    P::relax(cu[r], sm.Dd[a][r], ua, e);
+                    P::relax(cd[r], da, sm.Ud[a][r], e);
+                }
+            }
+        }
+    }
+#pragma unroll
+    for (int r = 0; r < NP; r++) {
+        if (r < pn) {
+            sm.cU[r][tid] = cu[r];
+            sm.cD[r][tid] = cd[r];
+        }
+    }
+}
+
 template <class P, class V, int CT>
 __device__ void panel_compute(PanelSmem<V, CT>& sm, int pn, bool hasj, int& e) {
     constexpr int RS = CT / 32;  // row stride of the diagonal mapping
@@ -127,34 +160,11 @@ __device__ void panel_compute(PanelSmem<V, CT>& sm, int pn, bool hasj, int& e) {
     if (!hasj) return;
     if constexpr (sizeof(V) == 4) {
         // 32-bit values: the thread's column lives in registers (fully
-        // unrolled, constant indices), the diagonal is read by broadcast;
-        // rows at or past pn are neither read nor relaxed
-        V cu[SN_P], cd[SN_P];
-#pragma unroll
-        for (int r = 0; r < SN_P; r++) {
-            cu[r] = r < pn ? sm.cU[r][tid] : P::inf();
-            cd[r] = r < pn ? sm.cD[r][tid] : P::inf();
-        }
-#pragma unroll
-        for (int a = 0; a + 1 < SN_P; a++) {
-            if (a + 1 < pn) {
-                const V ua = P::clean(cu[a]), da = P::clean(cd[a]);
-#pragma unroll
-                for (int r = a + 1; r < SN_P; r++) {
-                    if (r < pn) {
-                        P::relax(cu[r], sm.Dd[a][r], ua, e);
-                        P::relax(cd[r], da, sm.Ud[a][r], e);
-                    }
-                }
-            }
-        }
-#pragma unroll
-        for (int r = 0; r < SN_P; r++) {
-            if (r < pn) {
-                sm.cU[r][tid] = cu[r];
-                sm.cD[r][tid] = cd[r];
-            }
-        }
+        // unrolled for a bound of 8, 16 or 32 rows, the smallest that holds
+        // the panel; constant indices), the diagonal is read by broadcast
+        if (pn <= 8) panel_column<P, V, CT, 8>(sm, pn, e);
+        else if (pn <= 16) panel_column<P, V, CT, 16>(sm, pn, e);
+        else panel_column<P, V, CT, SN_P>(sm, pn, e);
     } else {
         for (int a = 0; a + 1 < pn; a++) {
             const V cu = P::clean(sm.cU[a][tid]), cd = P::clean(sm.cD[a][tid]);
@@ -472,6 +482,69 @@ __device__ void tile_store(const DevTopo& D, const SnDev& S, const TileCtx<T, TI
         }
 }
 
+// What a tile's store needs that does not depend on its product, loaded
+// before the product so that those loads overlap it: the ancestor arc of
+// every output pair (OUT), or the current values of every output arc.
+template <class T, int MT, bool OUT>
+struct TilePre {
+    int32_t a[MT][MT];                        // OUT: arc ids (-1: no output)
+    T u[OUT ? 1 : MT][OUT ? 1 : MT], d[OUT ? 1 : MT][OUT ? 1 : MT];  // !OUT: current values
+};
+
+template <class T, int TILE, int MT, bool OUT>
+__device__ __forceinline__ void tile_prefetch(const SnDev& S, const TileCtx<T, TILE, MT, OUT>& c,
+                                              const T* __restrict__ up, const T* __restrict__ dn,
+                                              TilePre<T, MT, OUT>& pre) {
+    constexpr int TH = TILE / MT;
+    const int tid = threadIdx.x, ty = tid / TH, tx = tid % TH;
+    const int64_t roff = OUT ? S.rel_off[c.s] : 0;
+#pragma unroll
+    for (int ii = 0; ii < MT; ii++)
+#pragma unroll
+        for (int jj = 0; jj < MT; jj++) {
+            const int rr = c.abase + ty + TH * ii, cc = c.bbase + tx + TH * jj;
+            const bool valid = !(cc <= rr || cc >= c.cols || rr >= c.alim);
+            if constexpr (OUT) {
+                const int p = rr - c.k, q = cc - c.k;
+                pre.a[ii][jj] = valid ? S.rel[roff + (int64_t)p * (2 * c.b - p - 1) / 2 + (q - p - 1)] : -1;
+            } else {
+                pre.a[ii][jj] = valid ? 1 : -1;
+                if (valid) {
+                    const int64_t a = sn_row_base(c.base, c.cols, rr) + (cc - rr - 1);
+                    pre.u[ii][jj] = up[a];
+                    pre.d[ii][jj] = dn[a];
+                }
+            }
+        }
+}
+
+template <class P, class T, int TILE, int MT, bool OUT>
+__device__ void tile_store_pre(const TileCtx<T, TILE, MT, OUT>& c, T* __restrict__ up, T* __restrict__ dn,
+                               const typename P::V (&accU)[MT][MT], const typename P::V (&accD)[MT][MT],
+                               const TilePre<T, MT, OUT>& pre) {
+    constexpr int TH = TILE / MT;
+    const int tid = threadIdx.x, ty = tid / TH, tx = tid % TH;
+#pragma unroll
+    for (int ii = 0; ii < MT; ii++)
+#pragma unroll
+        for (int jj = 0; jj < MT; jj++) {
+            if (pre.a[ii][jj] < 0) continue;
+            const bool fu = P::finite(accU[ii][jj]), fd = P::finite(accD[ii][jj]);
+            if (!fu && !fd) continue;
+            if constexpr (OUT) {
+                const int32_t a = pre.a[ii][jj];
+                if (fu) atomic_min_t(&up[a], (T)P::to(accU[ii][jj]));
+                if (fd) atomic_min_t(&dn[a], (T)P::to(accD[ii][jj]));
+            } else {
+                const int rr = c.abase + ty + TH * ii, cc = c.bbase + tx + TH * jj;
+                const int64_t a = sn_row_base(c.base, c.cols, rr) + (cc - rr - 1);
+                const T nu = (T)P::to(accU[ii][jj]), nv = (T)P::to(accD[ii][jj]);
+                if (fu && nu < pre.u[ii][jj]) up[a] = nu;
+                if (fd && nv < pre.d[ii][jj]) dn[a] = nv;
+            }
+        }
+}
+
 template <class T, int TILE, int MT, bool OUT>
 __global__ void __launch_bounds__((TILE / MT) * (TILE / MT))
     k_sn_tile(DevTopo D, SnDev S, const int32_t* __restrict__ items, int panel, T* __restrict__ up,
@@ -484,20 +557,22 @@ __global__ void __launch_bounds__((TILE / MT) * (TILE / MT))
     up += blockIdx.y * D.m_plus;  // metric blockIdx.y of a metric-major batch
     dn += blockIdx.y * D.m_plus;
     const auto c = tile_ctx<T, TILE, MT, OUT>(S, items + 3 * blockIdx.x, panel);
+    TilePre<T, MT, OUT> pre;
+    tile_prefetch<T, TILE, MT, OUT>(S, c, up, dn, pre);
     int e = 0;
     bool done = false;
     if constexpr (sizeof(T) == 4) {
         auto& fs = reinterpret_cast<TileSmem<int32_t, TILE, CH>&>(sm);
         int32_t accU[MT][MT], accD[MT][MT];
         if (tile_product<FastI32, T, TILE, MT, CH, OUT>(D, c, fs, up, dn, accU, accD, e)) {
-            tile_store<FastI32, T, TILE, MT, OUT>(D, S, c, up, dn, accU, accD);
+            tile_store_pre<FastI32, T, TILE, MT, OUT>(c, up, dn, accU, accD, pre);
             done = true;
         }
     }
     if (!done) {
         T accU[MT][MT], accD[MT][MT];
         tile_product<E, T, TILE, MT, CH, OUT>(D, c, sm, up, dn, accU, accD, e);
-        tile_store<E, T, TILE, MT, OUT>(D, S, c, up, dn, accU, accD);
+        tile_store_pre<E, T, TILE, MT, OUT>(c, up, dn, accU, accD, pre);
     }
     if (e) atomicOr(err, e);
 }
