@@ -1037,10 +1037,10 @@ def main():
                              "cpu_note": "the oracle's ET query, 1 thread, same graph, metric and pairs"},
         "e2e": {"value": round(statistics.median(R["e2e_ms"]), 4), "unit": "ms",
                 "h2d_bytes_per_step": int(W["w"].size * 4), "d2h_bytes_per_step": 8},
-        # per timed step: k_fill2 + k_base + the supernodal launches (those
+        # per timed step: k_base_gather + the supernodal launches (those
         # below the persistent top, plus k_sn_chain), the scan, and the query
         # batch's kernels
-        "gpu_launches": (2 + (T.chain_from + 1 if T.chain_phases else T.sn_launches) + 1 + R["query_launches"])
+        "gpu_launches": (1 + (T.chain_from + 1 if T.chain_phases else T.sn_launches) + 1 + R["query_launches"])
                         * args.steps,
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "peak_source": peak_src,
                      "unit": "GB/s", "frac": round(achieved / peak, 4),
@@ -1051,7 +1051,7 @@ def main():
                      "dram_gbs_at_traffic": (round(MEASURED_TRAFFIC[args.workload][0] / (cust / 1000) / 1e9, 1)
                                              if args.workload in MEASURED_TRAFFIC else None),
                      "algorithmic_bytes_per_launch": int(B),
-                     "launch": "one customization: CUDA graph of k_fill2, k_base, k_sn_thread, k_sn_warp, k_sn_panel, "
+                     "launch": "one customization: CUDA graph of k_base_gather, k_sn_thread, k_sn_warp, k_sn_panel, "
                                "k_sn_tile"},
         "cpu_baseline": {"value": round(cb["value"], 3), "unit": "ms", "cores": cb["cores"], "kind": "port",
                          "sample": f"{cb['runs']} level-parallel customizations (cpp/cch.cpp:468-529) + scans "

@@ -23,42 +23,35 @@
 
 namespace nwcch {
 
+// Base values gathered per shortcut arc: the minimum over the original arcs
+// mapped onto it, by direction (their list is grouped by shortcut arc, so
+// the arcs' values are written once, coalesced, with no fill and no atomics;
+// an arc with none gets INF).
 template <class T>
-__global__ void k_fill2(T* __restrict__ a, T* __restrict__ b, int64_t count, T v) {
+__global__ void __launch_bounds__(256) k_base_gather(DevTopo D, const int32_t* __restrict__ w, T* __restrict__ up,
+                                                      T* __restrict__ dn, int* __restrict__ err) {
     pdl_wait();
     pdl_launch_dependents();
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < count;
-         i += (int64_t)gridDim.x * blockDim.x) {
-        a[i] = v;
-        b[i] = v;
-    }
-}
-
-// base values: minimum over parallel original arcs, self-loops skipped
-// (cch_nb.py:533-542)
-template <class T>
-__global__ void k_base(DevTopo D, const int32_t* __restrict__ w, T* __restrict__ up, T* __restrict__ dn,
-                       int* __restrict__ err) {
-    pdl_wait();
-    pdl_launch_dependents();
-    // metric blockIdx.y of a metric-major batch (weights m apart, arcs m+ apart)
-    w += blockIdx.y * D.m;
+    w += blockIdx.y * D.m;  // metric blockIdx.y of a metric-major batch
     up += blockIdx.y * D.m_plus;
     dn += blockIdx.y * D.m_plus;
     int bad = 0;
-    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < D.m;
-         k += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t a = D.e_arc[k];
-        if (a < 0) continue;
-        const int32_t wk = w[k];
-        if (wk == INF32) {
-            bad |= ERR_ARG;
-            continue;
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < D.m_plus;
+         c += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t j0 = D.aeoff[c], j1 = D.aeoff[c + 1];
+        T nu = Lim<T>::INF, nd = Lim<T>::INF;
+        for (int64_t j = j0; j < j1; j++) {
+            const int32_t x = D.aedir[j];
+            const int32_t wk = w[x & 0x7fffffff];
+            if (wk == INF32) {
+                bad |= ERR_ARG;
+                continue;
+            }
+            if (x < 0) nu = min(nu, (T)wk);
+            else nd = min(nd, (T)wk);
         }
-        if (sizeof(T) == 4)
-            atomicMin(reinterpret_cast<int*>(D.e_up[k] ? &up[a] : &dn[a]), (int)wk);
-        else
-            atomicMin(reinterpret_cast<long long*>(D.e_up[k] ? &up[a] : &dn[a]), (long long)wk);
+        up[c] = nu;
+        dn[c] = nd;
     }
     if (bad) atomicOr(err, bad);
 }
@@ -154,10 +147,8 @@ int grid_for(int64_t count, int block) {
 template <class T>
 int base_init(nwcch_topology* t, const int32_t* w, T* up, T* dn, cudaStream_t s, int* err, int metrics) {
     const DevTopo& D = t->d;
-    k_fill2<T><<<grid_for(D.m_plus * metrics, 256), 256, 0, s>>>(up, dn, D.m_plus * metrics, Lim<T>::INF);
-    if (D.m > 0)
-        NWCCH_CUDA_TRY(launch_pdl(t->tune.pdl != 0, k_base<T>, dim3(grid_for(D.m, 256), metrics), dim3(256), 0, s, D,
-                                  w, up, dn, err));
+    NWCCH_CUDA_TRY(launch_pdl(t->tune.pdl != 0, k_base_gather<T>, dim3(grid_for(D.m_plus, 256), metrics), dim3(256),
+                              0, s, D, w, up, dn, err));
     return cudaGetLastError() == cudaSuccess ? NWCCH_OK : NWCCH_ERR_CUDA;
 }
 

@@ -54,6 +54,15 @@ void release(nwcch_topology* t) {
 
 }  // namespace
 
+// aedir[j] = aeidx[j] with the sign bit set when the original arc goes up.
+__global__ void k_arc_dir(int64_t count, const int32_t* __restrict__ aeidx, const int8_t* __restrict__ e_up,
+                          int32_t* __restrict__ dir) {
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < count; j += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t k = aeidx[j];
+        dir[j] = e_up[k] ? (int32_t)((uint32_t)k | 0x80000000u) : k;
+    }
+}
+
 // Allocates and zeroes one more block of kStreamSlots slots (caller holds
 // t->slot_mu).
 static int add_slot_block(nwcch_topology* t) {
@@ -167,6 +176,21 @@ extern "C" int nwcch_topology_create(int64_t n, const int64_t* first, const int3
         d.vlevel = D.vlevel;
         d.aeoff = D.aeoff;
         d.aeidx = D.aeidx_sorted;
+        {
+            // the base values' gather: each mapped original arc with its direction
+            const int64_t mapped = m - D.nloops;
+            int32_t* dir = nullptr;
+            if ((rc = alloc(t, std::max<int64_t>(1, mapped), &dir))) break;
+            if (mapped > 0) {
+                k_arc_dir<<<(unsigned)std::max<int64_t>(1, std::min<int64_t>((mapped + 255) / 256, 4096)), 256>>>(
+                    mapped, D.aeidx_sorted, d.e_up, dir);
+                if (cudaGetLastError() != cudaSuccess) {
+                    rc = NWCCH_ERR_CUDA;
+                    break;
+                }
+            }
+            d.aedir = dir;
+        }
         d.max_depth = D.max_depth;
         t->loops = D.aeidx_sorted + (m - D.nloops);
         t->nloops = D.nloops;

@@ -29,6 +29,7 @@ struct DevTopo {
     const int8_t* e_up;     // [m]   1 if the original arc goes up in rank
     const int64_t* aeoff;   // [m+ + 1] original arcs mapped onto each shortcut arc ...
     const int32_t* aeidx;   // [...]     ... as original arc ids
+    const int32_t* aedir;   // [...]     the same ids with the arc's direction in the sign bit (set: up)
 };
 
 // Schedules that depend on the graph and are picked by measurement
