@@ -158,10 +158,12 @@ __device__ void panel_compute(PanelSmem<V, CT>& sm, int pn, bool hasj, int& e) {
     }
     __syncthreads();
     if (!hasj) return;
-    if constexpr (sizeof(V) == 4) {
-        // 32-bit values: the thread's column lives in registers (fully
+    if constexpr (std::is_same<P, FastI32>::value) {
+        // the fast path: the thread's column lives in registers (fully
         // unrolled for a bound of 8, 16 or 32 rows, the smallest that holds
-        // the panel; constant indices), the diagonal is read by broadcast
+        // the panel; constant indices), the diagonal is read by broadcast.
+        // The exact path (rare) keeps the column in shared memory, which
+        // keeps the kernel's code small.
         if (pn <= 8) panel_column<P, V, CT, 8>(sm, pn, e);
         else if (pn <= 16) panel_column<P, V, CT, 16>(sm, pn, e);
         else panel_column<P, V, CT, SN_P>(sm, pn, e);
@@ -680,12 +682,12 @@ __global__ void __launch_bounds__(32 * WARPS) k_sn_warp(DevTopo D, SnDev S, cons
 // hit the same bank). The bottom levels of a road-like graph hold millions of
 // supernodes of 2 to 20 arcs, where a warp per supernode leaves most lanes
 // idle.
-template <class T, int TT>
+template <class T, int TT, int CAP>
 __global__ void __launch_bounds__(TT) k_sn_thread(DevTopo D, SnDev S, const int32_t* __restrict__ items,
                                                   int64_t count, T* __restrict__ up, T* __restrict__ dn,
                                                   int* __restrict__ err) {
-    __shared__ T su[SN_THREAD_CAP][TT];
-    __shared__ T sd[SN_THREAD_CAP][TT];
+    __shared__ T su[CAP][TT];  // CAP: the plan's trapezoid cap (16 or 32 arcs)
+    __shared__ T sd[CAP][TT];
     pdl_wait();
     pdl_launch_dependents();
     const int tid = threadIdx.x;
@@ -699,7 +701,7 @@ __global__ void __launch_bounds__(TT) k_sn_thread(DevTopo D, SnDev S, const int3
         const int32_t width = k + b;
         const int64_t base = nd.base;
         const int32_t total = (int32_t)sn_trapezoid(k, b);
-        if (total > SN_THREAD_CAP) {  // the plan never hands out such a supernode
+        if (total > CAP) {  // the plan never hands out such a supernode
             e |= ERR_CAPACITY;
             continue;
         }

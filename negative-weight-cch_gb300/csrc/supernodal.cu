@@ -412,10 +412,14 @@ int run_supernodal(nwcch_topology* t, SnPlan* P, const int32_t* w, T* up, T* dn,
                 e = launch_pdl(pdl, k_sn_tile<T, 16, 2, true>, grid, dim3(64), 0, s, D, P->dev, it, 0, up, dn, err);
                 break;
             case SN_THREAD: {
-                constexpr int TT = sizeof(T) == 4 ? 128 : 64;  // 32 KB of staged arcs a block
+                constexpr int TT = sizeof(T) == 4 ? 128 : 64;  // 16 or 32 KB of staged arcs a block
                 const int64_t blocks = std::min<int64_t>((la.count + TT - 1) / TT, (int64_t)device_sms() * 16);
-                e = launch_pdl(pdl, k_sn_thread<T, TT>, dim3((unsigned)blocks, metrics), dim3(TT), 0, s, D, P->dev,
-                               it, la.count, up, dn, err);
+                if (P->params.thread_cap <= 16)
+                    e = launch_pdl(pdl, k_sn_thread<T, TT, 16>, dim3((unsigned)blocks, metrics), dim3(TT), 0, s, D,
+                                   P->dev, it, la.count, up, dn, err);
+                else
+                    e = launch_pdl(pdl, k_sn_thread<T, TT, SN_THREAD_CAP>, dim3((unsigned)blocks, metrics), dim3(TT), 0,
+                                   s, D, P->dev, it, la.count, up, dn, err);
                 break;
             }
             case SN_WARP: {
