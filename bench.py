@@ -136,7 +136,6 @@ def algorithmic_bytes(n, m, m_plus, triangles, s_w=4):
 # `bench.py --profile customize` on the workload (dram__bytes_read.sum +
 # dram__bytes_write.sum over the customization's launches; the capture's
 # summary is profiles/customize_usa24m_launches_dram.md).
-MEASURED_TRAFFIC = {"usa24m": (21.146e9, "ncu, plan: warp cap 256, level threshold 1024")}
 
 
 def peak_hbm():
@@ -378,7 +377,8 @@ def run_ours(args, W, world):
     return dict(T=T, tuned=tuned, cust_tuned=cust_tuned, cust_ms=cust_ms, q_ms=q_ms, wall=wall, plain_ms=plain_ms, plain_equal=same,
                 e2e_ms=e2e_ms, graph_q=graph_q, bad_host=bad_host, batch_dist=ref_d.cpu().numpy(), topo_s=topo_s,
                 plain_q_ms=plain_q_ms, lat_dist=lat_dist, pot_ms=pot_ms, pot=pot.cpu().numpy(), good_host=good_host,
-                lat_us=lat, clocks=clocks.summary(), neg=neg_k, saturated=bool(sat), query_launches=q_launches)
+                lat_us=lat, clocks=clocks.summary(), neg=neg_k, saturated=bool(sat), query_launches=q_launches,
+                good=good)
 
 
 def scanned_arcs(top, qs, qt, sample: int = 1000) -> float:
@@ -531,6 +531,96 @@ def batched_bytes(n, m, m_plus, triangles, k, s_w=4):
             + m * (8 + 1 + 4 + 4 * k))
 
 
+def run_updates(T, m, top, new_weights, sizes, reps, cpu_budget_s, seed):
+    """Partial re-customizations (python/cch.py:349-402) of `size` random
+    original arcs of the resident metric m, `reps` per size, sizes in
+    ascending order. Each is timed on the host around the public call (the
+    statistics read back included) and with CUDA events, and checked equal to
+    a full customization of the new weights. The oracle's update runs the
+    same changes from the same arrays on one core, on the reference's update
+    index built once (python/cch.py:289-290), while its time stays within
+    cpu_budget_s: each compared in evaluated count and changed set, and the
+    arrays compared in full when it followed every update."""
+    import torch
+
+    import oracle as orc
+    stream = torch.cuda.current_stream()
+    rng = np.random.default_rng(seed)
+    OT = orc.Topo.from_dict(top)
+    t0 = time.perf_counter()
+    X = orc.UpdateIndex(OT)
+    index_s = time.perf_counter() - t0
+    w_o = m.w.cpu().numpy().astype(np.int32)
+    up_o, dn_o = m.to_numpy()
+    full = T.customize(m.w, m.storage)
+    cpu_on, cpu_spent, checked, oracle_equal = True, 0.0, 0, True
+    out = {}
+    for size in sizes:
+        wall, dev_ms, ev, cpu = [], [], [], []
+        for _ in range(reps):
+            idx = rng.choice(T.m, size=size, replace=False)
+            val = new_weights(idx, rng)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            t0 = time.perf_counter()
+            e0.record(stream)
+            ev.append(T.update(m, idx, val))
+            e1.record(stream)
+            torch.cuda.synchronize()
+            wall.append((time.perf_counter() - t0) * 1000)
+            dev_ms.append(e0.elapsed_time(e1))
+            assert m.stats["changed_negative"] == 0
+            T.customize(m.w, m.storage, out=full)
+            assert torch.equal(full.up, m.up) and torch.equal(full.dn, m.dn), "partial != full recompute"
+            if cpu_on:
+                ch = np.sort(m.last_changed.cpu().numpy().astype(np.int64))
+                t0 = time.perf_counter()
+                oev, och, _ = X.update(w_o, up_o, dn_o, idx, val)
+                dt = time.perf_counter() - t0
+                cpu.append(dt * 1000)
+                cpu_spent += dt
+                checked += 1
+                oracle_equal &= bool(oev == ev[-1] and np.array_equal(np.sort(och), ch))
+                cpu_on = cpu_spent <= cpu_budget_s
+        out[str(size)] = {"ms_median": round(statistics.median(wall), 3),
+                          "device_ms_median": round(statistics.median(dev_ms), 3),
+                          "evaluated_median": int(statistics.median(ev)), "reps": reps,
+                          "cpu_ms_median": round(statistics.median(cpu), 3) if cpu else None,
+                          "cpu_reps": len(cpu)}
+    arrays_equal = None
+    if cpu_on:
+        up, dn = m.to_numpy()
+        arrays_equal = bool(np.array_equal(up, up_o) and np.array_equal(dn, dn_o))
+        oracle_equal &= arrays_equal
+    X.close()
+    del full
+    return {"sizes": out, "equal_full_recompute": True, "oracle_checked": checked, "oracle_equal": oracle_equal,
+            "oracle_arrays_equal_after_last": arrays_equal,
+            "cpu": {"kind": "port", "cores": 1, "index_build_s": round(index_s, 3),
+                    "sample": f"the oracle's update (python/cch.py:349-402) on the first {checked} changes, "
+                              f"within {cpu_budget_s:g} s; index built once, outside the times"}}
+
+
+def run_updates_headline(args, W, R):
+    """Partial updates on the headline workload's resident conservative
+    metric: the tuner's sweep budget and dense threshold for this topology
+    first, then run_updates with new lengths L' in [1, 2L] (heights kept, so
+    the metric stays conservative)."""
+    T, m = R["T"], R["good"]
+    L = W["g"]["L"].astype(np.int64)
+    heights = W["w"].astype(np.int64) - L
+    tuned = None
+    if not args.no_tune:
+        from nwcch import tune
+        tuned = tune.tune_update(T, m, sizes=(1, 10, 100), factors=(0.5, 1.0, 2.0), picks_per_size=3,
+                                 seed=13)["best"]
+    sizes = tuple(int(x) for x in args.update_sizes.split(",") if x)
+    res = run_updates(T, m, W["top"], lambda idx, rng: heights[idx] + rng.integers(1, 2 * L[idx] + 1),
+                      sizes=sizes, reps=args.update_reps, cpu_budget_s=args.cpu_budget, seed=23)
+    res.update(workload=W["name"], schedule=tuned, full_customize_ms=round(statistics.median(R["cust_ms"]), 3))
+    return res
+
+
 def run_batch(args, Wd, K):
     """K metrics of one topology customized in one batched launch sequence,
     against K single customizations of the same metrics; then partial
@@ -595,44 +685,22 @@ def run_batch(args, Wd, K):
     b0_host = b.metric(0).to_numpy()
     # partial re-customization of metric 0: new lengths L' in [1, 2L] keep the
     # metric conservative (w' = height difference + L')
-    rng = np.random.default_rng(5)
     m0 = b.metric(0)
-    w_cur = Wk[0].astype(np.int64).copy()
     L = g["L"].astype(np.int64)
-    heights = w_cur - L  # w = length + height difference; lengths change, heights stay
-    full = T.customize(m0.w, "int32")
+    heights = Wk[0].astype(np.int64) - L  # w = length + height difference; lengths change, heights stay
     upd_tuning = None
     if not args.no_tune:
         # sweep budget and dense threshold of this topology (raise-and-restore
         # pairs on other arcs; the metric ends as it began)
         from nwcch import tune
         upd_tuning = tune.tune_update(T, m0, sizes=(1, 100, 1000), factors=(0.25, 0.5, 1.0), seed=9)["best"]
-    updates = {}
-    for size in (1, 100, 1000):
-        wall, dev_ms, ev = [], [], []
-        for rep in range(5):
-            idx = rng.choice(T.m, size=size, replace=False)
-            val = heights[idx] + rng.integers(1, 2 * L[idx] + 1)
-            torch.cuda.synchronize()
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            t0 = time.perf_counter()
-            e0.record(stream)
-            ev.append(T.update(m0, idx, val))
-            e1.record(stream)
-            torch.cuda.synchronize()
-            wall.append((time.perf_counter() - t0) * 1000)
-            dev_ms.append(e0.elapsed_time(e1))
-            w_cur[idx] = val
-            T.customize(m0.w, "int32", out=full)
-            assert torch.equal(full.up, m0.up) and torch.equal(full.dn, m0.dn), "partial != full recompute"
-            assert m0.stats["changed_negative"] == 0
-        updates[str(size)] = {"ms_median": round(statistics.median(wall), 3),
-                              "device_ms_median": round(statistics.median(dev_ms), 3),
-                              "evaluated_median": int(statistics.median(ev)), "reps": 5,
-                              "equal_full_recompute": True}
+    updates = run_updates(T, m0, top, lambda idx, rng: heights[idx] + rng.integers(1, 2 * L[idx] + 1),
+                          sizes=(1, 100, 1000), reps=5, cpu_budget_s=args.cpu_budget, seed=5)
     # parity at this size: metric 0 of the batch (before the updates) and 10k
     # queries on it against the oracle
     par = batch_parity(Wd, Wk[0], b0_host, qs=Wd["qs"], qt=Wd["qt"], T=T, m=b.metric(0))
+    par["updates_equal_oracle"] = updates["oracle_equal"]
+    par["equal"] = par["equal"] and updates["oracle_equal"]
     bm = statistics.median(batch_ms)
     B = batched_bytes(top["n"], top["e_arc"].size, T.m_plus, T.triangles, K)
     return {"workload": Wd["name"], "metrics": K, "batch_ms": round(bm, 3), "ms_per_metric": round(bm / K, 4),
@@ -792,6 +860,7 @@ def profile_part(args):
         "customize": lambda i: T.customize(w, "int32", out=m, sync=False),
         "potential": lambda i: T.potential(m),
         "queries": lambda i: T.query_batch(m, qs, qt),
+        "query1": lambda i: T.query_batch(m, qs[i:i + 1], qt[i:i + 1]),  # one query per call
         "update": lambda i: T.update(m, idx, w0 + (1 + i % 2)),
     }
     if args.profile == "battery":
@@ -898,6 +967,9 @@ def main():
     ap.add_argument("--batch-workload", default="delaunay264k", choices=list(WORKLOADS))
     ap.add_argument("--headline-batch-metrics", type=int, default=8,
                     help="metrics of a batched customization on the headline workload (0: skip it)")
+    ap.add_argument("--update-reps", type=int, default=3,
+                    help="partial updates per size on the headline workload (0: skip them)")
+    ap.add_argument("--update-sizes", default="1,10,100", help="changed arcs per partial update")
     ap.add_argument("--serve-workload", default="delaunay1m", choices=list(WORKLOADS) + ["none"])
     ap.add_argument("--serve-loads", default="1e4,1e5,1e6", help="offered query loads (queries/s)")
     ap.add_argument("--serve-seconds", type=float, default=1.0)
@@ -906,7 +978,7 @@ def main():
     ap.add_argument("--no-tune", action="store_true", help="keep the default query schedule")
     ap.add_argument("--plain-steps", type=int, default=-1,
                     help="plain per-level customizations to time (-1: one, none above 5M vertices)")
-    ap.add_argument("--profile", choices=["customize", "potential", "queries", "update", "battery"],
+    ap.add_argument("--profile", choices=["customize", "potential", "queries", "query1", "update", "battery"],
                     help="run only this part, --steps times after --warmup (for ncu captures); no bench line")
     ap.add_argument("--sn-warp-cap", type=int, default=None, help="customization plan: warp-kernel trapezoid cap")
     ap.add_argument("--sn-warp-min-count", type=int, default=None, help="customization plan: level threshold")
@@ -996,6 +1068,11 @@ def main():
     cq = cpu_queries(W, R["good_host"])
     parity["single_queries_equal"] = bool(np.array_equal(cq["dist"], R["lat_dist"][:cq["queries"]]))
     parity["potential_equal"] = bool(cp["equal"])
+    upd_head = None
+    if args.update_reps > 0:
+        upd_head = run_updates_headline(args, W, R)
+        parity["updates_equal_oracle"] = upd_head["oracle_equal"]
+        log(f"partial updates (headline workload): {upd_head}")
     if batch is not None:
         parity["batched_section"] = batch.pop("parity")
     line = {
@@ -1044,12 +1121,14 @@ def main():
                         * args.steps,
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "peak_source": peak_src,
                      "unit": "GB/s", "frac": round(achieved / peak, 4),
-                     "traffic": (int(MEASURED_TRAFFIC[args.workload][0]) if args.workload in MEASURED_TRAFFIC
-                                 else None),
-                     "traffic_source": (MEASURED_TRAFFIC[args.workload][1] if args.workload in MEASURED_TRAFFIC
-                                        else None),
-                     "dram_gbs_at_traffic": (round(MEASURED_TRAFFIC[args.workload][0] / (cust / 1000) / 1e9, 1)
-                                             if args.workload in MEASURED_TRAFFIC else None),
+                     # the DRAM bytes of a whole customization would need a
+                     # counter capture of its ~1,100 launches at full size;
+                     # per-kernel DRAM bytes come from single-launch captures
+                     # on the 8M road-like graph instead
+                     "traffic": None,
+                     "traffic_note": "not captured for the whole launch graph (multi-launch counter capture at "
+                                     "full size); single-launch DRAM captures of k_sn_thread and k_sn_panel on "
+                                     "the 8M road-like graph are summarised with the profiles",
                      "algorithmic_bytes_per_launch": int(B),
                      "launch": "one customization: CUDA graph of k_base_gather, k_sn_thread, k_sn_warp, k_sn_panel, "
                                "k_sn_tile"},
@@ -1061,6 +1140,7 @@ def main():
         "potential": {"gpu_ms": round(statistics.median(R["pot_ms"]), 3),
                       "cpu_ms": round(cp["ms"], 1), "cpu_cores": 1, "cpu_kind": "port of cpp/cch.cpp:631-655",
                       "equal": cp["equal"], "metric": "conservative (no injected cycle)"},
+        "partial_updates": upd_head,
         "batched_customization": batch,
         "batched_customization_headline": head_batch,
         "serving": serving,
@@ -1068,7 +1148,8 @@ def main():
     }
     print(json.dumps(line), flush=True)
     ok = (parity["customize_equal"] and parity["queries_equal"] and parity["single_queries_equal"]
-          and parity["potential_equal"] and parity.get("batched_section", {}).get("equal", True))
+          and parity["potential_equal"] and parity.get("batched_section", {}).get("equal", True)
+          and parity.get("updates_equal_oracle", True))
     if not ok:
         log("PARITY FAILURE: device results differ from the oracle's")
         sys.exit(3)

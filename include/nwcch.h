@@ -215,6 +215,17 @@ int nwcch_check(nwcch_topology* t, void* stream);
  * when the topology fits its shared memory (labels, boundary positions and
  * the copy ring; rows of at most 12,280 arcs). 0: off. Default 64. */
 #define NWCCH_TUNE_QUERY_STREAM_MAX 19
+/* Partial updates: the level sweep first runs in one CTA (block barriers, no
+ * grid barrier per level) until it has evaluated this many arcs; then it
+ * hands its pending levels to the sweep over the whole grid. Counts and
+ * values are the same either way. 0: the grid sweep from the start.
+ * Default 8192. */
+#define NWCCH_TUNE_UPDATE_SMALL_ARCS 20
+/* ... or until it has run this many nanoseconds (>= 1; default 300,000). A
+ * sweep out of time stops before its next arc, inside a level if need be;
+ * the level is finished by the grid sweep (or the dense finish, for the grid
+ * sweep's own budget, NWCCH_TUNE_UPDATE_BUDGET_NS), counted once. */
+#define NWCCH_TUNE_UPDATE_SMALL_NS 21
 int nwcch_tune_set(nwcch_topology* t, int key, int64_t value);
 int nwcch_tune_get(const nwcch_topology* t, int key, int64_t* value);
 

@@ -319,6 +319,14 @@ extern "C" int nwcch_tune_set(nwcch_topology* t, int key, int64_t value) {
             if (value < 0) return NWCCH_ERR_ARG;
             t->tune.query_stream_max = value;
             return NWCCH_OK;
+        case NWCCH_TUNE_UPDATE_SMALL_ARCS:
+            if (value < 0) return NWCCH_ERR_ARG;
+            t->tune.update_small_arcs = value;
+            return NWCCH_OK;
+        case NWCCH_TUNE_UPDATE_SMALL_NS:
+            if (value < 1) return NWCCH_ERR_ARG;
+            t->tune.update_small_ns = value;
+            return NWCCH_OK;
         case NWCCH_TUNE_TEST_BARRIER_EXTRA:
             if (value < 0 || value > 1024) return NWCCH_ERR_ARG;
             t->tune.test_barrier_extra = (int32_t)value;
@@ -358,6 +366,8 @@ extern "C" int nwcch_tune_get(const nwcch_topology* t, int key, int64_t* value) 
         case NWCCH_TUNE_TEST_BARRIER_EXTRA: *value = t->tune.test_barrier_extra; return NWCCH_OK;
         case NWCCH_TUNE_QUERY_TOP_CHAINS: *value = t->tune.query_top_chains; return NWCCH_OK;
         case NWCCH_TUNE_QUERY_STREAM_MAX: *value = t->tune.query_stream_max; return NWCCH_OK;
+        case NWCCH_TUNE_UPDATE_SMALL_ARCS: *value = t->tune.update_small_arcs; return NWCCH_OK;
+        case NWCCH_TUNE_UPDATE_SMALL_NS: *value = t->tune.update_small_ns; return NWCCH_OK;
         case NWCCH_TUNE_BATTERY_POOL: *value = t->tune.battery_pool; return NWCCH_OK;
         case NWCCH_TUNE_BATTERY_BUFFER: *value = t->tune.battery_buffer; return NWCCH_OK;
         case NWCCH_TUNE_SN_WARP_CAP:

@@ -60,11 +60,16 @@ struct UpdateWorkspace {
     void* dn2 = nullptr;
     // [0] evaluated [1] changed [2] changed with up+dn<0 [3] levels done
     // [5] barrier arrivals [6] barrier generation [7] stop level + 1
-    // [8], [9] stop requests by level parity
+    // [8], [9] stop requests by level parity [10] hand-over level + 1 of a
+    // one-CTA sweep [11], [12] part-way stop requests by level parity
+    // [13] the stop or hand-over level was left part way
     unsigned long long* stats = nullptr;
     int blocks32 = 0, blocks64 = 0;
-    int2* tiles = nullptr;            // dense finish: (supernode, 32-column tile) work items
-    int64_t ntiles = 0;
+    int2* tiles = nullptr;            // dense finish: (supernode, 32-column tile) work items,
+    int64_t ntiles = 0;               // those of the warp form (small supernodes) first
+    int64_t nsmall = 0;
+    int32_t* tsn = nullptr;           // dense finish: supernodes of at most 32 columns (a thread each)
+    int64_t ntsn = 0;
     const void* tiles_plan = nullptr; // the supernodal plan the tiles were made for
 };
 
@@ -83,6 +88,11 @@ struct UpdateArgs {
     int64_t max_arcs;     // evaluated arcs before the dense finish
     long long spin_limit; // spins of one barrier wait before ERR_TIMEOUT
     int barrier_extra;    // test hook: arrivals a barrier waits for beyond the grid (0)
+    int64_t small_arcs;   // one-CTA sweep: evaluated arcs before it hands over to the grid sweep
+    long long small_ns;   // one-CTA sweep: time before it hands over (changes that climb
+                          // thousands of elimination levels go faster with the whole grid)
+    int32_t resume_level; // >= 0: continue a handed-over sweep at this level (steps 1-2 done)
+    int32_t resume_counted;  // the resumed level's arcs are already in the evaluated count
 };
 
 static constexpr int kStatWords = 16;
@@ -115,8 +125,13 @@ static __device__ __forceinline__ void enqueue(const UpdateArgs<T>& A, int32_t c
 }
 
 // Bounded grid barrier. Returns false if it timed out (ERR_TIMEOUT recorded).
+// A one-CTA sweep (gridDim 1) only needs the block's barrier.
 template <class T>
 static __device__ bool grid_sync(const UpdateArgs<T>& A) {
+    if (gridDim.x == 1) {
+        __syncthreads();
+        return true;
+    }
     __shared__ int ok;
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -155,6 +170,21 @@ static __device__ __forceinline__ int64_t find_in_row(const DevTopo& D, int64_t 
     return lo;
 }
 
+// The pending levels from `from` up join the cleanup list of a stopped sweep.
+template <class T>
+static __device__ void list_pending_from(const UpdateArgs<T>& A, int32_t from) {
+    unsigned long long d = A.ws.stats[3];
+    for (int32_t wi = from >> 5; wi < ((A.levels + 31) >> 5); wi++) {
+        uint32_t bits = __ldcg(A.ws.pending + wi);
+        if (wi == (from >> 5)) bits &= ~((1u << (from & 31)) - 1u);
+        while (bits && d < (unsigned long long)A.levels) {
+            A.ws.done_levels[d++] = wi * 32 + __ffs(bits) - 1;
+            bits &= bits - 1;
+        }
+    }
+    A.ws.stats[3] = d;
+}
+
 template <class T>
 __global__ void __launch_bounds__(256) k_update(UpdateArgs<T> A) {
     const DevTopo& D = A.D;
@@ -164,22 +194,31 @@ __global__ void __launch_bounds__(256) k_update(UpdateArgs<T> A) {
     const int64_t gwarp = gtid >> 5, gwarps = gthreads >> 5;
     int e = 0;
     unsigned long long t_start = 0;
+    const bool small = gridDim.x == 1;  // the one-CTA sweep of a small update
+    // a level may be left part way when the sweep runs out of time: the top
+    // separators' levels hold arcs whose lower triangles number in the
+    // thousands each, and one such level outlasts the whole budget
+    const long long limit = small ? A.small_ns : A.budget_ns;
+    __shared__ unsigned long long t_block;
+    if (threadIdx.x == 0) t_block = globaltimer_ns();
     if (gtid == 0) {
         t_start = globaltimer_ns();
         if (A.budget_ns <= 0) A.ws.stats[8] = 1;  // dense from the first level
     }
-    // 1. new weights (python/cch.py:357-360)
-    for (int64_t j = gtid; j < A.k; j += gthreads) A.w[A.ws.edge_idx[j]] = A.ws.new_w[j];
-    if (!grid_sync(A)) return;
-    // 2. queue the arcs the changed original arcs map to
-    for (int64_t j = gtid; j < A.k; j += gthreads) {
-        const int64_t c = D.e_arc[A.ws.edge_idx[j]];
-        if (c >= 0) enqueue(A, (int32_t)c);
+    if (A.resume_level < 0) {
+        // 1. new weights (python/cch.py:357-360)
+        for (int64_t j = gtid; j < A.k; j += gthreads) A.w[A.ws.edge_idx[j]] = A.ws.new_w[j];
+        if (!grid_sync(A)) return;
+        // 2. queue the arcs the changed original arcs map to
+        for (int64_t j = gtid; j < A.k; j += gthreads) {
+            const int64_t c = D.e_arc[A.ws.edge_idx[j]];
+            if (c >= 0) enqueue(A, (int32_t)c);
+        }
+        if (!grid_sync(A)) return;
     }
-    if (!grid_sync(A)) return;
     // 3. levels, lowest first (python/cch.py:376-401)
     __shared__ int32_t next_level;
-    int32_t L = -1;
+    int32_t L = A.resume_level < 0 ? -1 : A.resume_level - 1;
     bool stopped = false;
     // a stop request for iteration i is written during iteration i-1 into
     // word 8 + (i & 1), so no block reads a word while it is being written
@@ -203,32 +242,42 @@ __global__ void __launch_bounds__(256) k_update(UpdateArgs<T> A) {
         __syncthreads();
         L = next_level;
         if (L < 0) break;
+        if (small && __ldcg(A.ws.stats + 8 + (iter & 1))) {
+            // the one-CTA sweep has grown: the grid sweep continues at L
+            if (gtid == 0) A.ws.stats[10] = (unsigned long long)L + 1;
+            if (e) atomicOr(A.err, e);
+            return;
+        }
         if (__ldcg(A.ws.stats + 8 + (iter & 1))) {
             stopped = true;
             if (gtid == 0) {
                 A.ws.stats[7] = (unsigned long long)L + 1;
-                // the pending levels from L up join the cleanup list
-                unsigned long long d = A.ws.stats[3];
-                for (int32_t wi = L >> 5; wi < ((A.levels + 31) >> 5); wi++) {
-                    uint32_t bits = __ldcg(A.ws.pending + wi);
-                    if (wi == (L >> 5)) bits &= ~((1u << (L & 31)) - 1u);
-                    while (bits && d < (unsigned long long)A.levels) {
-                        A.ws.done_levels[d++] = wi * 32 + __ffs(bits) - 1;
-                        bits &= bits - 1;
-                    }
-                }
-                A.ws.stats[3] = d;
+                list_pending_from(A, L);
             }
             break;
         }
         const int64_t base = A.level_arc_off[L];
         const int32_t cnt = (int32_t)min((int64_t)__ldcg(A.ws.bcount + L), A.level_arc_off[L + 1] - base);
-        if (gtid == 0) {
+        // a level handed over part way by the one-CTA sweep is evaluated
+        // again whole (its evaluated arcs keep their values: their lower
+        // sides are final) but is counted and listed once
+        if (gtid == 0 && !(iter == 0 && A.resume_counted && L == A.resume_level)) {
             const unsigned long long d = atomicAdd(A.ws.stats + 3, 1ull);
             if (d < (unsigned long long)A.levels) A.ws.done_levels[d] = L;  // (a level is done once)
             atomicAdd(A.ws.stats + 0, (unsigned long long)cnt);
         }
         for (int64_t i = gwarp; i < cnt; i += gwarps) {
+            // out of time: the warp stops before its next arc (an arc once
+            // started is finished, with its changes queued)
+            // (word 11 + (iter & 1): a word read after this level's barrier
+            // is never written by a block already in the next level)
+            int out = 0;
+            if (lane == 0)
+                out = __ldcg(A.ws.stats + 11 + (iter & 1)) != 0 || (long long)(globaltimer_ns() - t_block) > limit;
+            if (__shfl_sync(0xffffffffu, out, 0)) {
+                if (lane == 0) A.ws.stats[11 + (iter & 1)] = 1;
+                break;
+            }
             const int32_t c = __ldcg(A.ws.bucket + base + i);
             const int32_t y = D.tail[c], z = D.head[c];
             T nu = Lim<T>::INF, nd = Lim<T>::INF;
@@ -275,11 +324,33 @@ __global__ void __launch_bounds__(256) k_update(UpdateArgs<T> A) {
                 enqueue(A, (int32_t)r);
             }
         }
-        if (gtid == 0 && ((long long)(globaltimer_ns() - t_start) > A.budget_ns ||
-                          (long long)A.ws.stats[0] > A.max_arcs)) {
+        if (gtid == 0 && (small ? ((long long)A.ws.stats[0] > A.small_arcs ||
+                                   (long long)(globaltimer_ns() - t_start) > A.small_ns)
+                                : ((long long)(globaltimer_ns() - t_start) > A.budget_ns ||
+                                   (long long)A.ws.stats[0] > A.max_arcs))) {
             A.ws.stats[8 + ((iter + 1) & 1)] = 1;
         }
         if (!grid_sync(A)) return;
+        if (__ldcg(A.ws.stats + 11 + (iter & 1))) {
+            // level L was left part way (its arcs are all in the evaluated
+            // count and L in the cleanup list): the one-CTA sweep hands it
+            // over whole, the grid sweep stops for the dense finish, which
+            // counts from level L + 1 (stats[13])
+            if (gtid == 0) {
+                A.ws.stats[13] = 1;
+                if (small) A.ws.stats[10] = (unsigned long long)L + 1;
+                else {
+                    A.ws.stats[7] = (unsigned long long)L + 1;
+                    list_pending_from(A, L + 1);
+                }
+            }
+            if (small) {
+                if (e) atomicOr(A.err, e);
+                return;
+            }
+            stopped = true;
+            break;
+        }
     }
     if (stopped) {  // the host finishes densely and cleans the workspace
         if (e) atomicOr(A.err, e);
@@ -359,6 +430,99 @@ __global__ void __launch_bounds__(256) k_dense_diff(int64_t m_plus, T* __restric
 // inside, bflag at the column's last-row arc on the boundary), then the
 // marks, each warp starting from the OR of the row segments above its own.
 constexpr int kMarkWarps = 8;
+
+// Supernodes of at most 32 columns (k + b <= 32: nearly all of a road-like
+// graph's, one to a few rows each) take a thread each, both passes at once.
+// Their arcs are one contiguous range (row p follows row p - 1), walked in
+// order with a bit per column: bit j of `above` = an arc above the current
+// row in column j changed. Target (p, j) is marked when bit j (a side (i, j),
+// i < p) or bit p (a side (i, p)) is set, as in k_dense_mark; after the last
+// row the bits of the boundary columns decide the boundary pairs.
+__global__ void __launch_bounds__(256)
+    k_dense_thread(DevTopo D, SnDev S, const int32_t* __restrict__ items, int64_t nitems,
+                   const uint8_t* __restrict__ chg, uint8_t* __restrict__ dq) {
+    for (int64_t it = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; it < nitems;
+         it += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t sn = items[it];
+        const int32_t s0 = S.s0[sn], k = S.k[sn], b = S.b[sn];
+        const int32_t cols = k + b;  // <= 32 (host-checked)
+        int64_t a = D.first[s0];
+        uint32_t above = 0;
+        for (int32_t p = 0; p < k; p++) {
+            uint32_t row = 0;
+            for (int32_t j = p + 1; j < cols; j++, a++) {
+                if (((above >> j) | (above >> p)) & 1u) dq[a] = 1;
+                if (chg[a]) row |= 1u << j;
+            }
+            above |= row;
+        }
+        if (b > 1) {  // (then k <= 30)
+            const uint32_t B = above >> k;
+            if (!B) continue;
+            const int64_t ro = S.rel_off[sn];
+            for (int32_t q = 1; q < b; q++)
+                for (int32_t p = 0; p < q; p++)
+                    if (((B >> p) | (B >> q)) & 1u) dq[S.rel[ro + (int64_t)p * (2 * b - p - 1) / 2 + (q - p - 1)]] = 1;
+        }
+    }
+}
+
+// Supernodes of at most kWarpTileRows rows and kWarpTileBoundary boundary
+// columns (at the bottom of road-like graphs: tens of millions of them, one
+// to a few rows each) take a warp per tile instead: a lane per column walks
+// the rows, and its boundary pairs, in order, with no block barrier. Longer
+// boundaries keep the block's 8 warps on their pairs.
+constexpr int kWarpTileRows = 32;
+constexpr int kWarpTileBoundary = 256;
+
+__global__ void __launch_bounds__(256, 4)
+    k_dense_cols_warp(DevTopo D, SnDev S, const int2* __restrict__ tiles, int64_t ntiles,
+                      const uint8_t* __restrict__ chg, uint8_t* __restrict__ acol, uint8_t* __restrict__ bflag) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t it = warp; it < ntiles; it += nwarps) {
+        const int2 tl = tiles[it];
+        const int32_t s0 = S.s0[tl.x], k = S.k[tl.x], b = S.b[tl.x];
+        const int32_t j = tl.y * 32 + lane;
+        if (j >= k + b) continue;
+        const int32_t rows = min(j, k);
+        uint8_t r = 0;
+        for (int32_t p = 0; p < rows; p++) r |= chg[D.first[s0 + p] + (j - p - 1)];
+        if (j < k) acol[s0 + j] = r;
+        else bflag[D.first[s0 + k - 1] + (j - k)] = r;
+    }
+}
+
+__global__ void __launch_bounds__(256, 4)
+    k_dense_mark_warp(DevTopo D, SnDev S, const int2* __restrict__ tiles, int64_t ntiles,
+                      const uint8_t* __restrict__ chg, uint8_t* __restrict__ dq, const uint8_t* __restrict__ acol,
+                      const uint8_t* __restrict__ bflag) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t it = warp; it < ntiles; it += nwarps) {
+        const int2 tl = tiles[it];
+        const int32_t s0 = S.s0[tl.x], k = S.k[tl.x], b = S.b[tl.x];
+        const int32_t j = tl.y * 32 + lane;
+        if (j >= k + b) continue;
+        const int32_t rows = min(j, k);
+        uint8_t r = 0;
+        for (int32_t p = 0; p < rows; p++) {
+            const int64_t a = D.first[s0 + p] + (j - p - 1);
+            if (r || (p > 0 && acol[s0 + p])) dq[a] = 1;
+            r |= chg[a];
+        }
+        if (j >= k) {  // boundary pairs (B[p], B[q]), q = j - k, as in k_dense_mark
+            const int32_t q = j - k;
+            const int64_t last = D.first[s0 + k - 1];
+            const uint8_t aq = bflag[last + q];
+            const int64_t ro = S.rel_off[tl.x];
+            for (int32_t p = 0; p < q; p++)
+                if (aq | bflag[last + p]) dq[S.rel[ro + (int64_t)p * (2 * b - p - 1) / 2 + (q - p - 1)]] = 1;
+        }
+    }
+}
 
 __global__ void __launch_bounds__(32 * kMarkWarps)
     k_dense_cols(DevTopo D, SnDev S, const int2* __restrict__ tiles, int64_t ntiles, const uint8_t* __restrict__ chg,
@@ -458,6 +622,7 @@ __global__ void __launch_bounds__(256) k_update_clean(UpdateWorkspace ws, const 
 static void free_workspace(UpdateWorkspace* ws) {
     if (!ws) return;
     cudaFree(ws->tiles);
+    cudaFree(ws->tsn);
     cudaFree(ws->chg);
     cudaFree(ws->dq);
     cudaFree(ws->acol);
@@ -569,14 +734,15 @@ static int reset_workspace(nwcch_topology* t, UpdateWorkspace* ws, cudaStream_t 
 }
 
 // Time the level sweep may take before the update is finished densely: about
-// half a full customization (which runs near 1e11 triangles/s), at least
-// 0.2 ms. NWCCH_UPDATE_MODE=dense or =incremental forces one form.
+// a quarter of a full customization (which runs near 4e11 triangles/s on a
+// GB300), at least 0.2 ms; the autotuner measures a better one per
+// topology. NWCCH_UPDATE_MODE=dense or =incremental forces one form.
 long long sweep_budget_ns(const nwcch_topology* t) {
     const char* mode = getenv("NWCCH_UPDATE_MODE");
     if (mode && !strcmp(mode, "dense")) return 0;
     if (mode && !strcmp(mode, "incremental")) return LLONG_MAX;
     if (t->tune.update_budget_ns > 0) return t->tune.update_budget_ns;
-    return std::max<long long>(200000, (long long)(t->triangles / 200));
+    return std::max<long long>(200000, (long long)(t->triangles / 1600));
 }
 
 template <class T>
@@ -601,16 +767,30 @@ int finish_dense(nwcch_topology* t, UpdateWorkspace* ws, const int32_t* w_dev, T
     // up2 is free after the diff: its first m+ bytes hold the boundary
     // column flags
     uint8_t* bflag = static_cast<uint8_t*>(ws->up2);
-    if (ws->tiles_plan != P) {  // (supernode, 32-column tile) list of this plan
+    if (ws->tiles_plan != P) {  // work items of this plan: supernodes, (supernode, 32-column tile) pairs
         cudaFree(ws->tiles);
+        cudaFree(ws->tsn);
         ws->tiles = nullptr;
+        ws->tsn = nullptr;
         ws->tiles_plan = nullptr;
         std::vector<int32_t> kk(P->nsn), bb(P->nsn);
         NWCCH_CUDA_TRY(cudaMemcpy(kk.data(), P->dev.k, sizeof(int32_t) * P->nsn, cudaMemcpyDeviceToHost));
         NWCCH_CUDA_TRY(cudaMemcpy(bb.data(), P->dev.b, sizeof(int32_t) * P->nsn, cudaMemcpyDeviceToHost));
         std::vector<int2> tl;
+        std::vector<int32_t> th;
         for (int64_t sn = 0; sn < P->nsn; sn++)
-            for (int32_t c = 0; c * 32 < kk[sn] + bb[sn]; c++) tl.push_back(make_int2((int)sn, c));
+            if (kk[sn] + bb[sn] <= 32) th.push_back((int32_t)sn);
+        for (int pass = 0; pass < 2; pass++) {  // small supernodes first
+            for (int64_t sn = 0; sn < P->nsn; sn++)
+                if (kk[sn] + bb[sn] > 32 && (kk[sn] <= kWarpTileRows && bb[sn] <= kWarpTileBoundary) == (pass == 0))
+                    for (int32_t c = 0; c * 32 < kk[sn] + bb[sn]; c++) tl.push_back(make_int2((int)sn, c));
+            if (pass == 0) ws->nsmall = (int64_t)tl.size();
+        }
+        if (cudaMalloc(&ws->tsn, sizeof(int32_t) * std::max<size_t>(1, th.size())) != cudaSuccess)
+            return NWCCH_ERR_NOMEM;
+        if (!th.empty())
+            NWCCH_CUDA_TRY(cudaMemcpy(ws->tsn, th.data(), sizeof(int32_t) * th.size(), cudaMemcpyHostToDevice));
+        ws->ntsn = (int64_t)th.size();
         if (cudaMalloc(&ws->tiles, sizeof(int2) * std::max<size_t>(1, tl.size())) != cudaSuccess)
             return NWCCH_ERR_NOMEM;
         if (!tl.empty())
@@ -619,10 +799,22 @@ int finish_dense(nwcch_topology* t, UpdateWorkspace* ws, const int32_t* w_dev, T
         ws->ntiles = (int64_t)tl.size();
         ws->tiles_plan = P;
     }
-    const unsigned grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>(ws->ntiles, (int64_t)t->sms * 8));
-    k_dense_cols<<<grid, 32 * kMarkWarps, 0, s>>>(t->d, P->dev, ws->tiles, ws->ntiles, ws->chg, ws->acol, bflag);
-    k_dense_mark<<<grid, 32 * kMarkWarps, 0, s>>>(t->d, P->dev, ws->tiles, ws->ntiles, ws->chg, ws->dq, ws->acol,
-                                                  bflag);
+    // the column flags of every supernode before any mark reads them
+    const int64_t nbig = ws->ntiles - ws->nsmall;
+    const int2* big = ws->tiles + ws->nsmall;
+    const unsigned wgrid = (unsigned)std::max<int64_t>(1, std::min<int64_t>((ws->nsmall + 7) / 8, (int64_t)t->sms * 8));
+    const unsigned grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>(nbig, (int64_t)t->sms * 8));
+    if (ws->ntsn)
+        k_dense_thread<<<(unsigned)std::min<int64_t>((ws->ntsn + 255) / 256, (int64_t)t->sms * 16), 256, 0, s>>>(
+            t->d, P->dev, ws->tsn, ws->ntsn, ws->chg, ws->dq);
+    if (ws->nsmall)
+        k_dense_cols_warp<<<wgrid, 256, 0, s>>>(t->d, P->dev, ws->tiles, ws->nsmall, ws->chg, ws->acol, bflag);
+    if (nbig) k_dense_cols<<<grid, 32 * kMarkWarps, 0, s>>>(t->d, P->dev, big, nbig, ws->chg, ws->acol, bflag);
+    if (ws->nsmall)
+        k_dense_mark_warp<<<wgrid, 256, 0, s>>>(t->d, P->dev, ws->tiles, ws->nsmall, ws->chg, ws->dq, ws->acol,
+                                                bflag);
+    if (nbig)
+        k_dense_mark<<<grid, 32 * kMarkWarps, 0, s>>>(t->d, P->dev, big, nbig, ws->chg, ws->dq, ws->acol, bflag);
     k_dense_count<<<grid_for(mp, 256), 256, 0, s>>>(t->d, L, ws->queued, ws->dq, ws->stats);
     k_update_clean<<<t->sms * 4, 256, 0, s>>>(*ws, t->d_level_arc_off, mp, t->levels);
     NWCCH_CUDA_TRY(cudaGetLastError());
@@ -675,11 +867,34 @@ int update(nwcch_topology* t, int32_t* w_dev, T* up_dev, T* dn_dev, const int64_
     A.max_arcs = std::max<int64_t>(4096, t->d.m_plus / 8);
     A.spin_limit = t->tune.update_spin_limit;
     A.barrier_extra = t->tune.test_barrier_extra;
+    A.small_arcs = t->tune.update_small_arcs;
+    A.small_ns = t->tune.update_small_ns;
+    A.resume_level = -1;
+    A.resume_counted = 0;
     void* args[] = {&A};
     const int blocks = sizeof(T) == 4 ? ws->blocks32 : ws->blocks64;
-    NWCCH_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k_update<T>, dim3(blocks), dim3(256), args, 0, s));
     unsigned long long h[kStatWords];
     int herr = 0;
+    bool grid_sweep = true;
+    if (A.budget_ns > 0 && A.small_arcs > 0) {
+        // a small change first sweeps in one CTA, with block barriers; if it
+        // grows past small_arcs evaluated arcs it hands its pending levels
+        // to the grid sweep (stats[10] = the level to resume at, plus one)
+        k_update<T><<<1, 256, 0, s>>>(A);
+        NWCCH_CUDA_TRY(cudaGetLastError());
+        NWCCH_CUDA_TRY(cudaMemcpyAsync(h, ws->stats, sizeof(h), cudaMemcpyDeviceToHost, s));
+        NWCCH_CUDA_TRY(cudaStreamSynchronize(s));
+        grid_sweep = h[10] != 0;
+        if (grid_sweep) {
+            A.resume_level = (int32_t)(h[10] - 1);
+            A.resume_counted = h[13] != 0;
+            // the stop requests, the hand-over words and the part-way flags
+            // (words 8-13) back to zero; the counts stay
+            NWCCH_CUDA_TRY(cudaMemsetAsync(ws->stats + 8, 0, 6 * sizeof(unsigned long long), s));
+        }
+    }
+    if (grid_sweep)
+        NWCCH_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k_update<T>, dim3(blocks), dim3(256), args, 0, s));
     NWCCH_CUDA_TRY(cudaMemcpyAsync(h, ws->stats, sizeof(h), cudaMemcpyDeviceToHost, s));
     NWCCH_CUDA_TRY(cudaMemcpyAsync(&herr, A.err, sizeof(int), cudaMemcpyDeviceToHost, s));
     NWCCH_CUDA_TRY(cudaStreamSynchronize(s));
@@ -693,7 +908,9 @@ int update(nwcch_topology* t, int32_t* w_dev, T* up_dev, T* dn_dev, const int64_
         return rc ? rc : rc2;
     }
     if (h[7]) {  // the sweep stopped at level h[7] - 1: finish densely
-        rc = finish_dense<T>(t, ws, w_dev, up_dev, dn_dev, (int32_t)(h[7] - 1), s);
+        // (from the level above when that level was left part way: its arcs
+        // are counted already)
+        rc = finish_dense<T>(t, ws, w_dev, up_dev, dn_dev, (int32_t)(h[7] - 1) + (h[13] ? 1 : 0), s);
         if (rc) return rc;
         NWCCH_CUDA_TRY(cudaMemcpyAsync(h, ws->stats, sizeof(h), cudaMemcpyDeviceToHost, s));
         NWCCH_CUDA_TRY(cudaStreamSynchronize(s));

@@ -31,7 +31,8 @@ KEYS = {"query_dense_rows": 1, "query_smem_labels_max": 2, "update_budget_ns": 3
         "query_cta_max": 5, "sn_warp_cap": 6, "sn_warp_min_count": 7, "pdl": 8, "query_cta_wide_max": 9,
         "query_cta_dense_rows": 10, "battery_pool": 11, "battery_buffer": 12, "update_dense_min": 13,
         "update_spin_limit": 14, "test_barrier_extra": 15, "query_top_chains": 16, "sn_chain_max_items": 17,
-        "sn_thread_cap": 18, "query_stream_max": 19}
+        "sn_thread_cap": 18, "query_stream_max": 19, "update_small_arcs": 20,
+        "update_small_ns": 21}
 PLAN_KEYS = {"sn_warp_cap", "sn_warp_min_count", "sn_chain_max_items", "sn_thread_cap"}
 
 _lib.register("nwcch_tune_set", [C.c_void_p, C.c_int, C.c_int64])
@@ -231,7 +232,8 @@ def tune_latency(topo: DeviceTopology, metric: Metric, s_rank, t_rank, dense_row
 def tune_update(topo: DeviceTopology, metric: Metric, sizes=(1, 10, 100), factors=(0.25, 0.5, 1.0, 2.0),
                 seed: int = 0, picks_per_size: int = 5) -> dict:
     """Times raise-and-restore update pairs of each size under sweep budgets
-    of `factors` x the default estimate (about half a full customization),
+    of `factors` x the default estimate (about a quarter of a full
+    customization),
     and with the dense finish at once; keeps the budget and the size from
     which updates go dense at once (`update_dense_min`) with the least total
     time over `sizes`. Each size is timed on `picks_per_size` random arc sets
@@ -242,7 +244,7 @@ def tune_update(topo: DeviceTopology, metric: Metric, sizes=(1, 10, 100), factor
     import torch
     rng = np.random.default_rng(seed)
     w0 = metric.w.cpu().numpy().copy()
-    default = max(200_000, topo.triangles // 200)
+    default = max(200_000, topo.triangles // 1600)
     before = {k: get(topo, k) for k in ("update_budget_ns", "update_dense_min")}
     picks = {k: [rng.choice(topo.m, size=k, replace=False) for _ in range(picks_per_size)] for k in sizes}
     raises = {k: [w0[ix].astype(np.int64) + 1 + rng.integers(0, 50, k) for ix in picks[k]] for k in sizes}

@@ -237,42 +237,90 @@ static int64_t find_arc(const int64_t* first, const int32_t* head, int64_t lo, i
     return (a < hi_excl && head[a] == z) ? a : -1;
 }
 
-void orc_update(int64_t n, const int64_t* first, const int32_t* head, int64_t m, const int64_t* e_arc,
-                const int8_t* e_up, int32_t* w, int64_t* up, int64_t* dn, int64_t k, const int64_t* edge_idx,
-                const int32_t* new_w, int64_t* stats, int64_t* changed) {
-    const int64_t mp = first[n];
-    /* python/cch.py:289-347 build_update_index: tails, original arcs per
-     * arc, and (in place of the stored triangle lists) downward lists */
-    int32_t* tail = (int32_t*)malloc((size_t)(mp > 0 ? mp : 1) * sizeof(int32_t));
-    for (int64_t x = 0; x < n; x++)
-        for (int64_t a = first[x]; a < first[x + 1]; a++) tail[a] = (int32_t)x;
-    int64_t* aeoff = (int64_t*)calloc((size_t)mp + 1, sizeof(int64_t));
-    for (int64_t j = 0; j < m; j++)
-        if (e_arc[j] >= 0) aeoff[e_arc[j] + 1]++;
-    for (int64_t a = 0; a < mp; a++) aeoff[a + 1] += aeoff[a];
-    int64_t* aeidx = (int64_t*)malloc((size_t)(aeoff[mp] > 0 ? aeoff[mp] : 1) * sizeof(int64_t));
-    int64_t* fill = (int64_t*)malloc((size_t)(mp > 0 ? mp : 1) * sizeof(int64_t));
-    memcpy(fill, aeoff, (size_t)mp * sizeof(int64_t));
-    for (int64_t j = 0; j < m; j++)
-        if (e_arc[j] >= 0) aeidx[fill[e_arc[j]]++] = j;
-    int64_t* doff = (int64_t*)calloc((size_t)n + 1, sizeof(int64_t));
-    for (int64_t a = 0; a < mp; a++) doff[head[a] + 1]++;
-    for (int64_t v = 0; v < n; v++) doff[v + 1] += doff[v];
-    int64_t* darc = (int64_t*)malloc((size_t)(mp > 0 ? mp : 1) * sizeof(int64_t));
-    int64_t* dfill = (int64_t*)malloc((size_t)(n > 0 ? n : 1) * sizeof(int64_t));
-    memcpy(dfill, doff, (size_t)n * sizeof(int64_t));
-    for (int64_t a = 0; a < mp; a++) darc[dfill[head[a]]++] = a;
-    free(dfill);
-    free(fill);
+/* python/cch.py:289-347 build_update_index, built once per topology as the
+ * reference does (lazily, on the first update_edges): tails, original arcs
+ * per arc, and (in place of the stored triangle lists) downward lists. The
+ * queued set of one update is an epoch stamp per arc, so no call clears it. */
+struct OrcUpdateIndex {
+    int64_t n, m, mp;
+    const int64_t* first;
+    const int32_t* head;
+    const int64_t* e_arc;
+    const int8_t* e_up;
+    int32_t* tail;
+    int64_t *aeoff, *aeidx, *doff, *darc;
+    uint32_t* stamp;
+    uint32_t epoch;
+};
 
+OrcUpdateIndex* orc_update_index(int64_t n, const int64_t* first, const int32_t* head, int64_t m,
+                                 const int64_t* e_arc, const int8_t* e_up) {
+    OrcUpdateIndex* X = (OrcUpdateIndex*)calloc(1, sizeof(OrcUpdateIndex));
+    const int64_t mp = first[n];
+    X->n = n;
+    X->m = m;
+    X->mp = mp;
+    X->first = first;
+    X->head = head;
+    X->e_arc = e_arc;
+    X->e_up = e_up;
+    X->tail = (int32_t*)malloc((size_t)(mp > 0 ? mp : 1) * sizeof(int32_t));
+    for (int64_t x = 0; x < n; x++)
+        for (int64_t a = first[x]; a < first[x + 1]; a++) X->tail[a] = (int32_t)x;
+    X->aeoff = (int64_t*)calloc((size_t)mp + 1, sizeof(int64_t));
+    for (int64_t j = 0; j < m; j++)
+        if (e_arc[j] >= 0) X->aeoff[e_arc[j] + 1]++;
+    for (int64_t a = 0; a < mp; a++) X->aeoff[a + 1] += X->aeoff[a];
+    X->aeidx = (int64_t*)malloc((size_t)(X->aeoff[mp] > 0 ? X->aeoff[mp] : 1) * sizeof(int64_t));
+    int64_t* fill = (int64_t*)malloc((size_t)(mp > 0 ? mp : 1) * sizeof(int64_t));
+    memcpy(fill, X->aeoff, (size_t)mp * sizeof(int64_t));
+    for (int64_t j = 0; j < m; j++)
+        if (e_arc[j] >= 0) X->aeidx[fill[e_arc[j]]++] = j;
+    free(fill);
+    X->doff = (int64_t*)calloc((size_t)n + 1, sizeof(int64_t));
+    for (int64_t a = 0; a < mp; a++) X->doff[head[a] + 1]++;
+    for (int64_t v = 0; v < n; v++) X->doff[v + 1] += X->doff[v];
+    X->darc = (int64_t*)malloc((size_t)(mp > 0 ? mp : 1) * sizeof(int64_t));
+    int64_t* dfill = (int64_t*)malloc((size_t)(n > 0 ? n : 1) * sizeof(int64_t));
+    memcpy(dfill, X->doff, (size_t)n * sizeof(int64_t));
+    for (int64_t a = 0; a < mp; a++) X->darc[dfill[head[a]]++] = a;
+    free(dfill);
+    X->stamp = (uint32_t*)calloc((size_t)mp + 1, sizeof(uint32_t));
+    X->epoch = 0;
+    return X;
+}
+
+void orc_update_index_free(OrcUpdateIndex* X) {
+    if (!X) return;
+    free(X->tail);
+    free(X->aeoff);
+    free(X->aeidx);
+    free(X->doff);
+    free(X->darc);
+    free(X->stamp);
+    free(X);
+}
+
+void orc_update_indexed(OrcUpdateIndex* X, int32_t* w, int64_t* up, int64_t* dn, int64_t k,
+                        const int64_t* edge_idx, const int32_t* new_w, int64_t* stats, int64_t* changed) {
+    const int64_t* first = X->first;
+    const int32_t* head = X->head;
+    const int64_t* e_arc = X->e_arc;
+    const int8_t* e_up = X->e_up;
+    const int32_t* tail = X->tail;
+    if (++X->epoch == 0) { /* stamps wrapped: start over */
+        memset(X->stamp, 0, (size_t)(X->mp + 1) * sizeof(uint32_t));
+        X->epoch = 1;
+    }
+    const uint32_t ep = X->epoch;
+    uint32_t* queued = X->stamp;
     /* python/cch.py:357-371: new weights; touched arcs */
-    unsigned char* queued = (unsigned char*)calloc((size_t)mp + 1, 1);
     Heap h = {0, 0, 0};
     for (int64_t j = 0; j < k; j++) w[edge_idx[j]] = new_w[j];
     for (int64_t j = 0; j < k; j++) {
         const int64_t a = e_arc[edge_idx[j]];
-        if (a >= 0 && !queued[a]) {
-            queued[a] = 1;
+        if (a >= 0 && queued[a] != ep) {
+            queued[a] = ep;
             heap_push(&h, ((int64_t)tail[a] << 32) | a);
         }
     }
@@ -283,8 +331,8 @@ void orc_update(int64_t n, const int64_t* first, const int32_t* head, int64_t m,
         const int64_t c = heap_pop(&h) & 0xffffffffLL;
         evaluated++;
         int64_t nu = ORC_INF, nd = ORC_INF;
-        for (int64_t j = aeoff[c]; j < aeoff[c + 1]; j++) {
-            const int64_t e = aeidx[j];
+        for (int64_t j = X->aeoff[c]; j < X->aeoff[c + 1]; j++) {
+            const int64_t e = X->aeidx[j];
             if (e_up[e]) {
                 if ((int64_t)w[e] < nu) nu = w[e];
             } else if ((int64_t)w[e] < nd) {
@@ -293,8 +341,8 @@ void orc_update(int64_t n, const int64_t* first, const int32_t* head, int64_t m,
         }
         const int64_t y = tail[c];
         const int32_t z = head[c];
-        for (int64_t j = doff[y]; j < doff[y + 1]; j++) {
-            const int64_t a = darc[j];
+        for (int64_t j = X->doff[y]; j < X->doff[y + 1]; j++) {
+            const int64_t a = X->darc[j];
             const int64_t b = find_arc(first, head, a + 1, first[tail[a] + 1], z);
             if (b < 0) continue;
             int64_t v;
@@ -315,8 +363,8 @@ void orc_update(int64_t n, const int64_t* first, const int32_t* head, int64_t m,
             const int32_t v = head[kk];
             const int32_t lo = v < z ? v : z, hi = v < z ? z : v;
             const int64_t c2 = find_arc(first, head, first[lo], first[lo + 1], hi);
-            if (c2 >= 0 && !queued[c2]) {
-                queued[c2] = 1;
+            if (c2 >= 0 && queued[c2] != ep) {
+                queued[c2] = ep;
                 heap_push(&h, ((int64_t)lo << 32) | c2);
             }
         }
@@ -325,12 +373,14 @@ void orc_update(int64_t n, const int64_t* first, const int32_t* head, int64_t m,
     stats[1] = nchanged;
     stats[2] = neg;
     free(h.key);
-    free(queued);
-    free(tail);
-    free(aeoff);
-    free(aeidx);
-    free(doff);
-    free(darc);
+}
+
+void orc_update(int64_t n, const int64_t* first, const int32_t* head, int64_t m, const int64_t* e_arc,
+                const int8_t* e_up, int32_t* w, int64_t* up, int64_t* dn, int64_t k, const int64_t* edge_idx,
+                const int32_t* new_w, int64_t* stats, int64_t* changed) {
+    OrcUpdateIndex* X = orc_update_index(n, first, head, m, e_arc, e_up);
+    orc_update_indexed(X, w, up, dn, k, edge_idx, new_w, stats, changed);
+    orc_update_index_free(X);
 }
 
 /* ------------------------------------------------------------ Bellman-Ford */

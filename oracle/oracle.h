@@ -56,6 +56,17 @@ void orc_update(int64_t n, const int64_t* first, const int32_t* head, int64_t m,
                 const int8_t* e_up, int32_t* w, int64_t* up, int64_t* dn, int64_t k, const int64_t* edge_idx,
                 const int32_t* new_w, int64_t* stats, int64_t* changed);
 
+/* The same update split as the reference splits it: the update index
+ * (python/cch.py:289-347) built once per topology, then any number of
+ * updates on it (python/cch.py:349-402). The index keeps the topology's
+ * pointers, which must outlive it. */
+typedef struct OrcUpdateIndex OrcUpdateIndex;
+OrcUpdateIndex* orc_update_index(int64_t n, const int64_t* first, const int32_t* head, int64_t m,
+                                 const int64_t* e_arc, const int8_t* e_up);
+void orc_update_indexed(OrcUpdateIndex* X, int32_t* w, int64_t* up, int64_t* dn, int64_t k,
+                        const int64_t* edge_idx, const int32_t* new_w, int64_t* stats, int64_t* changed);
+void orc_update_index_free(OrcUpdateIndex* X);
+
 /* python/search.py:8-29 (queue-based Bellman-Ford) on the original graph,
  * single source, original vertex ids. Returns 1 if a negative cycle is
  * reachable from s (a vertex relaxed n times), else 0; dist int64[n]. */

@@ -48,6 +48,12 @@ def lib():
             L.orc_query_batch.restype = None
             L.orc_update.argtypes = [I64, P, P, I64, P, P, P, P, P, I64, P, P, P, P]
             L.orc_update.restype = None
+            L.orc_update_index.argtypes = [I64, P, P, I64, P, P]
+            L.orc_update_index.restype = P
+            L.orc_update_indexed.argtypes = [P, P, P, P, I64, P, P, P, P]
+            L.orc_update_indexed.restype = None
+            L.orc_update_index_free.argtypes = [P]
+            L.orc_update_index_free.restype = None
             L.orc_bellman_ford.argtypes = [I64, P, P, P, I64, P]
             L.orc_bellman_ford.restype = C.c_int
             L.orc_has_negative_cycle.argtypes = [I64, P, P, P]
@@ -152,6 +158,38 @@ def update(T: Topo, w, up, dn, edge_idx, new_w):
     lib().orc_update(T.n, _p(T.first), _p(T.head), T.m, _p(T.e_arc), _p(T.e_up), _p(w), _p(up), _p(dn),
                      edge_idx.size, _p(edge_idx), _p(new_w), _p(stats), _p(changed))
     return int(stats[0]), changed[:stats[1]].copy(), int(stats[2])
+
+
+class UpdateIndex:
+    """The reference's update index (python/cch.py:289-347), built once per
+    topology, and updates on it (python/cch.py:349-402): `update` has the
+    module-level update's arguments and results, without the index build in
+    every call (the reference builds it lazily, once)."""
+
+    def __init__(self, T: Topo):
+        self.T = T  # the index points into T's arrays
+        self._h = lib().orc_update_index(T.n, _p(T.first), _p(T.head), T.m, _p(T.e_arc), _p(T.e_up))
+        self._changed = np.empty(max(T.m_plus, 1), np.int64)
+
+    def update(self, w, up, dn, edge_idx, new_w):
+        assert self._h, "index freed"
+        assert w.dtype == np.int32 and up.dtype == np.int64 and dn.dtype == np.int64
+        edge_idx, new_w = _c(edge_idx, np.int64), _c(new_w, np.int32)
+        stats = np.zeros(3, np.int64)
+        lib().orc_update_indexed(self._h, _p(w), _p(up), _p(dn), edge_idx.size, _p(edge_idx), _p(new_w),
+                                 _p(stats), _p(self._changed))
+        return int(stats[0]), self._changed[:stats[1]].copy(), int(stats[2])
+
+    def close(self):
+        if self._h:
+            lib().orc_update_index_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def bellman_ford(n, off, tgt, w, s):

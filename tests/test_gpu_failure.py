@@ -38,6 +38,7 @@ def test_update_barrier_timeout_is_reported_and_recovered(gpu, oracle, storage):
     idx = rng.choice(w.size, size=50, replace=False)
     val = (w[idx] + rng.integers(1, 100, size=idx.size)).astype(np.int32)
 
+    tune.set(T, "update_small_arcs", 0)  # the grid sweep from the first level (its barriers are the test)
     tune.set(T, "update_spin_limit", 20_000)  # about 2 ms of 100 ns sleeps per wait
     tune.set(T, "test_barrier_extra", 1)
     t0 = time.perf_counter()

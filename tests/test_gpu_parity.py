@@ -500,3 +500,42 @@ def test_edge_arcs_device(gpu):
     g, top = _seeded("road", 80_000, seed=21)
     ea, eu = TT.edge_arcs_device(g["n"], g["off"], g["tgt"], top["rank"], top["first"], top["head"])
     assert np.array_equal(ea.cpu().numpy(), top["e_arc"]) and np.array_equal(eu.cpu().numpy(), top["e_up"])
+
+
+@pytest.mark.parametrize("small_arcs,small_ns,budget_ns", [
+    (0, 300_000, None), (12, 300_000, None), (1 << 20, 300_000, None),
+    # out of time inside a level: the one-CTA sweep hands the level over
+    # part way (1 ns: before its first arc), the grid sweep stops part way
+    # into the dense finish (1 ns, 20 us), or both in turn
+    (1 << 20, 1, None), (0, 300_000, 1), (0, 300_000, 20_000), (1 << 20, 1, 1)])
+def test_update_one_cta_sweep_and_hand_over(gpu, oracle, small_arcs, small_ns, budget_ns, monkeypatch):
+    """Partial updates that sweep in one CTA, hand over to the grid sweep
+    after a few evaluated arcs or part way through a level, use the grid
+    sweep from the start, or stop part way through a level for the dense
+    finish: the evaluated count, changed set and values equal the oracle's
+    update (python/cch.py:349-402 restated) in every case."""
+    if budget_ns is None:
+        monkeypatch.setenv("NWCCH_UPDATE_MODE", "incremental")
+    from nwcch import tune
+    from nwcch.device import DeviceTopology
+    g, top = _seeded("road", 40_000, seed=33)
+    T = DeviceTopology.from_dict(top)
+    OT = oracle.Topo.from_dict(top)
+    oup, odn = oracle.customize(OT, g["w"])
+    m = T.customize(g["w"], "int32")
+    tune.set(T, "update_small_arcs", small_arcs)
+    tune.set(T, "update_small_ns", small_ns)
+    if budget_ns is not None:
+        tune.set(T, "update_budget_ns", budget_ns)
+        tune.set(T, "update_dense_min", 0)
+    rng = np.random.default_rng(17)
+    w = g["w"].copy()
+    for k in (1, 3, 40, 300):
+        idx = rng.choice(w.size, size=k, replace=False)
+        val = (w[idx] + rng.integers(1, 200, size=k)).astype(np.int32)
+        ev = T.update(m, idx, val)
+        oev, och, _ = oracle.update(OT, w, oup, odn, idx, val)
+        assert ev == oev, (small_arcs, small_ns, budget_ns, k)
+        assert np.array_equal(np.sort(m.last_changed.cpu().numpy().astype(np.int64)), np.sort(och))
+        up, dn = m.to_numpy()
+        assert np.array_equal(up, oup) and np.array_equal(dn, odn), (small_arcs, small_ns, budget_ns, k)

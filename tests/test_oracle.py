@@ -80,6 +80,28 @@ def test_family_updates(oracle, i):
     assert np.array_equal(up, i32_to_i64(c["final_up"])) and np.array_equal(dn, i32_to_i64(c["final_dn"]))
 
 
+@pytest.mark.parametrize("i", [0, 4, 8, 11])
+def test_family_updates_on_one_index(oracle, i):
+    """The index built once (as the reference builds it) serves every step:
+    the same counts, changed sets and values as the recorded updates."""
+    c = family_case(load_golden("family.npz"), i)
+    T = topo(oracle, c)
+    w = np.array(c["w"], np.int32)
+    up, dn = oracle.customize(T, w)
+    X = oracle.UpdateIndex(T)
+    for st in c["step_list"]:
+        ev, changed, neg = X.update(w, up, dn, st["idx"], st["val"])
+        assert ev == int(st["evaluated"])
+        assert np.array_equal(np.sort(changed), st["changed"])
+        assert np.array_equal(up[st["changed"]], i32_to_i64(st["up"]))
+        assert np.array_equal(dn[st["changed"]], i32_to_i64(st["dn"]))
+        assert (neg > 0) == bool(st["created"])
+    X.update(w, up, dn, [int(c["negcycle_edge"])], [int(c["negcycle_w"])])
+    X.update(w, up, dn, [int(c["negcycle_edge"])], [int(c["negcycle_restore_w"])])
+    X.close()
+    assert np.array_equal(up, i32_to_i64(c["final_up"])) and np.array_equal(dn, i32_to_i64(c["final_dn"]))
+
+
 def test_grid64(oracle):
     z = load_golden("grid64.npz")
     T = topo(oracle, z)
