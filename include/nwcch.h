@@ -226,6 +226,11 @@ int nwcch_check(nwcch_topology* t, void* stream);
  * the level is finished by the grid sweep (or the dense finish, for the grid
  * sweep's own budget, NWCCH_TUNE_UPDATE_BUDGET_NS), counted once. */
 #define NWCCH_TUNE_UPDATE_SMALL_NS 21
+/* The streaming query kernel's shared-memory data ring, in KB (0: as large as
+ * the labels leave, at most 192; default 0). Smaller rings hold fewer rows
+ * per copied item; a topology whose longest row does not fit a third of the
+ * ring goes to the other query forms. */
+#define NWCCH_TUNE_QUERY_STREAM_RING_KB 22
 int nwcch_tune_set(nwcch_topology* t, int key, int64_t value);
 int nwcch_tune_get(const nwcch_topology* t, int key, int64_t* value);
 

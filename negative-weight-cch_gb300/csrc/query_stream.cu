@@ -41,8 +41,8 @@ namespace {
 constexpr int QS_CONSUMERS = 256;                   // consumer threads (8 warps)
 constexpr int QS_THREADS = QS_CONSUMERS + 32;       // + the producer warp
 constexpr int QS_ITEMS = 32;                        // items in flight at most (descriptor ring)
-constexpr int QS_DATA_WORDS = 36864;                // 144 KB data ring
-constexpr int QS_ITEM_WORDS = 12288;                // one item: at most 48 KB
+constexpr int QS_RING_MAX_WORDS = 49152;            // data ring: at most 192 KB, as much as the labels leave
+                                                    // (one item: at most a third of the ring)
 constexpr long long QS_SPIN = 1 << 22;              // polls of one bounded wait (~0.2-1 s)
 
 enum QsItem : int { QS_ROWS = 0, QS_BOUNDARY = 1, QS_END = 2 };
@@ -129,16 +129,18 @@ __global__ void __launch_bounds__(QS_THREADS, 1)
     k_qstream(DevTopo D, const QsNode* __restrict__ nodes, const int32_t* __restrict__ sn_id,
               const int32_t* __restrict__ up, const int32_t* __restrict__ dn, const int32_t* __restrict__ s_rank,
               const int32_t* __restrict__ t_rank, int64_t nq, int64_t* __restrict__ dist, int32_t thr,
-              int32_t* __restrict__ scratch, int32_t* __restrict__ wide, int* __restrict__ err) {
+              int32_t* __restrict__ scratch, int32_t* __restrict__ wide, int* __restrict__ err, int32_t ring_words,
+              int32_t item_words) {
     extern __shared__ __align__(128) unsigned char qs_smem[];
     const int64_t Dp = D.max_depth + 1;
-    int32_t* ring = reinterpret_cast<int32_t*>(qs_smem);  // QS_DATA_WORDS
-    int32_t* L = ring + QS_DATA_WORDS;                     // [Dp] labels by chain position
+    int32_t* ring = reinterpret_cast<int32_t*>(qs_smem);  // [ring_words] data ring
+    int32_t* L = ring + ring_words;                        // [Dp] labels by chain position
     int32_t* bpos = L + ((Dp + 3) & ~3LL);                 // boundary positions of the current supernode
     __shared__ __align__(8) uint64_t full[QS_ITEMS], empty[QS_ITEMS];
     __shared__ QsHeader hdr[QS_ITEMS];
     __shared__ int32_t clab[32];
-    __shared__ int abort_flag, go, second, wide_any;
+    __shared__ int abort_flag, second, wide_any;
+    __shared__ int go[2];  // by item parity: read after an item's barrier, written before the next one's
     __shared__ int32_t red[QS_THREADS / 32];
 
     const int64_t c = blockIdx.x;  // chain: query c >> 1, direction c & 1
@@ -194,12 +196,12 @@ __global__ void __launch_bounds__(QS_THREADS, 1)
             auto take = [&](int64_t words, int& slot, int32_t*& dst, int32_t& off) -> bool {
                 while (g - rel >= QS_ITEMS)
                     if (!release_one()) return false;
-                int64_t pos = head % QS_DATA_WORDS;
-                if (pos + words > QS_DATA_WORDS) {  // no wrap inside an item: skip to the ring's start
-                    head += QS_DATA_WORDS - pos;
+                int64_t pos = head % ring_words;
+                if (pos + words > ring_words) {  // no wrap inside an item: skip to the ring's start
+                    head += ring_words - pos;
                     pos = 0;
                 }
-                while (head + words - tail > QS_DATA_WORDS)
+                while (head + words - tail > ring_words)
                     if (!release_one()) return false;
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                 slot = (int)(g % QS_ITEMS);
@@ -241,8 +243,8 @@ __global__ void __launch_bounds__(QS_THREADS, 1)
                     auto words = [&](int32_t nn) {
                         return (int64_t)nn * (cols - c0 - 1) - (int64_t)nn * (nn - 1) / 2;
                     };
-                    while (n > 1 && words(n) + 8 > QS_ITEM_WORDS) n--;
-                    if (words(n) + 8 > QS_ITEM_WORDS) {  // a row longer than an item: the host excludes this
+                    while (n > 1 && words(n) + 8 > item_words) n--;
+                    if (words(n) + 8 > item_words) {  // a row longer than an item: the host excludes this
                         e |= ERR_CAPACITY;
                         ok = false;
                         break;
@@ -297,10 +299,13 @@ __global__ void __launch_bounds__(QS_THREADS, 1)
                     e |= ERR_TIMEOUT;
                     atomicExch(&abort_flag, 1);
                 }
-                go = ready ? 1 : 0;  // one decision for all consumers
+                go[g & 1] = ready ? 1 : 0;  // one decision for all consumers
             }
             consumers_sync();
-            if (!go) break;
+            // every consumer is done with item g - 1 (this barrier is its
+            // end): its slot goes back to the producer
+            if (g > 0 && tid == 0) mbar_arrive(&empty[(g - 1) % QS_ITEMS]);
+            if (!go[g & 1]) break;
             if (tid != 0 && !mbar_test(&full[slot], parity)) mbar_wait(&full[slot], parity);  // acquire per thread
             const QsHeader h = hdr[slot];
             if (h.type == QS_END) break;
@@ -355,8 +360,6 @@ __global__ void __launch_bounds__(QS_THREADS, 1)
                     }
                 }
             }
-            consumers_sync();
-            if (tid == 0) mbar_arrive(&empty[slot]);
         }
         if (hi > thr || lo < -thr) atomicOr(&wide_any, 1);
     }
@@ -417,10 +420,18 @@ int query_stream_async(nwcch_topology* t, const int32_t* up, const int32_t* dn, 
     auto* P = static_cast<SnPlan*>(t->sn_plan);
     if (!P || !P->d_qnodes || nq < 1 || nq > t->tune.query_stream_max) return NWCCH_OK;
     if (((uintptr_t)up | (uintptr_t)dn | (uintptr_t)t->d.hdep) & 15) return NWCCH_OK;  // bulk copies: 16-byte bases
-    if ((int64_t)t->max_deg + 8 > QS_ITEM_WORDS || (int64_t)P->max_b + 8 > QS_ITEM_WORDS) return NWCCH_OK;
     const int64_t Dp = t->d.max_depth + 1;
-    const size_t smem = (size_t)QS_DATA_WORDS * 4 + (size_t)((Dp + 3) & ~3LL) * 4 + (size_t)P->max_b * 4;
-    if (smem + 4096 > 227 * 1024) return NWCCH_OK;
+    // the data ring takes what the labels and boundary positions leave of
+    // the CTA's shared memory (4 KB kept for the static part), at most 192 KB
+    // or the tuned size; an item holds at most a third of it
+    const int64_t fixed = ((Dp + 3) & ~3LL) * 4 + (int64_t)P->max_b * 4;
+    int64_t ring_words = t->tune.query_stream_ring_kb > 0 ? t->tune.query_stream_ring_kb * 256 : QS_RING_MAX_WORDS;
+    ring_words = std::min<int64_t>(ring_words, (227 * 1024 - 4096 - fixed) / 4);
+    ring_words = ring_words / 12 * 12;
+    const int64_t item_words = ring_words / 3;  // a multiple of 4
+    if (item_words < 16 || (int64_t)t->max_deg + 8 > item_words || (int64_t)P->max_b + 8 > item_words)
+        return NWCCH_OK;
+    const size_t smem = (size_t)(ring_words * 4 + fixed);
     NWCCH_CUDA_TRY(allow_dynamic_smem((const void*)k_qstream, smem));
     // scratch: per query labels and vertices by depth and a counter, then a
     // flag per query
@@ -435,7 +446,7 @@ int query_stream_async(nwcch_topology* t, const int32_t* up, const int32_t* dn, 
     if (!rc) {
         k_qstream<<<(unsigned)(2 * nq), QS_THREADS, smem, s>>>(t->d, P->d_qnodes, P->dev.sn_id, up, dn, s_rank,
                                                                 t_rank, nq, dist, thr, static_cast<int32_t*>(scratch),
-                                                                wide, err);
+                                                                wide, err, (int32_t)ring_words, (int32_t)item_words);
         if (cudaGetLastError() != cudaSuccess) rc = NWCCH_ERR_CUDA;
     }
     if (!rc) rc = query_sn64_flagged(t, up, dn, s_rank, t_rank, nq, dist, wide, err, s);

@@ -327,6 +327,10 @@ extern "C" int nwcch_tune_set(nwcch_topology* t, int key, int64_t value) {
             if (value < 1) return NWCCH_ERR_ARG;
             t->tune.update_small_ns = value;
             return NWCCH_OK;
+        case NWCCH_TUNE_QUERY_STREAM_RING_KB:
+            if (value < 0 || value > 227) return NWCCH_ERR_ARG;
+            t->tune.query_stream_ring_kb = value;
+            return NWCCH_OK;
         case NWCCH_TUNE_TEST_BARRIER_EXTRA:
             if (value < 0 || value > 1024) return NWCCH_ERR_ARG;
             t->tune.test_barrier_extra = (int32_t)value;
@@ -368,6 +372,7 @@ extern "C" int nwcch_tune_get(const nwcch_topology* t, int key, int64_t* value) 
         case NWCCH_TUNE_QUERY_STREAM_MAX: *value = t->tune.query_stream_max; return NWCCH_OK;
         case NWCCH_TUNE_UPDATE_SMALL_ARCS: *value = t->tune.update_small_arcs; return NWCCH_OK;
         case NWCCH_TUNE_UPDATE_SMALL_NS: *value = t->tune.update_small_ns; return NWCCH_OK;
+        case NWCCH_TUNE_QUERY_STREAM_RING_KB: *value = t->tune.query_stream_ring_kb; return NWCCH_OK;
         case NWCCH_TUNE_BATTERY_POOL: *value = t->tune.battery_pool; return NWCCH_OK;
         case NWCCH_TUNE_BATTERY_BUFFER: *value = t->tune.battery_buffer; return NWCCH_OK;
         case NWCCH_TUNE_SN_WARP_CAP:

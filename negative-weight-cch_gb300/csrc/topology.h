@@ -41,6 +41,7 @@ struct Tuning {
     int64_t query_cta_max = 0;              // batches up to this many queries: a CTA per query (8 per SM)
     int64_t query_cta_wide_max = 0;         // ... of 16 warps up to this many (one per SM), else of 8
     int64_t query_stream_max = 64;          // batches up to this many queries: the streaming kernel (a CTA a chain)
+    int64_t query_stream_ring_kb = 0;       // its data ring (KB; 0: as large as fits, at most 192)
     int64_t update_small_arcs = 8192;       // updates sweep in one CTA until they evaluate this many arcs (0: never)
     int64_t update_small_ns = 300000;       // ... or until they have run this long (ns)
     int32_t query_cta_dense_rows = 1;       // the CTA form's row-by-row threshold

@@ -32,7 +32,7 @@ KEYS = {"query_dense_rows": 1, "query_smem_labels_max": 2, "update_budget_ns": 3
         "query_cta_dense_rows": 10, "battery_pool": 11, "battery_buffer": 12, "update_dense_min": 13,
         "update_spin_limit": 14, "test_barrier_extra": 15, "query_top_chains": 16, "sn_chain_max_items": 17,
         "sn_thread_cap": 18, "query_stream_max": 19, "update_small_arcs": 20,
-        "update_small_ns": 21}
+        "update_small_ns": 21, "query_stream_ring_kb": 22}
 PLAN_KEYS = {"sn_warp_cap", "sn_warp_min_count", "sn_chain_max_items", "sn_thread_cap"}
 
 _lib.register("nwcch_tune_set", [C.c_void_p, C.c_int, C.c_int64])

@@ -50,6 +50,31 @@ def test_stream_equals_oracle(gpu, oracle, kind, n):
     assert not T.check()
 
 
+@pytest.mark.parametrize("ring_kb", [12, 48, 144, 0])
+def test_stream_ring_sizes(gpu, oracle, ring_kb):
+    """Smaller data rings hold fewer rows per item and wrap more often (the
+    producer waits for released slots far more): the answers stay the
+    oracle's. 0 is the default (as large as fits, at most 192 KB)."""
+    from nwcch import graphs as G
+    from nwcch import tune
+    from nwcch.device import DeviceTopology
+    g, top = _graph("road", 80_000, seed=47)
+    T = DeviceTopology.from_dict(top)
+    OT = oracle.Topo.from_dict(top)
+    oup, odn = oracle.customize(OT, g["w"])
+    s, t = G.random_pairs(g["n"], 64, seed=9)
+    s, t = top["rank"][s].copy(), top["rank"][t].copy()
+    want = oracle.query_batch(OT, oup, odn, s, t)
+    m = T.customize(g["w"], "int32")
+    tune.set(T, "query_stream_ring_kb", ring_kb)
+    assert int(np.diff(top["first"]).max()) + 8 <= ring_kb * 256 // 3 or ring_kb == 0  # the kernel takes it
+    for i in range(16):
+        assert int(T.query_batch(m, s[i:i + 1], t[i:i + 1]).cpu().numpy()[0]) == want[i], (ring_kb, i)
+        assert T.last_query_launches() == 2  # k_qstream and the (idle) 64-bit pass
+    assert np.array_equal(T.query_batch(m, s, t).cpu().numpy(), want)
+    assert not T.check()
+
+
 def test_stream_on_a_forest_and_wide_values(gpu, oracle):
     from nwcch.device import DeviceTopology
     z = load_golden("techniques.npz")
