@@ -146,9 +146,14 @@ def _time(torch, fn, reps: int) -> float:
 
 
 def tune_queries(topo: DeviceTopology, metric: Metric, s_rank, t_rank, reps: int = 3,
-                 dense_rows=(1, 8, 16, 24, 33), occupancy=(1, 2, 3), labels=("auto", "global", "shared")) -> dict:
+                 dense_rows=(1, 8, 16, 24, 33), occupancy=(1, 2, 3), labels=("auto", "global", "shared"),
+                 top_chains=(16, 32, 64, 128, 256)) -> dict:
     """Times every candidate schedule on the batch (s_rank, t_rank) and keeps
-    the fastest. Returns {"best": {...}, "ms": best time, "trials": [...]}."""
+    the fastest: the per-chain kernel's schedule, then the form (a warp or a
+    CTA per query, or the tile pipeline of the top supernodes for large
+    batches), then, when the tile pipeline answers the batch, the size of its
+    top set (the supernodes crossed by about `top_chains` chains of a pass).
+    Returns {"best": {...}, "ms": best time, "trials": [...]}."""
     import torch
     s = torch.as_tensor(np.asarray(s_rank, np.int32)).cuda()
     t = torch.as_tensor(np.asarray(t_rank, np.int32)).cuda()
@@ -191,8 +196,26 @@ def tune_queries(topo: DeviceTopology, metric: Metric, s_rank, t_rank, reps: int
                        "ms": round(forms[form], 4)})
     form = min(forms, key=forms.get)
     set(topo, "query_cta_max", max(cta_before, nq) if form == "cta" else min(cta_before, nq - 1))
-    return {"best": {**{k: best[k] for k in ("query_dense_rows", "query_occupancy", "labels")}, "form": form},
-            "ms": round(min(forms.values()), 4), "trials": trials}
+    chosen = {**{k: best[k] for k in ("query_dense_rows", "query_occupancy", "labels")}, "form": form}
+    ms = min(forms.values())
+    if form == "warp" and nq > get(topo, "query_cta_max") and top_chains:
+        tc_before = get(topo, "query_top_chains")
+        tops = {}
+        try:
+            for tc in top_chains:
+                set(topo, "query_top_chains", tc)
+                tops[tc] = _time(torch, lambda: topo.query_batch(metric, s, t, out=out), reps)
+                if not torch.equal(ref, out):
+                    raise AssertionError(f"a top set of {tc} chains changed the answers")
+                trials.append({"query_top_chains": tc, "ms": round(tops[tc], 4)})
+        except BaseException:
+            set(topo, "query_top_chains", tc_before)
+            raise
+        tc = min(tops, key=tops.get)
+        set(topo, "query_top_chains", tc)
+        chosen["query_top_chains"] = tc
+        ms = tops[tc]
+    return {"best": chosen, "ms": round(ms, 4), "trials": trials}
 
 
 def tune_latency(topo: DeviceTopology, metric: Metric, s_rank, t_rank, dense_rows=(1, 8, 33), wide=(0, 1)) -> dict:

@@ -404,8 +404,12 @@ def test_autotuner_keeps_answers(gpu, oracle, kind, n):
     s, t = G.random_pairs(g["n"], 2000, seed=12)
     s, t = top["rank"][s], top["rank"][t]
     r = tune.tune_queries(T, m, s, t, reps=1)
-    assert len(r["trials"]) == 5 * 3 * 3 + 2  # schedules, then the two forms
+    # schedules, the two forms, then the top set sizes when the tile pipeline won
+    tops = 5 if r["best"]["form"] == "warp" else 0
+    assert len(r["trials"]) == 5 * 3 * 3 + 2 + tops
     assert tune.get(T, "query_dense_rows") == r["best"]["query_dense_rows"]
+    if tops:
+        assert tune.get(T, "query_top_chains") == r["best"]["query_top_chains"]
     assert np.array_equal(T.query_batch(m, s, t).cpu().numpy(), oracle.query_batch(OT, oup, odn, s, t))
     rl = tune.tune_latency(T, m, s[:6], t[:6])
     assert len(rl["trials"]) == 6
