@@ -102,6 +102,40 @@ def test_family_updates_on_one_index(oracle, i):
     assert np.array_equal(up, i32_to_i64(c["final_up"])) and np.array_equal(dn, i32_to_i64(c["final_dn"]))
 
 
+def test_kept_index_equals_index_per_call(oracle):
+    """The kept update index (the CPU baseline of the bench's update timings)
+    and the index built per call give the same counts, changed sets and
+    values over a run of random raises and drops, including a change to an
+    arc that the previous call changed (its queued stamp must not leak)."""
+    from nwcch import graphs as G
+    from nwcch import topology as TT
+    g = G.road_like(6000, seed=8)
+    top = TT.build_topology(g)
+    T = oracle.Topo.from_dict(top)
+    w1 = g["w"].astype(np.int32).copy()
+    w2 = w1.copy()
+    u1, d1 = oracle.customize(T, w1)
+    u2, d2 = u1.copy(), d1.copy()
+    X = oracle.UpdateIndex(T)
+    rng = np.random.default_rng(3)
+    last = None
+    for step in range(12):
+        k = int(rng.choice([1, 3, 20, 150]))
+        idx = rng.choice(w1.size, size=k, replace=False)
+        if last is not None:
+            idx[0] = last
+        val = (w1[idx].astype(np.int64) + rng.integers(-5, 60, size=k)).clip(1, 10**6).astype(np.int32)
+        r1 = oracle.update(T, w1, u1, d1, idx, val)
+        r2 = X.update(w2, u2, d2, idx, val)
+        assert r1[0] == r2[0] and r1[2] == r2[2], step
+        assert np.array_equal(np.sort(r1[1]), np.sort(r2[1])), step
+        assert np.array_equal(u1, u2) and np.array_equal(d1, d2), step
+        last = int(idx[-1])
+    X.close()
+    fu, fd = oracle.customize(T, w1)
+    assert np.array_equal(fu, u1) and np.array_equal(fd, d1)
+
+
 def test_grid64(oracle):
     z = load_golden("grid64.npz")
     T = topo(oracle, z)
