@@ -1133,7 +1133,7 @@ def main():
                      "launch": "one customization: CUDA graph of k_base_gather, k_sn_thread, k_sn_warp, k_sn_panel, "
                                "k_sn_tile"},
         "cpu_baseline": {"value": round(cb["value"], 3), "unit": "ms", "cores": cb["cores"], "kind": "port",
-                         "sample": f"{cb['runs']} level-parallel customizations (cpp/cch.cpp:468-529) + scans "
+                         "sample": f"{cb['runs']} x level-parallel customization (cpp/cch.cpp:468-529) + scan "
                                    f"of the same metric"},
         "parity": parity,
         "clocks": R["clocks"],
