@@ -18,6 +18,19 @@ def test_every_declared_symbol_is_exported(built_lib):
     assert not missing, missing
 
 
+def test_tuning_keys_match_the_header():
+    """nwcch.tune's key names and numbers are the header's NWCCH_TUNE_*
+    defines, one for one (a key added on one side only would set the wrong
+    schedule or fail at run time)."""
+    from nwcch import tune
+    header = (ROOT / "include" / "nwcch.h").read_text()
+    defined = {m.group(1).lower(): int(m.group(2))
+               for m in re.finditer(r"#define NWCCH_TUNE_([A-Z0-9_]+)\s+(\d+)", header)}
+    assert defined == tune.KEYS
+    assert len(set(defined.values())) == len(defined)  # no number used twice
+    assert tune.PLAN_KEYS <= set(defined)
+
+
 def test_library_is_cuda_sm103a_build():
     import build as nwbuild
     assert "arch=compute_103a,code=sm_103a" in " ".join(nwbuild.NVCC_FLAGS)
