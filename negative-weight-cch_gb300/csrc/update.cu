@@ -10,24 +10,31 @@
 // lower level, so evaluating one level at a time, lowest first, sees the same
 // final lower values and queues the same set of arcs.
 //
-// One cooperative launch runs the whole update: its blocks are co-resident,
-// and a level ends with a grid barrier whose spin is bounded (on timeout the
-// kernel records ERR_TIMEOUT and every block returns; the host then resets
-// the workspace and reports NWCCH_ERR_TIMEOUT). The kernel cleans its
-// workspace (queued flags, bucket counts, pending bits) before it exits.
+// A change first sweeps in one CTA: its levels end at a block barrier, which
+// is what most single-arc changes need (a few hundred arcs over some dozens
+// of levels). When that sweep has evaluated `update_small_arcs` arcs or run
+// `update_small_ns`, it hands its pending levels to one cooperative launch
+// over the whole grid: its blocks are co-resident, and a level ends with a
+// grid barrier whose spin is bounded (on timeout the kernel records
+// ERR_TIMEOUT and every block returns; the host then resets the workspace
+// and reports NWCCH_ERR_TIMEOUT). The kernel cleans its workspace (queued
+// flags, bucket counts, pending bits) before it exits.
 //
 // The level sweep pays a barrier per level and a row search per lower
 // triangle, so a change that spreads through the top separators costs more
-// than customizing from scratch. The sweep therefore runs under a budget
-// (about half the time of a full customization): past it, the sweep stops at
-// its next pending level L and the update is finished densely with the same
-// results and statistics: the whole metric is re-customized into scratch by
-// the supernodal kernels, the arcs whose values differ are the changed ones,
-// and an arc of level >= L counts as evaluated if it was queued before the
-// stop or one of its lower triangles has a changed side (the set the sweep
-// would have queued). Lower triangles are found through the supernode
-// layout: a triangle inside a supernode through its trapezoid columns, one
-// below it through the boundary pairs of a descendant supernode.
+// than customizing from scratch. The grid sweep therefore runs under a
+// budget (about a quarter of a full customization's time, or the tuned
+// value): past it, the sweep stops before its next arc, inside a level if
+// need be, and the update is finished densely with the same results and
+// statistics: the whole metric is re-customized into scratch by the
+// supernodal kernels, the arcs whose values differ are the changed ones, and
+// an arc above the stop counts as evaluated if it was queued before the stop
+// or one of its lower triangles has a changed side (the set the sweep would
+// have queued). Lower triangles are found through the supernode layout: a
+// triangle inside a supernode through its trapezoid columns, one below it
+// through the boundary pairs of a descendant supernode. A level left part
+// way is counted once, whole, when it starts (the one-CTA sweep hands it over
+// whole; the dense count starts at the level above it).
 
 #include <algorithm>
 #include <climits>
